@@ -1,0 +1,123 @@
+/*
+ * tp3.h -- C ABI of the GB300 c3 + Bayes scorer (libtp3.so).
+ *
+ * One hot path of ThreePhotons.jl: spherical-harmonic intensity coefficients of
+ * K shells up to order L  ->  model three-photon correlation c3(k1,k2,k3,alpha,beta)
+ *  ->  "Bayes" log-likelihood against a triplet histogram.
+ *
+ * Reference interfaces replaced (file:line inside ThreePhotons.jl):
+ *   src/cuda.jl:10-22        CUDA_init                      -> tp3_ctx_create (device side)
+ *   src/cuda.jl:45-69        CUDA_store_basis / CUDA_calculate_basis,
+ *   src/correlations.jl:87-153 calculate_basis              -> tp3_ctx_create (tables)
+ *   src/cuda.jl:74-108       FullCorrelation_parallized(::BasisTypeCuda) -> tp3_c3
+ *   src/correlations.jl:179-193 FullCorrelation_parallized(::BasisType)  -> tp3_c3
+ *   src/correlations.jl:201-226 energy(..., "Bayes")         -> tp3_energy, tp3_energy_batch
+ *   src/cuda_kernel.cu:18    calculate_coefficient_matrix (PTX entry bound by
+ *                            cudacall at src/cuda.jl:82-86) + cublasSgemm_v2 at
+ *                            src/cuda.jl:88                  -> internal kernels of tp3_c3/tp3_energy
+ *   src/datagen.jl:432-475   loadHistograms' c3 contract     -> tp3_set_histogram
+ *   src/determination.jl:281-338, 491-515 rotate_all_at_once / evaluate_step
+ *                                                            -> tp3_chains_* (device-resident chains)
+ *
+ * Conventions
+ *   - Every call returns an int status (TP3_OK = 0).  There is no CPU fallback:
+ *     without a usable GPU the calls fail with TP3_ERR_NO_DEVICE / TP3_ERR_CUDA.
+ *   - Host pointers are only read (or written, for outputs) during the call.
+ *   - Coefficients: interleaved (re, im) doubles, shell-major: shell k (0-based)
+ *     occupies doubles [2*LMAX^2*k, 2*LMAX^2*(k+1)), entry (l, m) at the
+ *     reference's seanindex(l, m, LMAX) - 1 (src/spherical_harmonics.jl:163-170).
+ *   - c3 output: 2N^2 x klength column-major float (the reference's raw
+ *     `return_raw=true` layout, src/cuda.jl:91): grid row g = a + N*b, column ki
+ *     enumerating k1 >= k2 >= k3 with k1 outermost (src/correlations.jl:72-81).
+ *   - Histogram: N x 2N x K3 x K3 x K3 column-major doubles (Julia's C3 array,
+ *     element (a, b, k3, k2, k1)), K3 >= K.
+ *   - One context = one CUDA stream; calls on a context must be serialised by the
+ *     caller.  Contexts are independent.
+ */
+#ifndef TP3_H
+#define TP3_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TP3_OK 0
+#define TP3_ERR_ARG 1            /* bad argument or shape */
+#define TP3_ERR_TABLE 2          /* table construction failed an invariant */
+#define TP3_ERR_CUDA 3           /* CUDA runtime error */
+#define TP3_ERR_NO_DEVICE 4      /* no usable CUDA device */
+#define TP3_ERR_NO_HISTOGRAM 5   /* energy requested before tp3_set_histogram */
+#define TP3_ERR_BAD_HISTOGRAM 6  /* NaN/Inf value or a slab with zero L1 norm */
+#define TP3_ERR_TIMEOUT 7        /* a bounded device wait ran out */
+#define TP3_ERR_UNSUPPORTED 8    /* mode not available for this (L, K, N, lambda) */
+#define TP3_ERR_ALLOC 9          /* device or host allocation failed */
+
+/* Evaluation modes (tp3_set_mode). */
+#define TP3_MODE_PLAIN_FP32 0    /* direct coupling + FP32 SIMT angular contraction, full grid */
+#define TP3_MODE_TC_BF16X3 1     /* pair-factorised coupling + tcgen05 BF16 hi/lo x3 */
+#define TP3_MODE_AUTO (-1)       /* fastest available mode for this shape */
+
+typedef struct tp3_ctx tp3_ctx;
+
+/* Text for a status code (static storage). */
+const char* tp3_status_string(int status);
+/* Detail of the last failing call on ctx (or of the last failed tp3_ctx_create
+ * on this thread when ctx is NULL). */
+const char* tp3_last_error(const tp3_ctx* ctx);
+/* ABI version, (major << 16) | minor. */
+int tp3_version(void);
+
+/* ---- host-only helpers (no GPU needed) ---------------------------------- */
+/* Wigner 3j symbol (j1 j2 j3; m1 m2 m3): role of gsl_sf_coupling_3j as used by
+ * wigner() at src/spherical_harmonics.jl:63-65 (argument order here is the
+ * symbol's: j1, j2, j3, m1, m2, m3). */
+double tp3_wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);
+/* sphPlm(l, m, theta): src/spherical_harmonics.jl:69-76. */
+double tp3_sphPlm(int l, int m, double theta);
+/* Basis sizes without a GPU: info[0] = basislen, [1] = n_lt, [2] = klength,
+ * [3] = grid points 2N^2, [4] = unique grid points evaluated, [5] = their
+ * multiplicity, [6] = compact coefficients per shell.  calculate_basis,
+ * src/correlations.jl:87-131. */
+int tp3_basis_info(int L, int LMAX, int N, int K, double lambda, double dq, int64_t* info);
+
+/* ---- context ------------------------------------------------------------ */
+/* Build tables for (L, LMAX, N, K, lambda, dq) and upload them to the current
+ * CUDA device.  lrange = 0:2:L; LMAX >= L+1. */
+int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_ctx** out);
+void tp3_ctx_destroy(tp3_ctx* ctx);
+/* Launch on this cudaStream_t from now on (NULL = the context's own stream). */
+int tp3_set_stream(tp3_ctx* ctx, void* cuda_stream);
+int tp3_set_mode(tp3_ctx* ctx, int mode);
+int tp3_get_mode(const tp3_ctx* ctx, int* mode);
+/* Pre-size scratch for batches of up to n proposals (otherwise sized on first use). */
+int tp3_reserve(tp3_ctx* ctx, int n);
+
+/* Reference histogram c3ref (loadHistograms output).  Slabs are L1-normalised per
+ * (k1, k2, k3) exactly as energy() does before the log-likelihood. */
+int tp3_set_histogram(tp3_ctx* ctx, const double* c3ref, int K3);
+
+/* Raw model correlation c3 (2N^2 x klength, column-major float). */
+int tp3_c3(tp3_ctx* ctx, const double* coeff, float* out);
+
+/* Bayes energy of one coefficient set. */
+int tp3_energy(tp3_ctx* ctx, const double* coeff, double* E);
+/* Bayes energies of n coefficient sets stored back to back (n * K * LMAX^2 complex). */
+int tp3_energy_batch(tp3_ctx* ctx, int n, const double* coeffs, double* E);
+/* Same with device pointers: d_coeffs = n * K * LMAX^2 complex doubles in device
+ * memory, d_E = n doubles in device memory.  Asynchronous on the context stream. */
+int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E);
+
+/* ---- per-launch timing of the dominant kernel ----------------------------- */
+/* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on
+ * the launching stream; tp3_profile_read returns the launch count and the summed
+ * milliseconds (synchronising the stream) and resets both. */
+int tp3_profile_enable(tp3_ctx* ctx, int on);
+int tp3_profile_read(tp3_ctx* ctx, int64_t* launches, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TP3_H */

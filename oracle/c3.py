@@ -1,0 +1,127 @@
+"""Three-photon correlation c3 and the Bayes energy (oracle, FP64).
+
+TEST INFRASTRUCTURE ONLY (see oracle/sh.py).
+
+Forms implemented here:
+
+* ``triple_products``   T[ki, lt] = sum_{j in lt} w_j Re(c_k1[i1] c_k2[i2] c_k3[i3])
+                         (correlations.jl:157-176, the ``As`` sum), FP64.
+* ``c3_reference_form`` the reference CPU path restated with its mixed precision:
+                         f32 B and h_P, f64 T / PA / accumulation
+                         (correlations.jl:157-193).  PA[j, ki] = T * h_P[j, ki]; c3 = B * PA.
+* ``c3_lt_form``        c3 = F T^T with an FP64 F table (lambda = 0).  Mathematically the
+                         same sum regrouped by l-triple; used as the FP64 oracle.
+* ``energy_bayes``      correlations.jl:196-226 with tripletFactor (datagen.jl:166-174).
+* ``load_histogram``    the c3ref contract of loadHistograms (datagen.jl:432-475).
+
+Coefficient input everywhere: complex128 array ``coeff[K', LMAX^2]`` in seanindex
+order (row k-1 is shell k), the reference's ``intensity.coeff[k]``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .basis import OracleBasis, lt_of_entry
+from .sh import tripletFactor
+
+
+def triple_products(b: OracleBasis, coeff: np.ndarray) -> np.ndarray:
+    """T[ki, lt] in FP64 (the As accumulator of correlations.jl:169-172)."""
+    coeff = np.asarray(coeff, dtype=np.complex128)
+    ks = b.klist - 1
+    i1 = b.indices[0] - 1
+    i2 = b.indices[1] - 1
+    i3 = b.indices[2] - 1
+    T = np.zeros((b.klength, b.n_lt), dtype=np.float64)
+    c1 = coeff[ks[:, 0]]
+    c2 = coeff[ks[:, 1]]
+    c3 = coeff[ks[:, 2]]
+    for t, (_, _, _, mc, js) in enumerate(b.mcombolist):
+        sl = slice(js - 1, js - 1 + mc)
+        prod = c1[:, i1[sl]] * c2[:, i2[sl]] * c3[:, i3[sl]]
+        T[:, t] = prod.real @ b.wignerlist[sl]
+    return T
+
+
+def c3_reference_form(b: OracleBasis, coeff: np.ndarray, B32: np.ndarray, P32: np.ndarray) -> np.ndarray:
+    """Reference CPU c3 (G x klength, f64) with the reference's f32 tables.
+
+    PA[j, ki] = As(ki, lt(j)) * h_P[j, ki]  (correlations.jl:173)
+    c3 = B * PA                              (correlations.jl:182)
+    """
+    T = triple_products(b, coeff)
+    lt = lt_of_entry(b)
+    PA = T[:, lt].T * P32.astype(np.float64)          # [basislen, klength]
+    return B32.astype(np.float64) @ PA
+
+
+def c3_lt_form(F: np.ndarray, T: np.ndarray) -> np.ndarray:
+    """c3[g, ki] = sum_lt F[g, lt] T[ki, lt] (FP64)."""
+    return F @ T.T
+
+
+def neumaier_sum(values) -> float:
+    s = 0.0
+    c = 0.0
+    for v in values:
+        t = s + v
+        if abs(s) >= abs(v):
+            c += (s - t) + v
+        else:
+            c += (v - t) + s
+        s = t
+    return s + c
+
+
+def slab_energies(c3: np.ndarray, c3ref: np.ndarray, K: int, N: int, K3_range=None) -> np.ndarray:
+    """Per-slab terms tf(k) * (-sum q^ log p^) of the Bayes energy (correlations.jl:203-224).
+
+    c3: G x klength raw correlation (column ki in k1>=k2>=k3 order).
+    c3ref: N x 2N x K3 x K3 x K3 histogram (c3ref[:, :, k3, k2, k1]).
+    """
+    if K3_range is None:
+        K3_range = range(1, K + 1)
+    p_all = np.maximum(c3, 1e-30)
+    kmin = min(K3_range)
+    out = []
+    i = 0
+    for k1 in K3_range:
+        for k2 in range(kmin, k1 + 1):
+            for k3 in range(kmin, k2 + 1):
+                p = p_all[:, i].reshape(N, 2 * N, order="F")
+                i += 1
+                q = c3ref[:, :, k3 - 1, k2 - 1, k1 - 1]
+                p = p / np.sum(np.abs(p))
+                q = q / np.sum(np.abs(q))
+                out.append(-1.0 * np.sum(q * np.log(p)) * tripletFactor(k1, k2, k3))
+    return np.asarray(out)
+
+
+def energy_bayes(c3: np.ndarray, c3ref: np.ndarray, K: int, N: int, K3_range=None) -> float:
+    """Bayes energy (correlations.jl:196-226) with a compensated slab sum."""
+    return neumaier_sum(slab_energies(c3, c3ref, K, N, K3_range).tolist())
+
+
+def load_histogram(c3_full: np.ndarray, K3: int) -> np.ndarray:
+    """loadHistograms' c3 contract (datagen.jl:445-468): double an N x N histogram to
+    N x 2N, clamp at 1e-30, cut to K3 shells, normalise globally (L1)."""
+    NA, NB = c3_full.shape[0], c3_full.shape[1]
+    if NA == NB:
+        c3_full = np.concatenate([c3_full, c3_full], axis=1)
+    c3_full = np.maximum(c3_full, 1e-30)
+    c3 = c3_full[:, :, :K3, :K3, :K3]
+    return c3 / np.sum(np.abs(c3))
+
+
+def c3_to_5d(c3: np.ndarray, K: int, N: int) -> np.ndarray:
+    """FullCorrelation_parallized's non-raw layout: t[:, :, k3, k2, k1] (correlations.jl:186-191)."""
+    t = np.zeros((N, 2 * N, K, K, K), dtype=np.float64, order="F")
+    i = 0
+    for k1 in range(1, K + 1):
+        for k2 in range(1, k1 + 1):
+            for k3 in range(1, k2 + 1):
+                t[:, :, k3 - 1, k2 - 1, k1 - 1] = c3[:, i].reshape(N, 2 * N, order="F")
+                i += 1
+    return t

@@ -1,0 +1,99 @@
+"""GPU parity of libtp3 against the oracle, called through the C ABI.
+
+Tolerances (spec correctness parts 1-3):
+  c3 relative L1 vs the reference-form restatement   <= 1e-5  (tests/test_cuda.jl:15)
+  energy relative vs the reference-form restatement  <= 1e-6  (tests/test_cuda.jl:34)
+  c3 max / RMS error vs the FP64 oracle are asserted below stated bounds.
+"""
+import numpy as np
+import pytest
+
+import tp3
+from tp3 import _lib
+from oracle.basis import enumerate_basis, lt_form_F
+from oracle.c3 import triple_products, c3_lt_form, energy_bayes
+
+pytestmark = pytest.mark.gpu
+
+MODES = [tp3.TP3_MODE_PLAIN_FP32]
+
+
+def rel_l1(a, b):
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+@pytest.fixture(scope="module")
+def basis1(config1):
+    p = config1["params"]
+    b = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    yield b
+    b.close()
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_c3_config1(basis1, config1, mode):
+    basis1.set_mode(mode)
+    vol = tp3.SphericalHarmonicsVolume(config1["coeff"], 9, 8, 8.0)
+    c3 = tp3.FullCorrelation_parallized(vol, basis1, True, False, True)
+    assert c3.shape == config1["c3_fp64"].shape
+    assert rel_l1(c3, config1["c3_refform"]) <= 1e-5
+    err = np.abs(c3 - config1["c3_fp64"]) / np.abs(config1["c3_fp64"]).max()
+    assert err.max() < 1e-5 and np.sqrt(np.mean(err ** 2)) < 2e-6
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_energy_config1(basis1, config1, config1_hist, mode):
+    basis1.set_mode(mode)
+    vol = tp3.SphericalHarmonicsVolume(config1["coeff"], 9, 8, 8.0)
+    E = tp3.energy(vol, basis1, config1_hist)
+    assert E == pytest.approx(float(config1["E_refform"]), rel=1e-6)
+    assert E == pytest.approx(float(config1["E_fp64"]), rel=1e-6)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_energy_batch_matches_single(basis1, config1, config1_hist, mode):
+    basis1.set_mode(mode)
+    basis1.set_histogram(config1_hist)
+    rng = np.random.default_rng(7)
+    coeffs = np.stack([config1["coeff"] * (1 + 0.05 * rng.normal(size=config1["coeff"].shape)) for _ in range(5)])
+    Eb = basis1.energy_batch(coeffs)
+    Es = np.array([basis1.energy_batch(c[None])[0] for c in coeffs])
+    np.testing.assert_array_equal(Eb, Es)  # deterministic, order-independent per proposal
+    p = config1["params"]
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    F = lt_form_F(b)
+    for c, e in zip(coeffs, Eb):
+        e64 = energy_bayes(c3_lt_form(F, triple_products(b, c)), config1_hist, p["K"], p["N"])
+        assert e == pytest.approx(e64, rel=1e-6)
+
+
+def test_energy_deterministic(basis1, config1, config1_hist):
+    basis1.set_histogram(config1_hist)
+    E1 = basis1.energy_batch(config1["coeff"][None])
+    E2 = basis1.energy_batch(config1["coeff"][None])
+    assert E1[0] == E2[0]
+
+
+def test_errors_are_statuses(config1):
+    p = config1["params"]
+    b = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    with pytest.raises(tp3.TP3Error) as e:
+        b.energy_batch(config1["coeff"][None])
+    assert e.value.status == _lib.TP3_ERR_NO_HISTOGRAM
+    bad = np.ones((p["N"], 2 * p["N"], p["K"], p["K"], p["K"]))
+    bad[0, 0, 0, 0, 0] = np.nan
+    with pytest.raises(tp3.TP3Error) as e:
+        b.set_histogram(bad)
+    assert e.value.status == _lib.TP3_ERR_BAD_HISTOGRAM
+    zero = np.ones((p["N"], 2 * p["N"], p["K"], p["K"], p["K"]))
+    zero[:, :, 1, 1, 2] = 0.0
+    with pytest.raises(tp3.TP3Error) as e:
+        b.set_histogram(zero)
+    assert e.value.status == _lib.TP3_ERR_BAD_HISTOGRAM
+    small = np.ones((p["N"], 2 * p["N"], p["K"] - 1, p["K"] - 1, p["K"] - 1))
+    with pytest.raises(tp3.TP3Error) as e:
+        b.set_histogram(small)
+    assert e.value.status == _lib.TP3_ERR_ARG
+    b.close()
+    with pytest.raises(tp3.TP3Error):
+        tp3.calculate_basis(8, 8, 16, 8)  # LMAX must exceed L

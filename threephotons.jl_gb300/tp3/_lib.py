@@ -1,0 +1,89 @@
+"""ctypes binding of libtp3.so (include/tp3.h).
+
+The library is built in-tree (threephotons.jl_gb300/lib/libtp3.so).  Loading
+fails loudly when it is missing: there is no Python or CPU fallback for any
+call that computes c3 or an energy.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libtp3.so")
+
+c_int, c_double, c_void_p, c_int64 = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_int64
+P = ctypes.POINTER
+
+TP3_OK = 0
+TP3_ERR_ARG = 1
+TP3_ERR_TABLE = 2
+TP3_ERR_CUDA = 3
+TP3_ERR_NO_DEVICE = 4
+TP3_ERR_NO_HISTOGRAM = 5
+TP3_ERR_BAD_HISTOGRAM = 6
+TP3_ERR_TIMEOUT = 7
+TP3_ERR_UNSUPPORTED = 8
+TP3_ERR_ALLOC = 9
+
+TP3_MODE_PLAIN_FP32 = 0
+TP3_MODE_TC_BF16X3 = 1
+TP3_MODE_AUTO = -1
+
+# name -> (restype, argtypes); every symbol include/tp3.h declares
+SIGNATURES = {
+    "tp3_status_string": (ctypes.c_char_p, [c_int]),
+    "tp3_last_error": (ctypes.c_char_p, [c_void_p]),
+    "tp3_version": (c_int, []),
+    "tp3_wigner3j": (c_double, [c_int] * 6),
+    "tp3_sphPlm": (c_double, [c_int, c_int, c_double]),
+    "tp3_basis_info": (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, P(c_int64)]),
+    "tp3_ctx_create": (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, P(c_void_p)]),
+    "tp3_ctx_destroy": (None, [c_void_p]),
+    "tp3_set_stream": (c_int, [c_void_p, c_void_p]),
+    "tp3_set_mode": (c_int, [c_void_p, c_int]),
+    "tp3_get_mode": (c_int, [c_void_p, P(c_int)]),
+    "tp3_reserve": (c_int, [c_void_p, c_int]),
+    "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),
+    "tp3_c3": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "tp3_energy": (c_int, [c_void_p, c_void_p, P(c_double)]),
+    "tp3_energy_batch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_energy_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_profile_enable": (c_int, [c_void_p, c_int]),
+    "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),
+}
+
+_lib = None
+
+
+class TP3Error(RuntimeError):
+    def __init__(self, status: int, detail: str = ""):
+        self.status = status
+        super().__init__(f"tp3 status {status} ({status_string(status)}): {detail}")
+
+
+def load() -> ctypes.CDLL:
+    """Load libtp3.so (building is a separate step: build.py / __graft_entry__.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libtp3.so not built at {LIB_PATH}; run threephotons.jl_gb300/build.py")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(s: int) -> str:
+    return load().tp3_status_string(s).decode()
+
+
+def check(status: int, ctx=None) -> None:
+    if status != TP3_OK:
+        detail = load().tp3_last_error(ctx).decode(errors="replace")
+        raise TP3Error(status, detail)
