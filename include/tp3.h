@@ -79,7 +79,8 @@ double tp3_wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);
 double tp3_sphPlm(int l, int m, double theta);
 /* Basis sizes without a GPU: info[0] = basislen, [1] = n_lt, [2] = klength,
  * [3] = grid points 2N^2, [4] = unique grid points evaluated, [5] = their
- * multiplicity, [6] = compact coefficients per shell.  calculate_basis,
+ * multiplicity, [6] = compact coefficients per shell, [7] = entries whose
+ * Legendre product is non-zero at theta = pi/2 (lambda = 0).  calculate_basis,
  * src/correlations.jl:87-131. */
 int tp3_basis_info(int L, int LMAX, int N, int K, double lambda, double dq, int64_t* info);
 

@@ -39,8 +39,12 @@ void tp3ref_tables(int N, int64_t basislen, const int64_t* indices, int K, int64
       const double b = (ib + 0.5) * pi / N;
       B[g + G * j] = (float)cos(m2 * a + m3 * b);
     }
-    for (int64_t ki = 0; ki < klength; ++ki) {
-      const int64_t k1 = klist[3 * ki] - 1, k2 = klist[3 * ki + 1] - 1, k3 = klist[3 * ki + 2] - 1;
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t ki = 0; ki < klength; ++ki) {
+    const int64_t k1 = klist[3 * ki] - 1, k2 = klist[3 * ki + 1] - 1, k3 = klist[3 * ki + 2] - 1;
+    for (int64_t j = 0; j < basislen; ++j) {
+      const int64_t* ix = indices + 9 * j;
       const double v = w[j] * Y[k1 * ncoef + ix[0] - 1] * Y[k2 * ncoef + ix[1] - 1] * Y[k3 * ncoef + ix[2] - 1];
       hP[j + basislen * ki] = (float)v;
     }

@@ -199,6 +199,10 @@ int tp3_basis_info(int L, int LMAX, int N, int K, double lambda, double dq, int6
   tp3::fold_grid(b, true);
   info[0] = b.basislen(); info[1] = b.n_lt(); info[2] = b.klength; info[3] = b.G;
   info[4] = b.Gu; info[5] = b.mult; info[6] = b.nc;
+  int64_t nnz0 = 0;  // entries whose Legendre product is non-zero at theta = pi/2
+  for (int j = 0; j < b.basislen(); ++j)
+    nnz0 += ((b.l1[j] + b.m1[j]) % 2 == 0 && (b.l2[j] + b.m2[j]) % 2 == 0 && (b.l3[j] + b.m3[j]) % 2 == 0);
+  info[7] = nnz0;
   return TP3_OK;
 }
 
