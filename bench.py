@@ -223,7 +223,8 @@ def main():
     B = args.batch
     basis.reserve(B)
     props = proposals(base, B, PROP_SEED + rank)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     basis.set_stream(stream.cuda_stream)
     d_coeff = torch.from_numpy(props.view(np.float64)).cuda()
     d_E = torch.empty(B, dtype=torch.float64, device="cuda")
@@ -267,7 +268,7 @@ def main():
     value = ws * B * args.steps / (ms / 1e3)
 
     # end to end through the public host API (pinned host copy, H2D + compute + D2H)
-    basis.set_stream(0)
+    basis.set_stream(None)
     host_props = props.copy()
     for _ in range(2):
         basis.energy_batch(host_props)

@@ -103,6 +103,11 @@ int tp3_set_histogram(tp3_ctx* ctx, const double* c3ref, int K3);
 /* Raw model correlation c3 (2N^2 x klength, column-major float). */
 int tp3_c3(tp3_ctx* ctx, const double* coeff, float* out);
 
+/* Rotation-invariant triple products T[ki][lt] = sum_{j in lt} w_j Re(c_k1 c_k2 c_k3)
+ * (klength x n_lt row-major float) with the current mode's coupling kernel: the
+ * As values of calculate_triple_products_fast, src/correlations.jl:157-176. */
+int tp3_triple_products(tp3_ctx* ctx, const double* coeff, float* out);
+
 /* Bayes energy of one coefficient set. */
 int tp3_energy(tp3_ctx* ctx, const double* coeff, double* E);
 /* Bayes energies of n coefficient sets stored back to back (n * K * LMAX^2 complex). */
@@ -110,6 +115,10 @@ int tp3_energy_batch(tp3_ctx* ctx, int n, const double* coeffs, double* E);
 /* Same with device pointers: d_coeffs = n * K * LMAX^2 complex doubles in device
  * memory, d_E = n doubles in device memory.  Asynchronous on the context stream. */
 int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E);
+
+/* Wait for the context stream and report any device-side error (TP3_ERR_TIMEOUT
+ * when a bounded wait inside a kernel ran out). */
+int tp3_sync(tp3_ctx* ctx);
 
 /* ---- per-launch timing of the dominant kernel ----------------------------- */
 /* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on

@@ -15,7 +15,7 @@ from oracle.c3 import triple_products, c3_lt_form, energy_bayes
 
 pytestmark = pytest.mark.gpu
 
-MODES = [tp3.TP3_MODE_PLAIN_FP32]
+MODES = [tp3.TP3_MODE_PLAIN_FP32, tp3.TP3_MODE_TC_BF16X3]
 
 
 def rel_l1(a, b):
@@ -28,6 +28,18 @@ def basis1(config1):
     b = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
     yield b
     b.close()
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_triple_products_config1(basis1, config1, mode):
+    """Stage (a) alone: T = sum_j w_j Re(c c c) per (shell triple, l-triple)."""
+    basis1.set_mode(mode)
+    p = config1["params"]
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    T64 = triple_products(b, config1["coeff"])
+    T = basis1.triple_products(config1["coeff"]).astype(np.float64)
+    scale = np.abs(T64).max(axis=1, keepdims=True)
+    assert np.max(np.abs(T - T64) / scale) < 2e-5
 
 
 @pytest.mark.parametrize("mode", MODES)

@@ -1,17 +1,20 @@
 // Context and C ABI of libtp3 (declared in include/tp3.h).
 //
 // A context owns every device buffer of one (L, LMAX, N, K, lambda) basis: the
-// tables built once by tables.cpp, the normalised histogram, and scratch sized
+// tables built once from tables.cpp, the normalised histogram, and scratch sized
 // for the largest batch seen (or reserved).  Nothing is allocated per call once
 // the scratch fits; no call falls back to the CPU.
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/tp3.h"
@@ -20,43 +23,55 @@
 
 using tp3::Basis;
 using tp3::DevTables;
+using tp3::PairBlock;
+using tp3::TcMaps;
+using tp3::TcTables;
 
 namespace {
-
 thread_local std::string g_create_error;
 
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 }  // namespace
 
 struct tp3_ctx {
   Basis b;
   DevTables t{};
+  TcTables tc{};
+  bool tc_ok = false;
+  std::string tc_why;
   int device = 0;
   int mode = TP3_MODE_PLAIN_FP32;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   std::string err;
   std::vector<void*> allocs;  // table allocations, freed at destroy
+  EncodeTiledFn encode = nullptr;
+  TcMaps maps{};
 
   // histogram
   bool has_hist = false;
   float* d_qfull = nullptr;    // [klength][G]
   double* d_Qfull = nullptr;   // [klength]
+  float* d_qt = nullptr;       // [klp/128][Gu][128] folded, tiled for the TMEM epilogue
+  double* d_Qfold = nullptr;   // [klength]
 
   // scratch (sized for cap proposals)
   int cap = 0;
   double2* d_coeff = nullptr;  // [cap][K][LMAX^2]
   float2* d_cc = nullptr;      // [cap][K][nc]
-  float* d_T = nullptr;        // [cap][klp][n_ltp]
-  double2* d_part = nullptr;   // [cap][ncg][klength]
+  float* d_T = nullptr;        // [cap][klp][n_ltp]      plain path
+  double2* d_part = nullptr;   // [cap][ncg][klength]    plain path
+  __nv_bfloat16* d_Thi = nullptr;  // [cap][klp][KP]    tensor-core path
+  __nv_bfloat16* d_Tlo = nullptr;
+  double* d_Eslab = nullptr;   // [cap][klength]         tensor-core path
   double* d_E = nullptr;       // [cap]
   float* d_c3 = nullptr;       // [klength][G] (one proposal)
+  int* d_err = nullptr;        // device error flag (timeouts)
   double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
   double* h_E = nullptr;       // pinned [cap]
+  int* h_err = nullptr;        // pinned
 
   // profiling of the angular + Bayes kernel
   bool prof = false;
@@ -87,10 +102,131 @@ cudaError_t upload(tp3_ctx* c, const std::vector<T>& h, const T** out) {
   return e;
 }
 
+// ---- tensor-core path tables -------------------------------------------------
+std::string build_tc_tables(const Basis& b, std::vector<PairBlock>& pbs, std::vector<int>& eofs,
+                            std::vector<float>& wtab, int& maxs, int& SDmax) {
+  std::map<std::tuple<int, int, int>, int> ltidx;
+  for (int t = 0; t < b.n_lt(); ++t) ltidx[{b.lt_l1[t], b.lt_l2[t], b.lt_l3[t]}] = t;
+  struct Item { PairBlock pb; double work; std::vector<int> e; std::vector<float> w; };
+  std::vector<Item> items;
+  maxs = 0;
+  SDmax = 0;
+  for (int l1 = 0; l1 <= b.L; l1 += 2)
+    for (int l2 = 0; l2 <= b.L; l2 += 2) {
+      const int l3min = std::abs(l1 - l2), l3max = std::min(l1 + l2, b.L - (b.L & 1));
+      if (l3min > l3max) continue;
+      Item it{};
+      PairBlock& pb = it.pb;
+      pb.l1 = l1; pb.l2 = l2; pb.l3min = l3min; pb.nl3 = (l3max - l3min) / 2 + 1; pb.M = l3max;
+      pb.SD = 0;
+      for (int s = 0; s < pb.nl3; ++s) {
+        const int l3 = l3min + 2 * s;
+        auto f = ltidx.find({l1, l2, l3});
+        if (f == ltidx.end()) return "pair block l-triple missing from the basis";
+        if (s == 0) pb.lt_base = f->second;
+        else if (f->second != pb.lt_base + s) return "pair block l-triples are not consecutive";
+        pb.SD += 2 * l3 + 1;
+      }
+      int run = 0;
+      for (int e = 0; e <= 2 * pb.M; ++e) {
+        const int m3 = e - pb.M;
+        it.e.push_back(run);
+        const int m1lo = std::max(-l1, -l2 - m3), m1hi = std::min(l1, l2 - m3);
+        for (int m1 = m1lo; m1 <= m1hi; ++m1) {
+          const int m2 = -m3 - m1;
+          for (int s = 0; s < pb.nl3; ++s) {
+            const int l3 = l3min + 2 * s;
+            it.w.push_back(std::abs(m3) <= l3 ? (float)tp3::wigner3j(l1, l2, l3, m1, m2, m3) : 0.f);
+          }
+          run += pb.nl3;
+        }
+      }
+      it.work = (double)run;
+      maxs = std::max(maxs, pb.nl3);
+      SDmax = std::max(SDmax, pb.SD);
+      items.push_back(std::move(it));
+    }
+  std::sort(items.begin(), items.end(), [](const Item& a, const Item& c) { return a.work > c.work; });
+  for (auto& it : items) {
+    it.pb.wofs = (int)wtab.size();
+    it.pb.eofs = (int)eofs.size();
+    wtab.insert(wtab.end(), it.w.begin(), it.w.end());
+    eofs.insert(eofs.end(), it.e.begin(), it.e.end());
+    pbs.push_back(it.pb);
+  }
+  return "";
+}
+
+cudaError_t encode_2d_bf16(tp3_ctx* c, CUtensorMap* m, void* ptr, uint64_t inner, uint64_t rows, uint32_t box_inner,
+                           uint32_t box_rows) {
+  cuuint64_t dims[2] = {inner, rows};
+  cuuint64_t strides[1] = {inner * 2};
+  cuuint32_t box[2] = {box_inner, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+std::string setup_tc(tp3_ctx* c) {
+  const Basis& b = c->b;
+  DevTables& t = c->t;
+  TcTables& tc = c->tc;
+  if (b.lambda != 0.0) return "needs lambda = 0";
+  if (b.mult != 4) return "needs even N (grid fold)";
+  if (b.Gu > 512) return "more than 512 unique grid points (N > 32)";
+  std::vector<PairBlock> pbs;
+  std::vector<int> eofs;
+  std::vector<float> wtab;
+  int maxs = 0, SDmax = 0;
+  std::string m = build_tc_tables(b, pbs, eofs, wtab, maxs, SDmax);
+  if (!m.empty()) return m;
+  if (maxs > 13) return "more than 13 l3 values per pair block (L > 24)";
+  if ((size_t)b.K * (b.nc + SDmax) * sizeof(float2) > 227 * 1024) return "coupling tile exceeds shared memory";
+  tc.n_pb = (int)pbs.size();
+  tc.maxs = maxs;
+  tc.SDmax = SDmax;
+  tc.KP = (b.n_lt() + 31) / 32 * 32;
+  tc.nhalf = (b.Gu + 255) / 256;
+  tc.NP = 256 * tc.nhalf;
+  // F on the unique grid points, split into bf16 hi + lo
+  std::vector<double> F;
+  tp3::build_F(b, F);
+  std::vector<__nv_bfloat16> Fhi((size_t)tc.NP * tc.KP, __float2bfloat16(0.f)), Flo(Fhi);
+  for (int u = 0; u < b.Gu; ++u)
+    for (int l = 0; l < b.n_lt(); ++l) {
+      const float v = (float)F[(size_t)u * b.n_lt() + l];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      Fhi[(size_t)u * tc.KP + l] = hi;
+      Flo[(size_t)u * tc.KP + l] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    }
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return "cuTensorMapEncodeTiled unavailable";
+  c->encode = (EncodeTiledFn)fn;
+  cudaError_t e;
+  if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
+      (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
+      (e = upload(c, Fhi, &tc.Fhi)) != cudaSuccess || (e = upload(c, Flo, &tc.Flo)) != cudaSuccess ||
+      (e = tp3::tc_configure()) != cudaSuccess)
+    return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
+  if ((e = encode_2d_bf16(c, &c->maps.b_hi, (void*)tc.Fhi, tc.KP, tc.NP, 32, 256)) != cudaSuccess ||
+      (e = encode_2d_bf16(c, &c->maps.b_lo, (void*)tc.Flo, tc.KP, tc.NP, 32, 256)) != cudaSuccess)
+    return "tensor map encoding of F failed";
+  (void)t;
+  return "";
+}
+
+// ---- scratch ------------------------------------------------------------------
 void free_scratch(tp3_ctx* c) {
   cudaFree(c->d_coeff); cudaFree(c->d_cc); cudaFree(c->d_T); cudaFree(c->d_part); cudaFree(c->d_E);
+  cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab);
   cudaFreeHost(c->h_coeff); cudaFreeHost(c->h_E);
   c->d_coeff = nullptr; c->d_cc = nullptr; c->d_T = nullptr; c->d_part = nullptr; c->d_E = nullptr;
+  c->d_Thi = nullptr; c->d_Tlo = nullptr; c->d_Eslab = nullptr;
   c->h_coeff = nullptr; c->h_E = nullptr;
   c->cap = 0;
 }
@@ -102,20 +238,31 @@ int ensure_cap(tp3_ctx* c, int n) {
   const int ncg = tp3::plain_ncg(t);
   const size_t ncoef = (size_t)t.LMAX * t.LMAX;
   cudaError_t e;
+  const size_t tbytes = (size_t)n * t.klp * t.n_ltp * sizeof(float);
+  const size_t tcb = c->tc_ok ? (size_t)n * t.klp * c->tc.KP * sizeof(__nv_bfloat16) : 0;
   if ((e = cudaMalloc(&c->d_coeff, (size_t)n * t.K * ncoef * sizeof(double2))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_cc, (size_t)n * t.K * t.nc * sizeof(float2))) != cudaSuccess ||
-      (e = cudaMalloc(&c->d_T, (size_t)n * t.klp * t.n_ltp * sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_T, tbytes)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_part, (size_t)n * ncg * t.klength * sizeof(double2))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_E, (size_t)n * sizeof(double))) != cudaSuccess ||
+      (c->tc_ok && (e = cudaMalloc(&c->d_Thi, tcb)) != cudaSuccess) ||
+      (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
+      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * t.klength * sizeof(double))) != cudaSuccess) ||
       (e = cudaMallocHost(&c->h_coeff, (size_t)n * t.K * ncoef * 2 * sizeof(double))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_E, (size_t)n * sizeof(double))) != cudaSuccess) {
     free_scratch(c);
     cudaGetLastError();
     return fail(c, TP3_ERR_ALLOC, std::string("scratch allocation: ") + cudaGetErrorString(e));
   }
-  // padding rows/columns of T stay zero for the lifetime of the buffer
-  if ((e = cudaMemset(c->d_T, 0, (size_t)n * t.klp * t.n_ltp * sizeof(float))) != cudaSuccess)
-    return cuda_fail(c, e, "cudaMemset T");
+  // padding rows/columns of the coupling outputs stay zero for the lifetime of the buffers
+  if ((e = cudaMemset(c->d_T, 0, tbytes)) != cudaSuccess) return cuda_fail(c, e, "cudaMemset T");
+  if (c->tc_ok) {
+    if ((e = cudaMemset(c->d_Thi, 0, tcb)) != cudaSuccess || (e = cudaMemset(c->d_Tlo, 0, tcb)) != cudaSuccess)
+      return cuda_fail(c, e, "cudaMemset T hi/lo");
+    if ((e = encode_2d_bf16(c, &c->maps.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 32, 128)) != cudaSuccess ||
+        (e = encode_2d_bf16(c, &c->maps.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 32, 128)) != cudaSuccess)
+      return fail(c, TP3_ERR_CUDA, "tensor map encoding of T failed");
+  }
   c->cap = n;
   return TP3_OK;
 }
@@ -135,22 +282,57 @@ int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) {
   return 1;
 }
 
+// Coupling stage for n proposals whose compact coefficients are in d_cc.
+int run_coupling(tp3_ctx* c, int n, bool want_T32) {
+  const auto& t = c->t;
+  cudaError_t e;
+  if (c->mode == TP3_MODE_TC_BF16X3) {
+    if ((e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_Thi, c->d_Tlo, want_T32 ? c->d_T : nullptr,
+                                     c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "couple_pair");
+  } else {
+    if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "couple_direct");
+  }
+  return TP3_OK;
+}
+
 // Score n proposals whose FP64 coefficients are already in d_coeff (device).
 int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E) {
   const auto& t = c->t;
   cudaError_t e;
   if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
   if ((e = tp3::launch_gather(t, n, d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
-  if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
-    return cuda_fail(c, e, "couple_direct");
-  const int ncg = tp3::plain_ncg(t);
+  if (int r = run_coupling(c, n, false)) return r;
   cudaEvent_t a, b;
   int pr = prof_begin(c, &a, &b);
-  if ((e = tp3::launch_angular_plain(t, n, c->d_T, c->d_qfull, c->d_part, ncg, nullptr, c->stream)) != cudaSuccess)
-    return cuda_fail(c, e, "angular_plain");
-  if (pr) cudaEventRecord(b, c->stream);
-  if ((e = tp3::launch_finalize(t, n, c->d_part, ncg, c->d_Qfull, 1, d_E, c->stream)) != cudaSuccess)
-    return cuda_fail(c, e, "finalize");
+  if (c->mode == TP3_MODE_TC_BF16X3) {
+    if ((e = tp3::launch_angular_tc(t, c->tc, c->maps, n, c->d_qt, c->d_Qfold, c->d_Eslab, nullptr, c->d_err,
+                                    c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "angular_tc");
+    if (pr) cudaEventRecord(b, c->stream);
+    if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "finalize_slabs");
+  } else {
+    const int ncg = tp3::plain_ncg(t);
+    if ((e = tp3::launch_angular_plain(t, n, c->d_T, c->d_qfull, c->d_part, ncg, nullptr, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "angular_plain");
+    if (pr) cudaEventRecord(b, c->stream);
+    if ((e = tp3::launch_finalize(t, n, c->d_part, ncg, c->d_Qfull, 1, d_E, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "finalize");
+  }
+  return TP3_OK;
+}
+
+// After a synchronising call: report a device-side timeout, if any.
+int check_device_error(tp3_ctx* c) {
+  cudaError_t e = cudaMemcpy(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "error flag read");
+  if (*c->h_err != 0) {
+    const int code = *c->h_err;
+    cudaMemset(c->d_err, 0, sizeof(int));
+    return fail(c, code, "a bounded device wait ran out; results of this call are invalid");
+  }
   return TP3_OK;
 }
 
@@ -183,7 +365,7 @@ const char* tp3_status_string(int s) {
 
 const char* tp3_last_error(const tp3_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
 
-int tp3_version(void) { return (1 << 16) | 0; }
+int tp3_version(void) { return (1 << 16) | 1; }
 
 double tp3_wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
   return tp3::wigner3j(j1, j2, j3, m1, m2, m3);
@@ -285,11 +467,17 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
       (e = upload(c, idx, &t.idx)) != cudaSuccess || (e = upload(c, lt, &t.lt)) != cudaSuccess ||
       (e = upload(c, kl, &t.kl)) != cudaSuccess || (e = upload(c, b.tf, &t.tf)) != cudaSuccess ||
       (e = upload(c, Ffull, &t.Ffull)) != cudaSuccess || (e = upload(c, b.u_to_g, &t.u_to_g)) != cudaSuccess ||
-      (e = upload(c, b.g_to_u, &t.g_to_u)) != cudaSuccess || (e = tp3::plain_configure()) != cudaSuccess) {
+      (e = upload(c, b.g_to_u, &t.g_to_u)) != cudaSuccess || (e = tp3::plain_configure()) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess || (e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess ||
+      (e = cudaMallocHost(&c->h_err, sizeof(int))) != cudaSuccess) {
     std::string msg = std::string("table upload: ") + cudaGetErrorString(e);
     tp3_ctx_destroy(c);
     return fail(nullptr, TP3_ERR_CUDA, msg);
   }
+  c->tc_why = setup_tc(c);
+  c->tc_ok = c->tc_why.empty();
+  cudaGetLastError();
+  c->mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
   *out = c;
   return TP3_OK;
 }
@@ -300,7 +488,9 @@ void tp3_ctx_destroy(tp3_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_scratch(c);
   for (void* p : c->allocs) cudaFree(p);
-  cudaFree(c->d_qfull); cudaFree(c->d_Qfull); cudaFree(c->d_c3);
+  cudaFree(c->d_qfull); cudaFree(c->d_Qfull); cudaFree(c->d_qt); cudaFree(c->d_Qfold); cudaFree(c->d_c3);
+  cudaFree(c->d_err);
+  cudaFreeHost(c->h_err);
   for (auto ev : c->ev) cudaEventDestroy(ev);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -314,8 +504,10 @@ int tp3_set_stream(tp3_ctx* c, void* s) {
 
 int tp3_set_mode(tp3_ctx* c, int mode) {
   if (int r = check_ctx(c)) return r;
-  if (mode == TP3_MODE_AUTO) mode = TP3_MODE_PLAIN_FP32;
-  if (mode != TP3_MODE_PLAIN_FP32) return fail(c, TP3_ERR_UNSUPPORTED, "mode not available in this build");
+  if (mode == TP3_MODE_AUTO) mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
+  if (mode == TP3_MODE_TC_BF16X3 && !c->tc_ok)
+    return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core mode unavailable: " + c->tc_why);
+  if (mode != TP3_MODE_PLAIN_FP32 && mode != TP3_MODE_TC_BF16X3) return fail(c, TP3_ERR_ARG, "unknown mode");
   c->mode = mode;
   return TP3_OK;
 }
@@ -336,13 +528,15 @@ int tp3_set_histogram(tp3_ctx* c, const double* c3ref, int K3) {
   if (int r = check_ctx(c)) return r;
   if (!c3ref) return fail(c, TP3_ERR_ARG, "c3ref is NULL");
   const Basis& b = c->b;
+  const DevTables& t = c->t;
   if (K3 < b.K) return fail(c, TP3_ERR_ARG, "histogram has fewer shells (K3) than the basis (K)");
-  const int N = b.N, G = b.G;
-  const size_t slab = (size_t)G;
+  const int G = b.G;
   std::vector<float> q((size_t)b.klength * G);
-  std::vector<double> Qs(b.klength);
+  std::vector<double> Qs(b.klength), Qf(b.klength);
+  std::vector<float> qt((size_t)t.klp * b.Gu, 0.f);  // [klp/128][Gu][128]
+  std::vector<double> fold(b.Gu);
   for (int ki = 0; ki < b.klength; ++ki) {
-    const size_t off = slab * ((size_t)b.k3s[ki] + (size_t)K3 * ((size_t)b.k2s[ki] + (size_t)K3 * b.k1s[ki]));
+    const size_t off = (size_t)G * ((size_t)b.k3s[ki] + (size_t)K3 * ((size_t)b.k2s[ki] + (size_t)K3 * b.k1s[ki]));
     const double* s = c3ref + off;
     double l1 = 0.0;
     for (int g = 0; g < G; ++g) {
@@ -351,21 +545,36 @@ int tp3_set_histogram(tp3_ctx* c, const double* c3ref, int K3) {
     }
     if (!(l1 > 0.0)) return fail(c, TP3_ERR_BAD_HISTOGRAM, "histogram slab with zero L1 norm");
     double qs = 0.0;
+    std::fill(fold.begin(), fold.end(), 0.0);
     for (int g = 0; g < G; ++g) {
-      float v = (float)(s[g] / l1);
-      q[(size_t)ki * G + g] = v;
-      qs += (double)v;
+      const double v = s[g] / l1;
+      const float vf = (float)v;
+      q[(size_t)ki * G + g] = vf;
+      qs += (double)vf;
+      fold[b.g_to_u[g]] += v;
     }
     Qs[ki] = qs;
+    double qf = 0.0;
+    const int tile = ki / 128, r = ki % 128;
+    for (int u = 0; u < b.Gu; ++u) {
+      const float vf = (float)fold[u];
+      qt[((size_t)tile * b.Gu + u) * 128 + r] = vf;
+      qf += (double)vf;
+    }
+    Qf[ki] = qf;
   }
-  (void)N;
   cudaError_t e;
   if (!c->d_qfull) {
-    if ((e = cudaMalloc(&c->d_qfull, q.size() * sizeof(float))) != cudaSuccess) return cuda_fail(c, e, "cudaMalloc q");
-    if ((e = cudaMalloc(&c->d_Qfull, Qs.size() * sizeof(double))) != cudaSuccess) return cuda_fail(c, e, "cudaMalloc Qs");
+    if ((e = cudaMalloc(&c->d_qfull, q.size() * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_Qfull, Qs.size() * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_qt, qt.size() * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(&c->d_Qfold, Qf.size() * sizeof(double))) != cudaSuccess)
+      return cuda_fail(c, e, "cudaMalloc histogram");
   }
   if ((e = cudaMemcpyAsync(c->d_qfull, q.data(), q.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(c->d_Qfull, Qs.data(), Qs.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(c->d_qt, qt.data(), qt.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(c->d_Qfold, Qf.data(), Qf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "histogram upload");
   c->has_hist = true;
@@ -385,13 +594,35 @@ int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {
   if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "H2D coeff");
   if ((e = tp3::launch_gather(t, 1, c->d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
-  if ((e = tp3::launch_couple_direct(t, 1, c->d_cc, c->d_T, c->stream)) != cudaSuccess) return cuda_fail(c, e, "couple");
-  if ((e = tp3::launch_angular_plain(t, 1, c->d_T, nullptr, nullptr, tp3::plain_ncg(t), c->d_c3, c->stream)) != cudaSuccess)
-    return cuda_fail(c, e, "angular store");
+  if (int r = run_coupling(c, 1, false)) return r;
+  if (c->mode == TP3_MODE_TC_BF16X3)
+    e = tp3::launch_angular_tc(t, c->tc, c->maps, 1, nullptr, nullptr, nullptr, c->d_c3, c->d_err, c->stream);
+  else
+    e = tp3::launch_angular_plain(t, 1, c->d_T, nullptr, nullptr, tp3::plain_ncg(t), c->d_c3, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "angular store");
   // device layout [ki][g] is the column-major G x klength layout of the reference
   if ((e = cudaMemcpyAsync(out, c->d_c3, (size_t)t.klength * t.G * sizeof(float), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "D2H c3");
+  return check_device_error(c);
+}
+
+int tp3_triple_products(tp3_ctx* c, const double* coeff, float* out) {
+  if (int r = check_ctx(c)) return r;
+  if (!coeff || !out) return fail(c, TP3_ERR_ARG, "NULL pointer");
+  if (int r = ensure_cap(c, 1)) return r;
+  const auto& t = c->t;
+  const size_t nco = (size_t)t.K * t.LMAX * t.LMAX;
+  cudaError_t e;
+  std::memcpy(c->h_coeff, coeff, nco * 2 * sizeof(double));
+  if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
+    return cuda_fail(c, e, "H2D coeff");
+  if ((e = tp3::launch_gather(t, 1, c->d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
+  if (int r = run_coupling(c, 1, true)) return r;
+  if ((e = cudaMemcpy2DAsync(out, t.n_lt * sizeof(float), c->d_T, t.n_ltp * sizeof(float), t.n_lt * sizeof(float),
+                             t.klength, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+    return cuda_fail(c, e, "D2H T");
   return TP3_OK;
 }
 
@@ -409,6 +640,7 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
   if ((e = cudaMemcpyAsync(c->h_E, c->d_E, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "D2H energy");
+  if (int r = check_device_error(c)) return r;
   std::memcpy(E, c->h_E, n * sizeof(double));
   return TP3_OK;
 }
@@ -420,6 +652,13 @@ int tp3_energy_batch_device(tp3_ctx* c, int n, const void* d_coeffs, void* d_E) 
   if (n < 1 || !d_coeffs || !d_E) return fail(c, TP3_ERR_ARG, "bad batch arguments");
   if (int r = ensure_cap(c, n)) return r;
   return run_energy(c, n, (const double2*)d_coeffs, (double*)d_E);
+}
+
+int tp3_sync(tp3_ctx* c) {
+  if (int r = check_ctx(c)) return r;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronize");
+  return check_device_error(c);
 }
 
 int tp3_profile_enable(tp3_ctx* c, int on) {

@@ -1,5 +1,7 @@
 // Internal declarations shared by the context code and the kernel files.
 #pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -30,6 +32,41 @@ cudaError_t launch_angular_plain(const DevTables& t, int n, const float* T, cons
                                  double2* part, int ncg, float* c3out, cudaStream_t s);
 cudaError_t launch_finalize(const DevTables& t, int n, const double2* part, int ncg,
                             const double* Qs, int mult, double* E, cudaStream_t s);
+
+// One (l1, l2) block of the pair-factorised coupling.
+struct PairBlock {
+  int l1, l2, l3min, nl3;  // l3 = l3min + 2 s, s < nl3
+  int M;                   // |m3| <= M
+  int SD;                  // sum_s (2 l3_s + 1)
+  int lt_base;             // l-triple index of (l1, l2, l3min); the block's l-triples are consecutive
+  int wofs;                // offset of the block in wtab
+  int eofs;                // offset of the block's per-m3 table in eofs[]
+};
+
+// Device tables of the tensor-core path.
+struct TcTables {
+  int n_pb = 0, maxs = 0, SDmax = 0;
+  int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
+  int NP = 0, nhalf = 0;   // unique grid points padded to 256 * nhalf
+  const int* coff = nullptr;
+  const PairBlock* pbs = nullptr;
+  const int* eofs = nullptr;
+  const float* wtab = nullptr;
+  const __nv_bfloat16* Fhi = nullptr;  // [NP][KP]
+  const __nv_bfloat16* Flo = nullptr;
+};
+
+struct TcMaps {
+  CUtensorMap a_hi, a_lo, b_hi, b_lo;
+};
+
+size_t tc_smem_bytes();
+cudaError_t tc_configure();
+cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc,
+                               __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
+cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
+                              const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s);
+cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s);
 
 int plain_ncg(const DevTables& t);
 // Per-device kernel attributes of the plain path (call with the device current).

@@ -1,0 +1,541 @@
+// Fast path: pair-factorised coupling (SIMT FP32) -> tcgen05 angular contraction
+// with BF16 hi/lo split operands (three MMA passes, FP32 accumulation in TMEM) and
+// the Bayes log-likelihood fused into the TMEM epilogue -> FP64 finalize.
+//
+// Stage (a), coupling.  For one (l1, l2) pair block and one shell k1, all shells
+// k2 <= k1 and every m3:
+//     D[k2][l3][m3] = sum_m1 w(l1 m1 l2 m2 l3 m3) c_k1[l1,m1] c_k2[l2,m2],  m2 = -m3 - m1
+// then for every k3 <= k2
+//     T[(k1,k2,k3)][(l1,l2,l3)] = Re sum_m3 D[k2][l3][m3] c_k3[l3,m3]
+// which is the reference's As sum (src/correlations.jl:169-172; src/cuda_kernel.cu:31-37)
+// regrouped so that each product c_k1 c_k2 is formed once per pair of shells and
+// reused by every l3 and every k3.  T is written as a BF16 pair (hi, lo = bf16(T - hi)).
+//
+// Stage (b)+(c), angular + Bayes.  At lambda = 0 the model correlation on the unique
+// grid points u of the symmetry fold is c3[ki][u] = sum_lt T[ki][lt] F[u][lt]
+// (F = w Y Y Y cos(m2 alpha + m3 beta) summed per l-triple; the reference's B * PA of
+// src/correlations.jl:182 / src/cuda.jl:88 regrouped).  One CTA owns 128 shell triples
+// (TMEM lanes) and all unique grid points (TMEM columns, two halves of 256).  Operand
+// tiles are staged by TMA (64-byte swizzle) through a 4-deep mbarrier ring; one thread
+// issues tcgen05.mma (M=128, N=256, K=16) for hi*hi, hi*lo and lo*hi.  Eight epilogue
+// warps read the accumulator with tcgen05.ld, clamp at 1e-30 (src/correlations.jl:203)
+// and accumulate Sp = sum p and Sql = sum q~ log p with the folded histogram q~, so
+// c3 never reaches global memory.  Every mbarrier wait is bounded; on timeout the
+// kernel records TP3_ERR_TIMEOUT in *err, skips the remaining work and frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/tp3.h"
+#include "internal.h"
+
+namespace tp3 {
+
+// ---------------------------------------------------------------------------
+// Stage (a): pair-factorised coupling
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ int ki_index(int k1, int k2, int k3) {
+  return k1 * (k1 + 1) * (k1 + 2) / 6 + k2 * (k2 + 1) / 2 + k3;
+}
+
+// grid: (n_pb, K, n); block 256; dyn smem = (K*nc + K*SDmax) float2.
+// T_hi / T_lo: [prop][klp][KP] bf16; T32 (optional): [prop][klp][n_ltp] fp32.
+template <int MAXS>
+__global__ void __launch_bounds__(256) k_couple_pair(
+    const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff,
+    const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
+    int klp, int KP, __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo,
+    float* __restrict__ T32, int ldT32) {
+  extern __shared__ float2 sm[];
+  const int prop = blockIdx.z;
+  const int k1 = K - 1 - (int)blockIdx.y;  // large shells first
+  const PairBlock pb = pbs[blockIdx.x];
+  const int nk = k1 + 1;
+  float2* sc = sm;                       // [nk][nc]
+  float2* sD = sm + (size_t)nk * nc;     // [nk][SD]
+  const float2* src = cc + (size_t)prop * K * nc;
+  for (int i = threadIdx.x; i < nk * nc; i += blockDim.x) sc[i] = src[i];
+  __syncthreads();
+
+  const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, l3min = pb.l3min, M = pb.M, SD = pb.SD;
+  const float2* c1 = sc + (size_t)k1 * nc + coff[l1 >> 1] + l1;  // index by m1
+  const int off2 = coff[l2 >> 1] + l2;
+  // phase 1: D[k2][s][m3]
+  const int items1 = nk * (2 * M + 1);
+  for (int it = threadIdx.x; it < items1; it += blockDim.x) {
+    const int e = it / nk, k2 = it - e * nk;
+    const int m3 = e - M;
+    const int m1lo = max(-l1, -l2 - m3), m1hi = min(l1, l2 - m3);
+    const float* wp = wtab + pb.wofs + eofs[pb.eofs + e];
+    const float2* c2 = sc + (size_t)k2 * nc + off2;
+    float ar[MAXS], ai[MAXS];
+#pragma unroll
+    for (int s = 0; s < MAXS; ++s) { ar[s] = 0.f; ai[s] = 0.f; }
+    for (int m1 = m1lo; m1 <= m1hi; ++m1) {
+      const float2 a = c1[m1];
+      const float2 b = c2[-m3 - m1];
+      const float xr = a.x * b.x - a.y * b.y;
+      const float xi = a.x * b.y + a.y * b.x;
+      const float* wr = wp + (m1 - m1lo) * nl3;
+#pragma unroll
+      for (int s = 0; s < MAXS; ++s) {
+        if (s < nl3) {
+          const float wv = wr[s];
+          ar[s] = fmaf(wv, xr, ar[s]);
+          ai[s] = fmaf(wv, xi, ai[s]);
+        }
+      }
+    }
+    float2* d = sD + (size_t)k2 * SD;
+    int dofs = 0;
+#pragma unroll
+    for (int s = 0; s < MAXS; ++s) {
+      if (s < nl3) {
+        const int l3 = l3min + 2 * s;
+        if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
+        dofs += 2 * l3 + 1;
+      }
+    }
+  }
+  __syncthreads();
+
+  // phase 2: 2 x 2 tiles over (k2, k3), k3 <= k2 <= k1, for every l3
+  const int nb = (nk + 1) >> 1;
+  const int tiles = nb * (nb + 1) / 2;
+  const int items2 = tiles * nl3;
+  __nv_bfloat16* th = Thi + (size_t)prop * klp * KP;
+  __nv_bfloat16* tl = Tlo + (size_t)prop * klp * KP;
+  for (int it = threadIdx.x; it < items2; it += blockDim.x) {
+    const int s = it / tiles;
+    int t = it - s * tiles;
+    int rb = 0;
+    while (t > rb) { t -= rb + 1; ++rb; }  // lower-triangular tile (rb, cb = t)
+    const int cb = t;
+    const int l3 = l3min + 2 * s;
+    int dofs = 0;
+    for (int q = 0; q < s; ++q) dofs += 2 * (l3min + 2 * q) + 1;
+    const int k2a = 2 * rb, k2b = 2 * rb + 1, k3a = 2 * cb, k3b = 2 * cb + 1;
+    const bool v2b = k2b < nk, v3b = k3b < nk;
+    const float2* da = sD + (size_t)k2a * SD + dofs + l3;
+    const float2* db = sD + (size_t)(v2b ? k2b : k2a) * SD + dofs + l3;
+    const int off3 = coff[l3 >> 1] + l3;
+    const float2* ca = sc + (size_t)k3a * nc + off3;
+    const float2* cbp = sc + (size_t)(v3b ? k3b : k3a) * nc + off3;
+    float t00 = 0.f, t01 = 0.f, t10 = 0.f, t11 = 0.f;
+    for (int m3 = -l3; m3 <= l3; ++m3) {
+      const float2 x0 = da[m3], x1 = db[m3], y0 = ca[m3], y1 = cbp[m3];
+      t00 = fmaf(x0.x, y0.x, fmaf(-x0.y, y0.y, t00));
+      t01 = fmaf(x0.x, y1.x, fmaf(-x0.y, y1.y, t01));
+      t10 = fmaf(x1.x, y0.x, fmaf(-x1.y, y0.y, t10));
+      t11 = fmaf(x1.x, y1.x, fmaf(-x1.y, y1.y, t11));
+    }
+    const int lt = pb.lt_base + s;
+    const float vals[4] = {t00, t01, t10, t11};
+    const int k2s[4] = {k2a, k2a, k2b, k2b}, k3s[4] = {k3a, k3b, k3a, k3b};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k2 = k2s[q], k3 = k3s[q];
+      if (k2 < nk && k3 <= k2) {
+        const int ki = ki_index(k1, k2, k3);
+        const float v = vals[q];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+        th[(size_t)ki * KP + lt] = hi;
+        tl[(size_t)ki * KP + lt] = lo;
+        if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Stage (b)+(c): tcgen05 angular contraction + fused Bayes epilogue
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kStages = 4;
+constexpr int kBK = 32;                       // K elements per stage (64 bytes of bf16)
+constexpr int kBM = 128;                      // shell triples per CTA (TMEM lanes)
+constexpr int kBN = 256;                      // grid columns per MMA (one TMEM half)
+constexpr int kABytes = kBM * kBK * 2;        // 8 KB
+constexpr int kBBytes = kBN * kBK * 2;        // 16 KB
+constexpr int kStageBytes = 2 * kABytes + 2 * kBBytes;  // 48 KB
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // producer warp, MMA warp, 8 epilogue warps
+constexpr long long kTimeoutCycles = 4000000000LL;  // about 2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false (and records the timeout) when the limit is hit or
+// another thread of the CTA already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kTimeoutCycles) {
+      *abort_flag = 1;
+      atomicExch(err, TP3_ERR_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// K-major operand, 64-byte swizzle: 8-row atoms of 512 bytes, SBO = 512 B.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;                 // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(512u >> 4) << 32;        // SBO
+  d |= (uint64_t)1u << 46;                 // descriptor version (sm_100 family)
+  d |= (uint64_t)4u << 61;                 // SWIZZLE_64B
+  return d;
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both K-major, M = 128, N = 256.
+__host__ __device__ constexpr uint32_t idesc_bf16_m128_n256() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcSmemHeader {
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
+  uint64_t tmem_full[2];
+  uint32_t tmem_base;
+  int abort_flag;
+  float part_sp[2][kBM];
+  float part_sq[2][kBM];
+};
+
+// grid: (klp / 128, n); block kThreads; dyn smem = 1 KB alignment slack + stages + header.
+// STORE: write c3 (all four images of every unique point) instead of the Bayes terms.
+template <bool STORE>
+__global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
+    const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
+    const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
+    int Gu, int nhalf, int klength, const float* __restrict__ qt, const double* __restrict__ Qs,
+    const double* __restrict__ tf, int mult, double* __restrict__ Eslab, float* __restrict__ c3out,
+    const int* __restrict__ u_to_g, int N, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stages = base;
+  TcSmemHeader* hd = (TcSmemHeader*)(base + kStages * kStageBytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int prop = blockIdx.y;
+  const int mtile = blockIdx.x;
+  const int row0 = prop * klp + mtile * kBM;  // row coordinate in the A tensor
+  const int nk = KP / kBK;
+  const uint32_t tcols = nhalf == 2 ? 512u : 256u;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&hd->full[s], 1);
+      mbar_init(&hd->empty[s], 1);
+    }
+    mbar_init(&hd->tmem_full[0], 1);
+    mbar_init(&hd->tmem_full[1], 1);
+    hd->abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&hd->tmem_base)),
+                 "r"(tcols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = hd->tmem_base;
+  volatile int* abort_flag = &hd->abort_flag;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      int last[kStages];
+#pragma unroll
+      for (int s = 0; s < kStages; ++s) last[s] = -1;
+      for (int h = 0; h < nhalf && !*abort_flag; ++h) {
+        for (int kc = 0; kc < nk; ++kc, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)((it / kStages) & 1);
+          if (!mbar_wait(&hd->empty[s], ph ^ 1u, abort_flag, err)) break;
+          last[s] = it;
+          uint8_t* st = stages + s * kStageBytes;
+          mbar_expect_tx(&hd->full[s], kStageBytes);
+          tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kBK, row0);
+          tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kBK, row0);
+          tma_load_2d(st + 2 * kABytes, &tmB_hi, &hd->full[s], kc * kBK, h * kBN);
+          tma_load_2d(st + 2 * kABytes + kBBytes, &tmB_lo, &hd->full[s], kc * kBK, h * kBN);
+        }
+      }
+      if (*abort_flag) {
+        // let this CTA's copies in flight land before its shared memory is released
+        for (int s = 0; s < kStages; ++s) {
+          if (last[s] < 0) continue;
+          const long long t0 = clock64();
+          while (!mbar_try_wait(&hd->full[s], (uint32_t)((last[s] / kStages) & 1)) &&
+                 clock64() - t0 < kTimeoutCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_m128_n256();
+      int it = 0;
+      for (int h = 0; h < nhalf && !*abort_flag; ++h) {
+        const uint32_t dt = tmem + (uint32_t)(h * kBN);
+        for (int kc = 0; kc < nk; ++kc, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)((it / kStages) & 1);
+          if (!mbar_wait(&hd->full[s], ph, abort_flag, err)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(stages + s * kStageBytes);
+          const uint64_t ahi = smem_desc_sw64(st), alo = smem_desc_sw64(st + kABytes);
+          const uint64_t bhi = smem_desc_sw64(st + 2 * kABytes), blo = smem_desc_sw64(st + 2 * kABytes + kBBytes);
+#pragma unroll
+          for (int ks = 0; ks < kBK / 16; ++ks) {
+            const uint64_t dk = (uint64_t)(ks * 32 / 16);  // +32 bytes per K=16 step, in 16-byte units
+            mma_bf16(dt, ahi + dk, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+            mma_bf16(dt, ahi + dk, blo + dk, idesc, 1u);
+            mma_bf16(dt, alo + dk, bhi + dk, idesc, 1u);
+          }
+          mma_commit(&hd->empty[s]);
+        }
+        mma_commit(&hd->tmem_full[h]);
+      }
+    }
+  } else {
+    // ---------------- epilogue: 8 warps ----------------
+    const int ew = warp - 2;
+    const int quarter = warp & 3;           // TMEM lane quarter this warp may access
+    const int cblk = ew >> 2;               // which 128-column block of each half
+    const int r = quarter * 32 + lane;      // row inside the tile
+    const int ki = mtile * kBM + r;
+    float sp = 0.f, sq = 0.f;
+    for (int h = 0; h < nhalf; ++h) {
+      if (!mbar_wait(&hd->tmem_full[h], 0u, abort_flag, err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int cc = 0; cc < 4; ++cc) {
+        const int col = h * kBN + cblk * 128 + cc * 32;
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col, v);
+        if (STORE) {
+          if (ki < klength) {
+            float* o = c3out + ((size_t)prop * klength + ki) * (size_t)(2 * N * N);
+#pragma unroll 4
+            for (int j = 0; j < 32; ++j) {
+              const int u = col + j;
+              if (u < Gu) {
+                const int g = u_to_g[u];
+                const int a = g % N, b = g / N;
+                o[g] = v[j];
+                if (mult == 4) {
+                  o[a + N * (b + N)] = v[j];
+                  o[(N - 1 - a) + N * (N - 1 - b)] = v[j];
+                  o[(N - 1 - a) + N * (2 * N - 1 - b)] = v[j];
+                }
+              }
+            }
+          }
+        } else {
+          const float* qrow = qt + ((size_t)mtile * Gu) * kBM + r;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int u = col + j;
+            if (u < Gu) {
+              const float p = fmaxf(v[j], 1e-30f);
+              sp += p;
+              sq = fmaf(qrow[(size_t)u * kBM], __logf(p), sq);
+            }
+          }
+        }
+      }
+    }
+    if (!STORE) {
+      hd->part_sp[cblk][r] = sp;
+      hd->part_sq[cblk][r] = sq;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (!STORE && warp >= 2 && warp < 6) {
+    const int r = (warp & 3) * 32 + lane;
+    const int ki = mtile * kBM + r;
+    if (ki < klength && !*abort_flag) {
+      const double Sp = (double)hd->part_sp[0][r] + (double)hd->part_sp[1][r];
+      const double Sq = (double)hd->part_sq[0][r] + (double)hd->part_sq[1][r];
+      Eslab[(size_t)prop * klength + ki] = tf[ki] * (Qs[ki] * log((double)mult * Sp) - Sq);
+    }
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols) : "memory");
+  }
+}
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// grid: n; block 256.  Deterministic compensated sum of per-slab energies.
+__global__ void __launch_bounds__(256) k_finalize_slabs(const double* __restrict__ Eslab, int klength,
+                                                        double* __restrict__ E) {
+  __shared__ double ss[256], sc[256];
+  const int prop = blockIdx.x;
+  const double* e = Eslab + (size_t)prop * klength;
+  double s = 0.0, c = 0.0;
+  for (int ki = threadIdx.x; ki < klength; ki += blockDim.x) {
+    double t, err;
+    two_sum(s, e[ki], t, err);
+    s = t;
+    c += err;
+  }
+  ss[threadIdx.x] = s;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      double t, err;
+      two_sum(ss[threadIdx.x], ss[threadIdx.x + h], t, err);
+      ss[threadIdx.x] = t;
+      sc[threadIdx.x] += sc[threadIdx.x + h] + err;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) E[prop] = ss[0] + sc[0];
+}
+
+}  // namespace
+
+size_t tc_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(TcSmemHeader); }
+
+cudaError_t tc_configure() {
+  cudaError_t e;
+  const int smem = (int)tc_smem_bytes();
+  if ((e = cudaFuncSetAttribute(k_angular_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_angular_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+    return e;
+  const int cs = 227 * 1024;
+  if ((e = cudaFuncSetAttribute(k_couple_pair<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_pair<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_pair<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_pair<13>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
+    return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc,
+                               __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s) {
+  const size_t smem = (size_t)t.K * (t.nc + tc.SDmax) * sizeof(float2);
+  dim3 grid(tc.n_pb, t.K, n);
+  if (tc.maxs <= 4)
+    k_couple_pair<4><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
+                                             Tlo, T32, t.n_ltp);
+  else if (tc.maxs <= 7)
+    k_couple_pair<7><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
+                                             Tlo, T32, t.n_ltp);
+  else if (tc.maxs <= 10)
+    k_couple_pair<10><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
+                                              Tlo, T32, t.n_ltp);
+  else
+    k_couple_pair<13><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
+                                              Tlo, T32, t.n_ltp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
+                              const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s) {
+  dim3 grid(t.klp / kBM, n);
+  const size_t smem = tc_smem_bytes();
+  if (c3out)
+    k_angular_tc<true><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu,
+                                                    tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out,
+                                                    t.u_to_g, t.N, err);
+  else
+    k_angular_tc<false><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP,
+                                                     t.Gu, tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab,
+                                                     nullptr, t.u_to_g, t.N, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s) {
+  k_finalize_slabs<<<n, 256, 0, s>>>(Eslab, klength, E);
+  return cudaGetLastError();
+}
+
+}  // namespace tp3

@@ -115,8 +115,10 @@ class BasisTypeGB300:
         check(self._lib.tp3_get_mode(self._ctx, ctypes.byref(m)), self._ctx)
         return m.value
 
-    def set_stream(self, stream_ptr: int) -> None:
-        check(self._lib.tp3_set_stream(self._ctx, ctypes.c_void_p(stream_ptr)), self._ctx)
+    def set_stream(self, stream_ptr) -> None:
+        """Launch on this cudaStream_t handle; None restores the context's own stream."""
+        check(self._lib.tp3_set_stream(self._ctx, None if stream_ptr is None else ctypes.c_void_p(stream_ptr)),
+              self._ctx)
 
     def reserve(self, n: int) -> None:
         check(self._lib.tp3_reserve(self._ctx, n), self._ctx)
@@ -163,6 +165,16 @@ class BasisTypeGB300:
         out = np.empty((self.klength, 2 * self.N * self.N), dtype=np.float32)
         check(self._lib.tp3_c3(self._ctx, cc.ctypes.data, out.ctypes.data), self._ctx)
         return out.T  # [G, klength]
+
+    def triple_products(self, coeff: np.ndarray) -> np.ndarray:
+        """T[ki, lt] (klength x n_lt, float32) from the current mode's coupling kernel."""
+        cc = self.pack(coeff)
+        out = np.empty((self.klength, self.n_lt), dtype=np.float32)
+        check(self._lib.tp3_triple_products(self._ctx, cc.ctypes.data, out.ctypes.data), self._ctx)
+        return out
+
+    def sync(self) -> None:
+        check(self._lib.tp3_sync(self._ctx), self._ctx)
 
     def energy_batch(self, coeffs: np.ndarray) -> np.ndarray:
         """Energies of a batch of coefficient sets, complex128 [n, >=K, LMAX^2]."""
