@@ -43,6 +43,28 @@ def test_triple_products_config1(basis1, config1, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("kind", ["general", "real_function"])
+def test_triple_products_random(basis1, config1, mode, kind):
+    """Stage (a) on random coefficients: arbitrary complex ones (general path) and ones
+    of a real function, c[l,-m] = (-1)^m conj(c[l,m]) (the symmetric path)."""
+    basis1.set_mode(mode)
+    p = config1["params"]
+    LMAX = p["LMAX"]
+    rng = np.random.default_rng(11)
+    c = rng.normal(size=(p["K"], LMAX * LMAX)) + 1j * rng.normal(size=(p["K"], LMAX * LMAX))
+    if kind == "real_function":
+        from tp3.structure import seanindex0
+        for l in range(LMAX):
+            c[:, seanindex0(l, 0, LMAX)] = c[:, seanindex0(l, 0, LMAX)].real
+            for m in range(1, l + 1):
+                c[:, seanindex0(l, -m, LMAX)] = (-1) ** m * np.conj(c[:, seanindex0(l, m, LMAX)])
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    T64 = triple_products(b, c)
+    T = basis1.triple_products(c).astype(np.float64)
+    assert np.max(np.abs(T - T64)) / np.abs(T64).max() < 2e-5
+
+
+@pytest.mark.parametrize("mode", MODES)
 def test_c3_config1(basis1, config1, mode):
     basis1.set_mode(mode)
     vol = tp3.SphericalHarmonicsVolume(config1["coeff"], 9, 8, 8.0)

@@ -69,6 +69,7 @@ struct tp3_ctx {
   double* d_E = nullptr;       // [cap]
   float* d_c3 = nullptr;       // [klength][G] (one proposal)
   int* d_err = nullptr;        // device error flag (timeouts)
+  int* d_sym = nullptr;        // [cap] real-function symmetry flag per proposal
   double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
   double* h_E = nullptr;       // pinned [cap]
   int* h_err = nullptr;        // pinned
@@ -127,6 +128,7 @@ std::string build_tc_tables(const Basis& b, std::vector<PairBlock>& pbs, std::ve
         else if (f->second != pb.lt_base + s) return "pair block l-triples are not consecutive";
         pb.SD += 2 * l3 + 1;
       }
+      pb.nl3p = (pb.nl3 + 1) / 2 * 2;
       int run = 0;
       for (int e = 0; e <= 2 * pb.M; ++e) {
         const int m3 = e - pb.M;
@@ -134,13 +136,15 @@ std::string build_tc_tables(const Basis& b, std::vector<PairBlock>& pbs, std::ve
         const int m1lo = std::max(-l1, -l2 - m3), m1hi = std::min(l1, l2 - m3);
         for (int m1 = m1lo; m1 <= m1hi; ++m1) {
           const int m2 = -m3 - m1;
-          for (int s = 0; s < pb.nl3; ++s) {
+          for (int s = 0; s < pb.nl3p; ++s) {
             const int l3 = l3min + 2 * s;
-            it.w.push_back(std::abs(m3) <= l3 ? (float)tp3::wigner3j(l1, l2, l3, m1, m2, m3) : 0.f);
+            it.w.push_back(s < pb.nl3 && std::abs(m3) <= l3 ? (float)tp3::wigner3j(l1, l2, l3, m1, m2, m3) : 0.f);
           }
-          run += pb.nl3;
+          run += pb.nl3p;
         }
       }
+      while (run % 4) { it.w.push_back(0.f); ++run; }  // block length: whole float4s
+      pb.wcount = run;
       it.work = (double)run;
       maxs = std::max(maxs, pb.nl3);
       SDmax = std::max(SDmax, pb.SD);
@@ -148,7 +152,7 @@ std::string build_tc_tables(const Basis& b, std::vector<PairBlock>& pbs, std::ve
     }
   std::sort(items.begin(), items.end(), [](const Item& a, const Item& c) { return a.work > c.work; });
   for (auto& it : items) {
-    it.pb.wofs = (int)wtab.size();
+    it.pb.wofs = (int)wtab.size();  // multiple of 4: every block starts on a 16-byte boundary
     it.pb.eofs = (int)eofs.size();
     wtab.insert(wtab.end(), it.w.begin(), it.w.end());
     eofs.insert(eofs.end(), it.e.begin(), it.e.end());
@@ -182,11 +186,45 @@ std::string setup_tc(tp3_ctx* c) {
   int maxs = 0, SDmax = 0;
   std::string m = build_tc_tables(b, pbs, eofs, wtab, maxs, SDmax);
   if (!m.empty()) return m;
-  if (maxs > 13) return "more than 13 l3 values per pair block (L > 24)";
-  if ((size_t)b.K * (b.nc + SDmax) * sizeof(float2) > 227 * 1024) return "coupling tile exceeds shared memory";
+  if (maxs > 16) return "more than 16 l3 values per pair block (L > 30)";
+  for (const auto& pb : pbs)
+    if (pb.wofs % 4 != 0 || pb.wcount % 4 != 0 || pb.nl3p % 2 != 0) return "3j block alignment invariant violated";
+  for (int v : eofs)
+    if (v % 2 != 0) return "3j row alignment invariant violated";
   tc.n_pb = (int)pbs.size();
   tc.maxs = maxs;
   tc.SDmax = SDmax;
+  // coupling kernel shared memory: coefficients [K][ncp], 3j block, D [pmax][SDp]
+  tc.ncp = b.nc | 1;
+  tc.SDp = SDmax | 1;
+  int wmax = 0;
+  for (const auto& pb : pbs) wmax = std::max(wmax, pb.wcount);
+  tc.wsmem = wmax;
+  const size_t limit = 227 * 1024 - 1024;
+  // coefficient block rounded up to 16 bytes so the 3j block (float4 copies) stays aligned
+  const size_t base = ((size_t)b.K * tc.ncp * sizeof(float2) + 15) / 16 * 16;
+  // D is double-buffered: two chunks of up to pmax shell pairs
+  int pmax = std::max(b.K, 128);
+  tc.w_smem = true;
+  auto need = [&](int pm, bool ws) {
+    return base + (ws ? (size_t)wmax * 4 : 0) + 2 * (size_t)pm * tc.SDp * sizeof(float2);
+  };
+  while (need(pmax, true) > limit && pmax > b.K) --pmax;
+  if (need(pmax, true) > limit) { tc.w_smem = false; pmax = std::max(b.K, 128); }
+  while (need(pmax, false) > limit && pmax > b.K) --pmax;
+  if (need(pmax, tc.w_smem) > limit) return "coupling tile exceeds shared memory";
+  tc.pmax = pmax;
+  tc.couple_smem = need(pmax, tc.w_smem);
+  // chunks of whole k1 values, largest shells first, at most pmax shell pairs each
+  std::vector<int2> chunks;
+  for (int k1 = b.K - 1; k1 >= 0;) {
+    int hi = k1, cnt = 0;
+    while (k1 >= 0 && cnt + k1 + 1 <= pmax) { cnt += k1 + 1; --k1; }
+    chunks.push_back(make_int2(hi, k1 + 1));
+  }
+  tc.nchunks = (int)chunks.size();
+  std::vector<int> cmir(b.nc);
+  for (int i = 0; i < b.nc; ++i) cmir[i] = b.coff[b.c_l[i] / 2] + b.c_l[i] - b.c_m[i];
   tc.KP = (b.n_lt() + 31) / 32 * 32;
   tc.nhalf = (b.Gu + 255) / 256;
   tc.NP = 256 * tc.nhalf;
@@ -210,6 +248,8 @@ std::string setup_tc(tp3_ctx* c) {
   cudaError_t e;
   if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
       (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
+      (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
+      (e = upload(c, cmir, &tc.cmir)) != cudaSuccess ||
       (e = upload(c, Fhi, &tc.Fhi)) != cudaSuccess || (e = upload(c, Flo, &tc.Flo)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
@@ -223,8 +263,9 @@ std::string setup_tc(tp3_ctx* c) {
 // ---- scratch ------------------------------------------------------------------
 void free_scratch(tp3_ctx* c) {
   cudaFree(c->d_coeff); cudaFree(c->d_cc); cudaFree(c->d_T); cudaFree(c->d_part); cudaFree(c->d_E);
-  cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab);
+  cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab); cudaFree(c->d_sym);
   cudaFreeHost(c->h_coeff); cudaFreeHost(c->h_E);
+  c->d_sym = nullptr;
   c->d_coeff = nullptr; c->d_cc = nullptr; c->d_T = nullptr; c->d_part = nullptr; c->d_E = nullptr;
   c->d_Thi = nullptr; c->d_Tlo = nullptr; c->d_Eslab = nullptr;
   c->h_coeff = nullptr; c->h_E = nullptr;
@@ -248,6 +289,7 @@ int ensure_cap(tp3_ctx* c, int n) {
       (c->tc_ok && (e = cudaMalloc(&c->d_Thi, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * t.klength * sizeof(double))) != cudaSuccess) ||
+      (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_coeff, (size_t)n * t.K * ncoef * 2 * sizeof(double))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_E, (size_t)n * sizeof(double))) != cudaSuccess) {
     free_scratch(c);
@@ -282,15 +324,18 @@ int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) {
   return 1;
 }
 
-// Coupling stage for n proposals whose compact coefficients are in d_cc.
-int run_coupling(tp3_ctx* c, int n, bool want_T32) {
+// Gather + coupling stage for n proposals whose FP64 coefficients are in d_coeff.
+int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32) {
   const auto& t = c->t;
   cudaError_t e;
   if (c->mode == TP3_MODE_TC_BF16X3) {
-    if ((e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_Thi, c->d_Tlo, want_T32 ? c->d_T : nullptr,
-                                     c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "gather_sym");
+    if ((e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo,
+                                     want_T32 ? c->d_T : nullptr, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "couple_pair");
   } else {
+    if ((e = tp3::launch_gather(t, n, d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
     if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "couple_direct");
   }
@@ -302,8 +347,7 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E) {
   const auto& t = c->t;
   cudaError_t e;
   if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
-  if ((e = tp3::launch_gather(t, n, d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
-  if (int r = run_coupling(c, n, false)) return r;
+  if (int r = run_coupling(c, n, d_coeff, false)) return r;
   cudaEvent_t a, b;
   int pr = prof_begin(c, &a, &b);
   if (c->mode == TP3_MODE_TC_BF16X3) {
@@ -593,8 +637,7 @@ int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {
   std::memcpy(c->h_coeff, coeff, nco * 2 * sizeof(double));
   if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "H2D coeff");
-  if ((e = tp3::launch_gather(t, 1, c->d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
-  if (int r = run_coupling(c, 1, false)) return r;
+  if (int r = run_coupling(c, 1, c->d_coeff, false)) return r;
   if (c->mode == TP3_MODE_TC_BF16X3)
     e = tp3::launch_angular_tc(t, c->tc, c->maps, 1, nullptr, nullptr, nullptr, c->d_c3, c->d_err, c->stream);
   else
@@ -617,8 +660,7 @@ int tp3_triple_products(tp3_ctx* c, const double* coeff, float* out) {
   std::memcpy(c->h_coeff, coeff, nco * 2 * sizeof(double));
   if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "H2D coeff");
-  if ((e = tp3::launch_gather(t, 1, c->d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
-  if (int r = run_coupling(c, 1, true)) return r;
+  if (int r = run_coupling(c, 1, c->d_coeff, true)) return r;
   if ((e = cudaMemcpy2DAsync(out, t.n_lt * sizeof(float), c->d_T, t.n_ltp * sizeof(float), t.n_lt * sizeof(float),
                              t.klength, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)

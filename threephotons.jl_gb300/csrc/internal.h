@@ -39,13 +39,21 @@ struct PairBlock {
   int M;                   // |m3| <= M
   int SD;                  // sum_s (2 l3_s + 1)
   int lt_base;             // l-triple index of (l1, l2, l3min); the block's l-triples are consecutive
-  int wofs;                // offset of the block in wtab
+  int wofs;                // offset of the block in wtab (16-byte aligned)
   int eofs;                // offset of the block's per-m3 table in eofs[]
+  int nl3p;                // nl3 rounded up to 4 (row length of the 3j table)
+  int wcount;              // floats in the block's 3j table (multiple of 4)
 };
 
 // Device tables of the tensor-core path.
 struct TcTables {
   int n_pb = 0, maxs = 0, SDmax = 0;
+  int ncp = 0, SDp = 0, pmax = 0, nchunks = 0, wsmem = 0;  // coupling kernel shared-memory layout
+  bool w_smem = false;
+  size_t couple_smem = 0;
+  const int2* chunks = nullptr;  // (k1 high, k1 low) runs of shells, pairs per run <= pmax
+  const int* cm = nullptr;       // [nc] m of each compact coefficient
+  const int* cmir = nullptr;     // [nc] compact index of (l, -m)
   int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
   int NP = 0, nhalf = 0;   // unique grid points padded to 256 * nhalf
   const int* coff = nullptr;
@@ -62,7 +70,9 @@ struct TcMaps {
 
 size_t tc_smem_bytes();
 cudaError_t tc_configure();
-cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc,
+cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, float2* cc,
+                              int* sym, cudaStream_t s);
+cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
                               const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s);

@@ -42,111 +42,237 @@ __device__ __forceinline__ int ki_index(int k1, int k2, int k3) {
   return k1 * (k1 + 1) * (k1 + 2) / 6 + k2 * (k2 + 1) / 2 + k3;
 }
 
-// grid: (n_pb, K, n); block 256; dyn smem = (K*nc + K*SDmax) float2.
-// T_hi / T_lo: [prop][klp][KP] bf16; T32 (optional): [prop][klp][n_ltp] fp32.
-template <int MAXS>
-__global__ void __launch_bounds__(256) k_couple_pair(
-    const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff,
-    const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
-    int klp, int KP, __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo,
-    float* __restrict__ T32, int ldT32) {
-  extern __shared__ float2 sm[];
-  const int prop = blockIdx.z;
-  const int k1 = K - 1 - (int)blockIdx.y;  // large shells first
-  const PairBlock pb = pbs[blockIdx.x];
-  const int nk = k1 + 1;
-  float2* sc = sm;                       // [nk][nc]
-  float2* sD = sm + (size_t)nk * nc;     // [nk][SD]
-  const float2* src = cc + (size_t)prop * K * nc;
-  for (int i = threadIdx.x; i < nk * nc; i += blockDim.x) sc[i] = src[i];
-  __syncthreads();
-
-  const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, l3min = pb.l3min, M = pb.M, SD = pb.SD;
-  const float2* c1 = sc + (size_t)k1 * nc + coff[l1 >> 1] + l1;  // index by m1
-  const int off2 = coff[l2 >> 1] + l2;
-  // phase 1: D[k2][s][m3]
-  const int items1 = nk * (2 * M + 1);
-  for (int it = threadIdx.x; it < items1; it += blockDim.x) {
-    const int e = it / nk, k2 = it - e * nk;
-    const int m3 = e - M;
-    const int m1lo = max(-l1, -l2 - m3), m1hi = min(l1, l2 - m3);
-    const float* wp = wtab + pb.wofs + eofs[pb.eofs + e];
-    const float2* c2 = sc + (size_t)k2 * nc + off2;
-    float ar[MAXS], ai[MAXS];
-#pragma unroll
-    for (int s = 0; s < MAXS; ++s) { ar[s] = 0.f; ai[s] = 0.f; }
-    for (int m1 = m1lo; m1 <= m1hi; ++m1) {
-      const float2 a = c1[m1];
-      const float2 b = c2[-m3 - m1];
-      const float xr = a.x * b.x - a.y * b.y;
-      const float xi = a.x * b.y + a.y * b.x;
-      const float* wr = wp + (m1 - m1lo) * nl3;
-#pragma unroll
-      for (int s = 0; s < MAXS; ++s) {
-        if (s < nl3) {
-          const float wv = wr[s];
-          ar[s] = fmaf(wv, xr, ar[s]);
-          ai[s] = fmaf(wv, xi, ai[s]);
-        }
-      }
+// Coefficients of a real function satisfy c[l,-m] = (-1)^m conj(c[l,m]) (intensities
+// are real; the reference's moves rtc * R * ctr with real orthogonal R preserve it).
+// grid: n; block 256.  Converts one proposal's FP64 seanindex-ordered coefficients to
+// the compact FP32 layout and sets sym[prop] = 1 when every shell satisfies the
+// relation to 1e-10 of the shell's largest coefficient; the m < 0 entries are then
+// rebuilt from m >= 0 so the relation holds exactly in FP32.
+__global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, const int* __restrict__ csean,
+                                                    const int* __restrict__ cm, const int* __restrict__ cmir,
+                                                    const double2* __restrict__ coeff, float2* __restrict__ cc,
+                                                    int* __restrict__ sym) {
+  const int prop = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const double2* cp = coeff + (size_t)prop * K * ncoef;
+  int ok = 1;
+  for (int k = warp; k < K; k += nw) {
+    const double2* ck = cp + (size_t)k * ncoef;
+    double amax = 0.0;
+    for (int c = lane; c < nc; c += 32) {
+      const double2 a = ck[csean[c]];
+      amax = fmax(amax, fabs(a.x) + fabs(a.y));
     }
-    float2* d = sD + (size_t)k2 * SD;
-    int dofs = 0;
-#pragma unroll
-    for (int s = 0; s < MAXS; ++s) {
-      if (s < nl3) {
-        const int l3 = l3min + 2 * s;
-        if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
-        dofs += 2 * l3 + 1;
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    const double tol = 1e-10 * amax;
+    for (int c = lane; c < nc; c += 32) {
+      const int m = cm[c];
+      if (m < 0) continue;
+      const double2 a = ck[csean[c]];
+      if (m == 0) {
+        ok &= fabs(a.y) <= tol;
+      } else {
+        const double2 b = ck[csean[cmir[c]]];
+        const double sg = (m & 1) ? -1.0 : 1.0;
+        ok &= fabs(b.x - sg * a.x) + fabs(b.y + sg * a.y) <= tol;
       }
     }
   }
-  __syncthreads();
+  const int s = __syncthreads_and(ok);
+  float2* out = cc + (size_t)prop * K * nc;
+  for (int i = threadIdx.x; i < K * nc; i += blockDim.x) {
+    const int k = i / nc, c = i - k * nc;
+    const int m = cm[c];
+    const double2* ck = cp + (size_t)k * ncoef;
+    float2 v;
+    if (s && m < 0) {
+      const double2 a = ck[csean[cmir[c]]];
+      const double sg = (m & 1) ? -1.0 : 1.0;
+      v = make_float2((float)(sg * a.x), (float)(-sg * a.y));
+    } else {
+      const double2 a = ck[csean[c]];
+      v = make_float2((float)a.x, (s && m == 0) ? 0.f : (float)a.y);
+    }
+    out[i] = v;
+  }
+  if (threadIdx.x == 0) sym[prop] = s;
+}
 
-  // phase 2: 2 x 2 tiles over (k2, k3), k3 <= k2 <= k1, for every l3
-  const int nb = (nk + 1) >> 1;
-  const int tiles = nb * (nb + 1) / 2;
-  const int items2 = tiles * nl3;
+// One CTA = one (l1, l2) pair block of one proposal; it loops over chunks of shell
+// pairs (k1, k2 <= k1), each chunk a run of whole k1 values.
+// Shared memory: coefficients [K][ncp] (ncp odd: conflict-free strided float2 reads),
+// the block's 3j table [e][m1][nl3p] (when W_SMEM), and D [pairs in chunk][SDp].
+// Phase 1: item = (m3, pair); the lanes of a warp share m3, so they share the m1
+//          range and read the 3j values as broadcasts.
+// Phase 2: item = (k1, l3, 4 x 4 tile of (k2, k3)) with k3 <= k2.
+// grid: (n_pb, n); block kCoupleThreads.
+constexpr int kCoupleThreads = 512;
+
+template <int MAXS, bool W_SMEM>
+__global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
+    const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
+    const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
+    const int2* __restrict__ chunks, int nchunks, int pmax, int SDp, int wsmem, int klp, int KP,
+    const int* __restrict__ symflags, __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo,
+    float* __restrict__ T32, int ldT32) {
+  extern __shared__ __align__(16) float smf[];
+  const int prop = blockIdx.y;
+  // real-function coefficients: only m3 >= 0 of D is formed, D[-m3] = (-1)^m3 conj(D[m3])
+  // and T = Re(D[0] c[0]) + 2 sum_{m3 > 0} Re(D[m3] c[m3])
+  const bool sym = symflags[prop] != 0;
+  const PairBlock pb = pbs[blockIdx.x];
+  float2* sc = reinterpret_cast<float2*>(smf);                 // [K][ncp]
+  float* sw = smf + (2 * (size_t)K * ncp + 3) / 4 * 4;          // [wsmem], 16-byte aligned
+  float2* sD = reinterpret_cast<float2*>(sw + (W_SMEM ? wsmem : 0));  // [pmax][SDp]
+  const float2* src = cc + (size_t)prop * K * nc;
+  for (int i = threadIdx.x; i < K * nc; i += blockDim.x) {
+    const int k = i / nc, c = i - k * nc;
+    sc[k * ncp + c] = src[i];
+  }
+  const float* wblk = wtab + pb.wofs;
+  if (W_SMEM) {
+    const float4* w4 = reinterpret_cast<const float4*>(wblk);
+    float4* s4 = reinterpret_cast<float4*>(sw);
+    for (int i = threadIdx.x; i < pb.wcount / 4; i += blockDim.x) s4[i] = w4[i];
+  }
+  __syncthreads();
+  const float* wsrc = W_SMEM ? sw : wblk;
+
+  const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, nl3p = pb.nl3p, l3min = pb.l3min, M = pb.M;
+  const int off1 = coff[l1 >> 1] + l1, off2 = coff[l2 >> 1] + l2;
   __nv_bfloat16* th = Thi + (size_t)prop * klp * KP;
   __nv_bfloat16* tl = Tlo + (size_t)prop * klp * KP;
-  for (int it = threadIdx.x; it < items2; it += blockDim.x) {
-    const int s = it / tiles;
-    int t = it - s * tiles;
-    int rb = 0;
-    while (t > rb) { t -= rb + 1; ++rb; }  // lower-triangular tile (rb, cb = t)
-    const int cb = t;
-    const int l3 = l3min + 2 * s;
-    int dofs = 0;
-    for (int q = 0; q < s; ++q) dofs += 2 * (l3min + 2 * q) + 1;
-    const int k2a = 2 * rb, k2b = 2 * rb + 1, k3a = 2 * cb, k3b = 2 * cb + 1;
-    const bool v2b = k2b < nk, v3b = k3b < nk;
-    const float2* da = sD + (size_t)k2a * SD + dofs + l3;
-    const float2* db = sD + (size_t)(v2b ? k2b : k2a) * SD + dofs + l3;
-    const int off3 = coff[l3 >> 1] + l3;
-    const float2* ca = sc + (size_t)k3a * nc + off3;
-    const float2* cbp = sc + (size_t)(v3b ? k3b : k3a) * nc + off3;
-    float t00 = 0.f, t01 = 0.f, t10 = 0.f, t11 = 0.f;
-    for (int m3 = -l3; m3 <= l3; ++m3) {
-      const float2 x0 = da[m3], x1 = db[m3], y0 = ca[m3], y1 = cbp[m3];
-      t00 = fmaf(x0.x, y0.x, fmaf(-x0.y, y0.y, t00));
-      t01 = fmaf(x0.x, y1.x, fmaf(-x0.y, y1.y, t01));
-      t10 = fmaf(x1.x, y0.x, fmaf(-x1.y, y0.y, t10));
-      t11 = fmaf(x1.x, y1.x, fmaf(-x1.y, y1.y, t11));
-    }
-    const int lt = pb.lt_base + s;
-    const float vals[4] = {t00, t01, t10, t11};
-    const int k2s[4] = {k2a, k2a, k2b, k2b}, k3s[4] = {k3a, k3b, k3a, k3b};
+
+  // D is double-buffered: phase 2 of chunk ch and phase 1 of chunk ch+1 need no
+  // barrier between them, so one __syncthreads per chunk suffices and uneven items
+  // of the two phases overlap across warps.
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int k1hi = chunks[ch].x, k1lo = chunks[ch].y;
+    float2* Dbuf = sD + (size_t)(ch & 1) * pmax * SDp;
+    int npairs = 0;
+    for (int k1 = k1hi; k1 >= k1lo; --k1) npairs += k1 + 1;
+    // ---- phase 1: longest diagonals (small |m3|) first ----
+    const int items1 = npairs * (sym ? M + 1 : 2 * M + 1);
+    for (int it = threadIdx.x; it < items1; it += blockDim.x) {
+      const int eo = it / npairs, p = it - eo * npairs;
+      const int m3 = sym ? eo : ((eo & 1) ? -((eo + 1) >> 1) : (eo >> 1));
+      const int e = m3 + M;
+      int k1 = k1hi, q = p;
+      while (q > k1) { q -= k1 + 1; --k1; }
+      const int k2 = q;
+      const int m1lo = max(-l1, -l2 - m3), m1hi = min(l1, l2 - m3);
+      const float* wp = wsrc + eofs[pb.eofs + e];
+      const float2* c1 = sc + k1 * ncp + off1;
+      const float2* c2 = sc + k2 * ncp + off2 - m3;
+      float ar[MAXS], ai[MAXS];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int k2 = k2s[q], k3 = k3s[q];
-      if (k2 < nk && k3 <= k2) {
-        const int ki = ki_index(k1, k2, k3);
-        const float v = vals[q];
-        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-        th[(size_t)ki * KP + lt] = hi;
-        tl[(size_t)ki * KP + lt] = lo;
-        if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
+      for (int s = 0; s < MAXS; ++s) { ar[s] = 0.f; ai[s] = 0.f; }
+      for (int m1 = m1lo; m1 <= m1hi; ++m1) {
+        const float2 a = c1[m1];
+        const float2 b = c2[-m1];
+        const float xr = a.x * b.x - a.y * b.y;
+        const float xi = a.x * b.y + a.y * b.x;
+        const float2* wr = reinterpret_cast<const float2*>(wp + (m1 - m1lo) * nl3p);
+#pragma unroll
+        for (int s2 = 0; s2 < (MAXS + 1) / 2; ++s2) {
+          if (2 * s2 < nl3) {
+            const float2 wv = wr[s2];
+            ar[2 * s2] = fmaf(wv.x, xr, ar[2 * s2]);
+            ai[2 * s2] = fmaf(wv.x, xi, ai[2 * s2]);
+            if (2 * s2 + 1 < MAXS) {
+              ar[2 * s2 + 1] = fmaf(wv.y, xr, ar[2 * s2 + 1]);
+              ai[2 * s2 + 1] = fmaf(wv.y, xi, ai[2 * s2 + 1]);
+            }
+          }
+        }
+      }
+      float2* d = Dbuf + (size_t)p * SDp;
+      int dofs = 0;
+#pragma unroll
+      for (int s = 0; s < MAXS; ++s) {
+        if (s < nl3) {
+          const int l3 = l3min + 2 * s;
+          if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
+          dofs += 2 * l3 + 1;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- phase 2: largest l3 first ----
+    int items2 = 0;
+    for (int k1 = k1hi; k1 >= k1lo; --k1) {
+      const int nq = (k1 + 4) >> 2;
+      items2 += nq * (nq + 1) / 2 * nl3;
+    }
+    for (int it = threadIdx.x; it < items2; it += blockDim.x) {
+      int k1 = k1hi, q = it, pbase = 0;
+      for (;;) {
+        const int nq = (k1 + 4) >> 2;
+        const int cnt = nq * (nq + 1) / 2 * nl3;
+        if (q < cnt) break;
+        q -= cnt;
+        pbase += k1 + 1;
+        --k1;
+      }
+      const int nq = (k1 + 4) >> 2;
+      const int tiles = nq * (nq + 1) / 2;
+      const int s = nl3 - 1 - q / tiles;
+      int t = q % tiles;
+      int ra = 0;
+      while (t > ra) { t -= ra + 1; ++ra; }
+      const int rb = t;  // k2 quad ra, k3 quad rb <= ra
+      const int l3 = l3min + 2 * s;
+      const int dofs = s * (2 * l3min + 2 * s - 1);  // sum_{j<s} (2 (l3min + 2j) + 1)
+      const int off3 = coff[l3 >> 1] + l3;
+      const float2* drow[4];
+      const float2* crow[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k2 = min(4 * ra + i, k1);
+        const int k3 = min(4 * rb + i, k1);
+        drow[i] = Dbuf + (size_t)(pbase + k2) * SDp + dofs + l3;
+        crow[i] = sc + k3 * ncp + off3;
+      }
+      float acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+      for (int m3 = sym ? 1 : -l3; m3 <= l3; ++m3) {
+        float2 x[4], y[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { x[i] = drow[i][m3]; y[i] = crow[i][m3]; }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, acc[i][j]));
+      }
+      if (sym) {
+        float2 x[4], y[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { x[i] = drow[i][0]; y[i] = crow[i][0]; }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, 2.f * acc[i][j]));
+      }
+      const int lt = pb.lt_base + s;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k2 = 4 * ra + i;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k3 = 4 * rb + j;
+          if (k2 <= k1 && k3 <= k2) {
+            const int ki = ki_index(k1, k2, k3);
+            const float v = acc[i][j];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+            const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+            th[(size_t)ki * KP + lt] = hi;
+            tl[(size_t)ki * KP + lt] = lo;
+            if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
+          }
+        }
       }
     }
   }
@@ -491,30 +617,42 @@ cudaError_t tc_configure() {
   if ((e = cudaFuncSetAttribute(k_angular_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
     return e;
   const int cs = 227 * 1024;
-  if ((e = cudaFuncSetAttribute(k_couple_pair<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_pair<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_pair<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_pair<13>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
+#define TP3_CP_ATTR(S, W)                                                                              \
+  if ((e = cudaFuncSetAttribute(k_couple_pair<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
+      cudaSuccess)                                                                                     \
     return e;
+  TP3_CP_ATTR(4, true) TP3_CP_ATTR(8, true) TP3_CP_ATTR(12, true) TP3_CP_ATTR(16, true)
+  TP3_CP_ATTR(4, false) TP3_CP_ATTR(8, false) TP3_CP_ATTR(12, false) TP3_CP_ATTR(16, false)
+#undef TP3_CP_ATTR
   return cudaSuccess;
 }
 
-cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc,
+cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, float2* cc,
+                              int* sym, cudaStream_t s) {
+  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, t.LMAX * t.LMAX, t.csean, tc.cm, tc.cmir, coeff, cc, sym);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s) {
-  const size_t smem = (size_t)t.K * (t.nc + tc.SDmax) * sizeof(float2);
-  dim3 grid(tc.n_pb, t.K, n);
-  if (tc.maxs <= 4)
-    k_couple_pair<4><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
-                                             Tlo, T32, t.n_ltp);
-  else if (tc.maxs <= 7)
-    k_couple_pair<7><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
-                                             Tlo, T32, t.n_ltp);
-  else if (tc.maxs <= 10)
-    k_couple_pair<10><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
-                                              Tlo, T32, t.n_ltp);
-  else
-    k_couple_pair<13><<<grid, 256, smem, s>>>(cc, t.K, t.nc, tc.coff, tc.pbs, tc.eofs, tc.wtab, t.klp, tc.KP, Thi,
-                                              Tlo, T32, t.n_ltp);
+  dim3 grid(tc.n_pb, n);
+  const size_t smem = tc.couple_smem;
+#define TP3_CP_LAUNCH(S, W)                                                                                \
+  k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, \
+                                                        tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,   \
+                                                        tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, T32, t.n_ltp)
+  if (tc.w_smem) {
+    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true);
+    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true);
+    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, true);
+    else TP3_CP_LAUNCH(16, true);
+  } else {
+    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, false);
+    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, false);
+    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, false);
+    else TP3_CP_LAUNCH(16, false);
+  }
+#undef TP3_CP_LAUNCH
   return cudaGetLastError();
 }
 
