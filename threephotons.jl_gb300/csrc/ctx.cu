@@ -200,7 +200,7 @@ std::string setup_tc(tp3_ctx* c) {
   int wmax = 0;
   for (const auto& pb : pbs) wmax = std::max(wmax, pb.wcount);
   tc.wsmem = wmax;
-  const size_t limit = 227 * 1024 - 1024;
+  const size_t limit = tp3::kCoupleMaxDynSmem;
   // coefficient block rounded up to 16 bytes so the 3j block (float4 copies) stays aligned
   const size_t base = ((size_t)b.K * tc.ncp * sizeof(float2) + 15) / 16 * 16;
   // D is double-buffered: two chunks of up to pmax shell pairs
@@ -223,6 +223,7 @@ std::string setup_tc(tp3_ctx* c) {
     chunks.push_back(make_int2(hi, k1 + 1));
   }
   tc.nchunks = (int)chunks.size();
+  if (tc.nchunks > 64) return "too many shell-pair chunks for the coupling kernel";
   std::vector<int> cmir(b.nc);
   for (int i = 0; i < b.nc; ++i) cmir[i] = b.coff[b.c_l[i] / 2] + b.c_l[i] - b.c_m[i];
   tc.KP = (b.n_lt() + 31) / 32 * 32;

@@ -69,6 +69,9 @@ struct TcMaps {
 };
 
 size_t tc_smem_bytes();
+// Dynamic shared memory the coupling kernel may request (the opt-in maximum of
+// 227 KB minus its static counters and slack).
+constexpr int kCoupleMaxDynSmem = 227 * 1024 - 2048;
 cudaError_t tc_configure();
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, float2* cc,
                               int* sym, cudaStream_t s);

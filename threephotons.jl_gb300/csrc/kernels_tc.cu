@@ -616,7 +616,7 @@ cudaError_t tc_configure() {
     return e;
   if ((e = cudaFuncSetAttribute(k_angular_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
     return e;
-  const int cs = 227 * 1024;
+  const int cs = kCoupleMaxDynSmem;
 #define TP3_CP_ATTR(S, W)                                                                              \
   if ((e = cudaFuncSetAttribute(k_couple_pair<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
       cudaSuccess)                                                                                     \
