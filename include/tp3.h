@@ -120,6 +120,28 @@ int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E
  * when a bounded wait inside a kernel ran out). */
 int tp3_sync(tp3_ctx* ctx);
 
+/* ---- scoring without device allocation ------------------------------------ */
+/* No counterpart in the reference.  Bayes energy of a model correlation that is
+ * already in device memory, for callers that cannot allocate device memory at the
+ * time they score: code recording the step into a CUDA graph by stream capture,
+ * runtimes whose device memory belongs to their own pooling allocator, and loops
+ * that must not stall on cudaMalloc's device synchronisation.  The call allocates
+ * nothing and needs no context:
+ *   d_c3   [klength][2N^2] float, device: c3 in tp3_c3's layout;
+ *   d_qhat [klength][2N^2] float, device: histogram slabs, each L1-normalised;
+ *   d_E    1 double, device: the energy (src/correlations.jl:201-226);
+ *   stream cudaStream_t to launch on (NULL = legacy default stream).
+ * klength = K(K+1)(K+2)/6 must be <= 65536 (K <= 72): per-slab partials go to a
+ * fixed 512 KiB array in the library's device memory that every GPU which loads
+ * the library keeps until the process exits; larger K is rejected with
+ * TP3_ERR_ARG.  The first call on each device looks up that array's address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All
+ * calls share the array: calls whose kernels overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  Each call
+ * writes every entry it reads, so no clearing is needed.  Asynchronous; errors in
+ * the arguments return at once (detail in tp3_last_error(NULL)). */
+int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, int K, int N, double* d_E, void* stream);
+
 /* ---- per-launch timing of the dominant kernel ----------------------------- */
 /* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on
  * the launching stream; tp3_profile_read returns the launch count and the summed

@@ -80,6 +80,8 @@ struct tp3_ctx {
   size_t ev_used = 0;
 };
 
+void tp3::set_thread_error(const std::string& msg) { g_create_error = msg; }
+
 namespace {
 
 int fail(tp3_ctx* c, int code, const std::string& msg) {

@@ -4,6 +4,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
 
 namespace tp3 {
 
@@ -82,6 +83,8 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s);
 
 int plain_ncg(const DevTables& t);
+// Detail text returned by tp3_last_error(NULL) on this thread.
+void set_thread_error(const std::string& msg);
 // Per-device kernel attributes of the plain path (call with the device current).
 cudaError_t plain_configure();
 constexpr int kPlainMaxSmem = 200 * 1024;

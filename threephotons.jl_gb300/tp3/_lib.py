@@ -52,6 +52,7 @@ SIGNATURES = {
     "tp3_energy": (c_int, [c_void_p, c_void_p, P(c_double)]),
     "tp3_energy_batch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "tp3_energy_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_bayes_energy_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "tp3_profile_enable": (c_int, [c_void_p, c_int]),
     "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),
 }
