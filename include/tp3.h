@@ -120,6 +120,47 @@ int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E
  * when a bounded wait inside a kernel ran out). */
 int tp3_sync(tp3_ctx* ctx);
 
+/* ---- device-resident annealing chains ------------------------------------- */
+/* nchains independent simulated-annealing chains of the reference's plain method
+ * (rotate_all_at_once + evaluate_step, src/determination.jl:281-338, 491-515),
+ * state kept on the device.  Move: get_MC_step (src/determination.jl:232-241) --
+ * one random plane rotation by N(0, sigma_l) per even l in 2..L, applied to every
+ * shell.  Step sizes start at initial_stepsize * (l - 1) (src/determination.jl:295)
+ * and are multiplied (accept) or divided (reject) by stepsizefactor; T decays by
+ * temperature_decay before each step; a step is accepted when dE < 0 or when
+ * dE > 0 and u < exp(-dE/T) (src/determination.jl:497-509).
+ * Each tp3_chains_run launch scores ncand speculative steps per chain in one
+ * batch (candidate i assumes the i previous ones were rejected) and advances every
+ * chain to its first accepted candidate, so the trajectory is the sequential
+ * chain's for the same random numbers (Philox4x32-10, counter = step, chain,
+ * purpose, index; key = seed), independent of ncand.  One launch is one replay of
+ * a captured CUDA graph.
+ *   coeff0: nchains x K x LMAX^2 complex (the layout of tp3_energy_batch)
+ *   T0:     nchains initial temperatures (calculate_temperature's result)
+ *   log_capacity: per-chain ring of the last steps' det.out columns (0 = none). */
+typedef struct tp3_chains tp3_chains;
+int tp3_chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
+                      double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
+                      int log_capacity, tp3_chains** out);
+void tp3_chains_destroy(tp3_chains* chains);
+/* Enqueue `launches` graph replays (ncand speculative steps per chain each). */
+int tp3_chains_run(tp3_chains* chains, int launches);
+/* Synchronise and read E, T, step sizes (nchains x (L/2+1), index l/2), steps
+ * taken and steps accepted per chain; any pointer may be NULL. */
+int tp3_chains_state(tp3_chains* chains, double* E, double* T, double* sigma, int64_t* steps, int64_t* accepted);
+/* Current coefficients, nchains x K x LMAX^2 complex. */
+int tp3_chains_coeff(tp3_chains* chains, double* coeff);
+/* Last min(steps, log_capacity) steps of one chain, 8 doubles per row: step, sign,
+ * E_new, E, dE, T, acceptance probability, sigma_L. */
+int tp3_chains_log(tp3_chains* chains, int chain, double* rows, int64_t* nrows);
+/* Checkpoint: with buf NULL, *bytes receives the size; otherwise the chain state
+ * (coefficients, E, T, counters, step sizes) is written to buf.  Restore is
+ * bit-exact; the RNG needs no state beyond the step counters. */
+int tp3_chains_snapshot(tp3_chains* chains, void* buf, size_t capacity, size_t* bytes);
+int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
+/* *captured = 1 when launches replay a CUDA graph. */
+int tp3_chains_graph(const tp3_chains* chains, int* captured);
+
 /* ---- scoring without device allocation ------------------------------------ */
 /* No counterpart in the reference.  Bayes energy of a model correlation that is
  * already in device memory, for callers that cannot allocate device memory at the

@@ -1,0 +1,118 @@
+"""Sequential FP64 annealing chain (oracle).
+
+TEST INFRASTRUCTURE ONLY (see oracle/sh.py).
+
+Restates rotate_all_at_once / evaluate_step (src/determination.jl:281-338,
+491-515) with the move get_MC_step (src/determination.jl:232-241): per even l in
+2..L the complex rotation rtc[l] * (C^T R(beta) C) * ctr[l], beta ~ N(0, sigma_l),
+applied to every shell, built here as a dense (2l+1) x (2l+1) matrix product.
+
+The random numbers follow the stream the device chains use, so both walk the same
+trajectory: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) with key = seed and
+counter = (step, chain, purpose, index); purpose 0 draws the angle of order l
+(index l), purpose 1 the plane (index 64 l + j, four normals per call, Box-Muller
+on (x + 0.5) 2^-32), purpose 2 the Metropolis uniform.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .sh import Umat, seanindex
+
+M32 = 0xFFFFFFFF
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32 with 10 rounds (Random123's philox4x32_R, R = 10)."""
+    c = [int(x) & M32 for x in ctr]
+    k0, k1 = int(key[0]) & M32, int(key[1]) & M32
+    for _ in range(10):
+        p0 = 0xD2511F53 * c[0]
+        p1 = 0xCD9E8D57 * c[2]
+        hi0, lo0 = p0 >> 32, p0 & M32
+        hi1, lo1 = p1 >> 32, p1 & M32
+        c = [(hi1 ^ c[1] ^ k0) & M32, lo1, (hi0 ^ c[3] ^ k1) & M32, lo0]
+        k0 = (k0 + 0x9E3779B9) & M32
+        k1 = (k1 + 0xBB67AE85) & M32
+    return c
+
+
+def _key(seed: int):
+    return (seed & M32, (seed >> 32) & M32)
+
+
+def u01(x: int) -> float:
+    return (x + 0.5) * 2.0 ** -32
+
+
+def normals4(seed: int, step: int, chain: int, purpose: int, index: int):
+    c = philox4x32_10((step & M32, chain, purpose, index), _key(seed))
+    out = []
+    for h in range(2):
+        r = math.sqrt(-2.0 * math.log(u01(c[2 * h])))
+        a = 2.0 * math.pi * u01(c[2 * h + 1])
+        out += [r * math.cos(a), r * math.sin(a)]
+    return out
+
+
+def plane(seed: int, step: int, chain: int, l: int):
+    d = 2 * l + 1
+    z = []
+    j = 0
+    while len(z) < 2 * d:
+        z += normals4(seed, step, chain, 1, 64 * l + j)
+        j += 1
+    p = np.array(z[:d])
+    q = np.array(z[d:2 * d])
+    p /= math.sqrt(p @ p)
+    q -= (p @ q) * p
+    q /= math.sqrt(q @ q)
+    return p, q
+
+
+def propose(coeff: np.ndarray, L: int, LMAX: int, sigma: dict, seed: int, step: int, chain: int) -> np.ndarray:
+    """One get_MC_step with the device stream's random numbers (dense matrices)."""
+    out = coeff.copy()
+    for l in range(2, L + 1, 2):
+        p, q = plane(seed, step, chain, l)
+        beta = normals4(seed, step, chain, 0, l)[0] * sigma[l]
+        d = 2 * l + 1
+        M = (np.eye(d) + (math.cos(beta) - 1.0) * (np.outer(p, p) + np.outer(q, q))
+             + math.sin(beta) * (np.outer(q, p) - np.outer(p, q)))
+        U = Umat(l)
+        rot = U.conj().T @ M @ U
+        idx = [seanindex(l, m, LMAX) - 1 for m in range(-l, l + 1)]
+        out[:, idx] = (rot @ coeff[:, idx].T).T
+    return out
+
+
+def run_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, initial_stepsize: float,
+              stepsizefactor: float, temperature_decay: float, seed: int, chain: int, nsteps: int):
+    """Sequential chain; returns (final coeff, E, T, sigma, log rows [step, sign, E_new, E, dE, T, ap, sigma_L])."""
+    state = coeff0.copy()
+    E = energy_fn(state)
+    T = T0
+    sigma = {l: initial_stepsize * (l - 1) for l in range(2, L + 1, 2)}
+    rows = []
+    for s in range(nsteps):
+        T *= temperature_decay
+        cand = propose(state, L, LMAX, sigma, seed, s, chain)
+        En = energy_fn(cand)
+        dE = En - E
+        ap = math.exp(-dE / T) if -dE / T < 700 else float("inf")
+        u = u01(philox4x32_10((s & M32, chain, 2, 0), _key(seed))[0])
+        acc = dE < 0.0 or (dE > 0.0 and u < ap)
+        sign = 0.0
+        if acc:
+            sign = 1.0 if dE < 0.0 else -1.0
+            for l in sigma:
+                sigma[l] *= stepsizefactor
+            E = En
+            state = cand
+        else:
+            for l in sigma:
+                sigma[l] /= stepsizefactor
+        rows.append([s + 1, sign, En, E, dE, T, ap, sigma[max(sigma)] if sigma else 0.0])
+    return state, E, T, sigma, np.array(rows)

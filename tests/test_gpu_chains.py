@@ -1,0 +1,118 @@
+"""Device-resident annealing chains vs the sequential FP64 oracle chain.
+
+North-star correctness part 4: seeded plain chains reproduce the reference
+method's accept/reject sequence except at steps whose decision lies within the
+energy tolerance (|dE| or |dE + T log u| below 1e-6 |E| + 1e-9).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import tp3
+from tp3.chains import Chains, calculate_temperature
+from oracle import chain as oc
+from oracle.basis import enumerate_basis, lt_form_F
+from oracle.c3 import triple_products, c3_lt_form, energy_bayes
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5EED1234ABCD
+
+
+@pytest.fixture(scope="module")
+def setup(config1, config1_hist):
+    p = config1["params"]
+    basis = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    basis.set_histogram(config1_hist)
+    ob = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    F = lt_form_F(ob)
+
+    def e64(c):
+        return energy_bayes(c3_lt_form(F, triple_products(ob, c)), config1_hist, p["K"], p["N"])
+
+    coeff = config1["coeff"][: p["K"]]
+    stepsizes = {l: (math.pi / 4) * (l - 1) for l in range(2, p["L"] + 1, 2)}
+    T0 = calculate_temperature(coeff, basis, config1_hist, stepsizes, 0.3, iterations=20)
+    yield basis, e64, coeff, T0, p
+    basis.close()
+
+
+def _compare(dev_rows, ref_rows, E0, chain):
+    """Decisions must agree step by step; the comparison ends at the first step whose
+    decision is within tolerance of a boundary (|dE| small, or dE close to -T log u),
+    since a flip there legitimately changes the rest of the trajectory."""
+    tol = 1e-6 * abs(E0) + 1e-9
+    n = min(len(dev_rows), len(ref_rows))
+    compared = 0
+    for i in range(n):
+        d, r = dev_rows[i], ref_rows[i]
+        s = int(r[0]) - 1
+        dE, T = r[4], r[5]
+        u = oc.u01(oc.philox4x32_10((s, chain, 2, 0), (SEED & oc.M32, SEED >> 32))[0])
+        ambiguous = abs(dE) <= tol or abs(dE + T * math.log(u)) <= tol
+        if d[1] != r[1]:
+            assert ambiguous, f"decision differs at step {i + 1}: dev {d} ref {r}"
+            return compared
+        assert d[0] == r[0]
+        assert d[2] == pytest.approx(r[2], rel=2e-6)
+        compared += 1
+        if ambiguous:
+            return compared
+    return compared
+
+
+@pytest.mark.parametrize("mode", [tp3.TP3_MODE_PLAIN_FP32, tp3.TP3_MODE_TC_BF16X3])
+def test_chain_matches_oracle(setup, mode):
+    basis, e64, coeff, T0, p = setup
+    basis.set_mode(mode)
+    ch = Chains(basis, np.stack([coeff, coeff]), T0, math.pi / 4, 1.02, 0.99, SEED, ncand=4, log_capacity=64)
+    assert ch.graph_captured
+    ch.run(6)
+    st = ch.state()
+    for c in range(2):
+        rows = ch.log(c)
+        nsteps = int(st["steps"][c])
+        assert len(rows) == nsteps >= 6
+        _, E, T, sigma, ref = oc.run_chain(e64, coeff, p["L"], p["LMAX"], T0, math.pi / 4, 1.02, 0.99, SEED, c,
+                                           nsteps)
+        compared = _compare(rows, ref, ref[0][3], c)
+        assert compared >= min(6, nsteps)
+        if compared == nsteps:
+            assert st["E"][c] == pytest.approx(E, rel=1e-6)
+            assert st["T"][c] == pytest.approx(T, rel=1e-12)
+            assert st["sigma"][c][-1] == pytest.approx(sigma[p["L"]], rel=1e-12)
+    ch.close()
+
+
+def test_candidates_per_launch_do_not_change_the_trajectory(setup):
+    basis, e64, coeff, T0, p = setup
+    basis.set_mode(tp3.TP3_MODE_TC_BF16X3)
+    a = Chains(basis, coeff[None], T0, math.pi / 4, 1.02, 0.99, SEED, ncand=1, log_capacity=64)
+    a.run(12)
+    b = Chains(basis, coeff[None], T0, math.pi / 4, 1.02, 0.99, SEED, ncand=5, log_capacity=64)
+    b.run(12)
+    ra, rb = a.log(0), b.log(0)
+    n = min(len(ra), len(rb))
+    assert n >= 12
+    np.testing.assert_array_equal(ra[:n], rb[:n])
+    a.close(); b.close()
+
+
+def test_snapshot_restore_is_bit_exact(setup):
+    basis, e64, coeff, T0, p = setup
+    basis.set_mode(tp3.TP3_MODE_TC_BF16X3)
+    ch = Chains(basis, np.stack([coeff, coeff, coeff]), T0, math.pi / 4, 1.02, 0.99, SEED + 1, ncand=3)
+    ch.run(2)
+    blob = ch.snapshot()
+    ch.run(3)
+    s1, c1 = ch.state(), ch.coeff()
+    ch.restore(blob)
+    ch.run(3)
+    s2, c2 = ch.state(), ch.coeff()
+    for k in s1:
+        np.testing.assert_array_equal(s1[k], s2[k])
+    np.testing.assert_array_equal(c1, c2)
+    with pytest.raises(tp3.TP3Error):
+        ch.restore(blob[:-8])
+    ch.close()

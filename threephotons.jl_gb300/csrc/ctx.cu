@@ -17,9 +17,7 @@
 #include <tuple>
 #include <vector>
 
-#include "../../include/tp3.h"
-#include "internal.h"
-#include "tables.h"
+#include "ctx_internal.h"
 
 using tp3::Basis;
 using tp3::DevTables;
@@ -30,55 +28,7 @@ using tp3::TcTables;
 namespace {
 thread_local std::string g_create_error;
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 }  // namespace
-
-struct tp3_ctx {
-  Basis b;
-  DevTables t{};
-  TcTables tc{};
-  bool tc_ok = false;
-  std::string tc_why;
-  int device = 0;
-  int mode = TP3_MODE_PLAIN_FP32;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  std::vector<void*> allocs;  // table allocations, freed at destroy
-  EncodeTiledFn encode = nullptr;
-  TcMaps maps{};
-
-  // histogram
-  bool has_hist = false;
-  float* d_qfull = nullptr;    // [klength][G]
-  double* d_Qfull = nullptr;   // [klength]
-  float* d_qt = nullptr;       // [klp/128][Gu][128] folded, tiled for the TMEM epilogue
-  double* d_Qfold = nullptr;   // [klength]
-
-  // scratch (sized for cap proposals)
-  int cap = 0;
-  double2* d_coeff = nullptr;  // [cap][K][LMAX^2]
-  float2* d_cc = nullptr;      // [cap][K][nc]
-  float* d_T = nullptr;        // [cap][klp][n_ltp]      plain path
-  double2* d_part = nullptr;   // [cap][ncg][klength]    plain path
-  __nv_bfloat16* d_Thi = nullptr;  // [cap][klp][KP]    tensor-core path
-  __nv_bfloat16* d_Tlo = nullptr;
-  double* d_Eslab = nullptr;   // [cap][klength]         tensor-core path
-  double* d_E = nullptr;       // [cap]
-  float* d_c3 = nullptr;       // [klength][G] (one proposal)
-  int* d_err = nullptr;        // device error flag (timeouts)
-  int* d_sym = nullptr;        // [cap] real-function symmetry flag per proposal
-  double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
-  double* h_E = nullptr;       // pinned [cap]
-  int* h_err = nullptr;        // pinned
-
-  // profiling of the angular + Bayes kernel
-  bool prof = false;
-  std::vector<cudaEvent_t> ev;  // pairs
-  size_t ev_used = 0;
-};
 
 void tp3::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
@@ -247,7 +197,7 @@ std::string setup_tc(tp3_ctx* c) {
   if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
       q != cudaDriverEntryPointSuccess || !fn)
     return "cuTensorMapEncodeTiled unavailable";
-  c->encode = (EncodeTiledFn)fn;
+  c->encode = (tp3::EncodeTiledFn)fn;
   cudaError_t e;
   if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
       (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
@@ -309,6 +259,7 @@ int ensure_cap(tp3_ctx* c, int n) {
       return fail(c, TP3_ERR_CUDA, "tensor map encoding of T failed");
   }
   c->cap = n;
+  ++c->scratch_gen;
   return TP3_OK;
 }
 
@@ -391,6 +342,15 @@ int check_ctx(tp3_ctx* c) {
 }
 
 }  // namespace
+
+int tp3::ctx_fail(tp3_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
+int tp3::ctx_cuda_fail(tp3_ctx* c, cudaError_t e, const char* where) { return cuda_fail(c, e, where); }
+int tp3::ctx_check(tp3_ctx* c) { return check_ctx(c); }
+int tp3::ctx_ensure_cap(tp3_ctx* c, int n) { return ensure_cap(c, n); }
+int tp3::ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E) {
+  return run_energy(c, n, d_coeff, d_E);
+}
+int tp3::ctx_check_device_error(tp3_ctx* c) { return check_device_error(c); }
 
 extern "C" {
 

@@ -1,0 +1,77 @@
+// Definition of the library context, shared by the C ABI files (ctx.cu, chains.cu).
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tp3.h"
+#include "internal.h"
+#include "tables.h"
+
+namespace tp3 {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+}  // namespace tp3
+
+
+struct tp3_ctx {
+  tp3::Basis b;
+  tp3::DevTables t{};
+  tp3::TcTables tc{};
+  bool tc_ok = false;
+  std::string tc_why;
+  int device = 0;
+  int mode = TP3_MODE_PLAIN_FP32;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<void*> allocs;  // table allocations, freed at destroy
+  tp3::EncodeTiledFn encode = nullptr;
+  tp3::TcMaps maps{};
+
+  // histogram
+  bool has_hist = false;
+  float* d_qfull = nullptr;    // [klength][G]
+  double* d_Qfull = nullptr;   // [klength]
+  float* d_qt = nullptr;       // [klp/128][Gu][128] folded, tiled for the TMEM epilogue
+  double* d_Qfold = nullptr;   // [klength]
+
+  // scratch (sized for cap proposals)
+  int cap = 0;
+  int scratch_gen = 0;         // incremented whenever the scratch below is reallocated
+  double2* d_coeff = nullptr;  // [cap][K][LMAX^2]
+  float2* d_cc = nullptr;      // [cap][K][nc]
+  float* d_T = nullptr;        // [cap][klp][n_ltp]      plain path
+  double2* d_part = nullptr;   // [cap][ncg][klength]    plain path
+  __nv_bfloat16* d_Thi = nullptr;  // [cap][klp][KP]    tensor-core path
+  __nv_bfloat16* d_Tlo = nullptr;
+  double* d_Eslab = nullptr;   // [cap][klength]         tensor-core path
+  double* d_E = nullptr;       // [cap]
+  float* d_c3 = nullptr;       // [klength][G] (one proposal)
+  int* d_err = nullptr;        // device error flag (timeouts)
+  int* d_sym = nullptr;        // [cap] real-function symmetry flag per proposal
+  double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
+  double* h_E = nullptr;       // pinned [cap]
+  int* h_err = nullptr;        // pinned
+
+  // profiling of the angular + Bayes kernel
+  bool prof = false;
+  std::vector<cudaEvent_t> ev;  // pairs
+  size_t ev_used = 0;
+};
+
+
+namespace tp3 {
+// Helpers of ctx.cu used by the other C ABI files.
+int ctx_fail(tp3_ctx* c, int code, const std::string& msg);
+int ctx_cuda_fail(tp3_ctx* c, cudaError_t e, const char* where);
+int ctx_check(tp3_ctx* c);
+int ctx_ensure_cap(tp3_ctx* c, int n);
+// Score n proposals whose FP64 seanindex-ordered coefficients are in device memory.
+int ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E);
+int ctx_check_device_error(tp3_ctx* c);
+}  // namespace tp3

@@ -52,6 +52,16 @@ SIGNATURES = {
     "tp3_energy": (c_int, [c_void_p, c_void_p, P(c_double)]),
     "tp3_energy_batch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "tp3_energy_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_chains_create": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_double,
+                                  ctypes.c_uint64, c_int, P(c_void_p)]),
+    "tp3_chains_destroy": (None, [c_void_p]),
+    "tp3_chains_run": (c_int, [c_void_p, c_int]),
+    "tp3_chains_state": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tp3_chains_coeff": (c_int, [c_void_p, c_void_p]),
+    "tp3_chains_log": (c_int, [c_void_p, c_int, c_void_p, P(c_int64)]),
+    "tp3_chains_snapshot": (c_int, [c_void_p, c_void_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
+    "tp3_chains_restore": (c_int, [c_void_p, c_void_p, ctypes.c_size_t]),
+    "tp3_chains_graph": (c_int, [c_void_p, P(c_int)]),
     "tp3_bayes_energy_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "tp3_profile_enable": (c_int, [c_void_p, c_int]),
     "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),
