@@ -91,7 +91,9 @@ __global__ void __launch_bounds__(256) k_angular_plain(
   const float* Tp = T + (int64_t)prop * T_stride;
   const int cbeg = cg * cols_per_group;
   const int cend = min(G, cbeg + cols_per_group);
+  // compensated (Kahan) per-row sums
   float Sp[4] = {0.f, 0.f, 0.f, 0.f}, Sql[4] = {0.f, 0.f, 0.f, 0.f};
+  float Cp[4] = {0.f, 0.f, 0.f, 0.f}, Cq[4] = {0.f, 0.f, 0.f, 0.f};
   // loader mapping: 64 rows x 16 k = 256 float4
   const int lrow = tid >> 2, lk = (tid & 3) * 4;
   for (int c0 = cbeg; c0 < cend; c0 += 64) {
@@ -135,8 +137,14 @@ __global__ void __launch_bounds__(256) k_angular_plain(
         for (int j = 0; j < 4; ++j) {
           if (col + j < cend) {
             const float p = fmaxf(acc[i][j], 1e-30f);
-            Sp[i] += p;
-            Sql[i] = fmaf(qr[col + j], __logf(p), Sql[i]);
+            const float y1 = p - Cp[i];
+            const float t1 = Sp[i] + y1;
+            Cp[i] = (t1 - Sp[i]) - y1;
+            Sp[i] = t1;
+            const float y2 = qr[col + j] * __logf(p) - Cq[i];
+            const float t2 = Sql[i] + y2;
+            Cq[i] = (t2 - Sql[i]) - y2;
+            Sql[i] = t2;
           }
         }
       }
@@ -145,7 +153,7 @@ __global__ void __launch_bounds__(256) k_angular_plain(
   if (STORE) return;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    double sp = Sp[i], sq = Sql[i];
+    double sp = (double)Sp[i] - (double)Cp[i], sq = (double)Sql[i] - (double)Cq[i];
 #pragma unroll
     for (int off = 8; off > 0; off >>= 1) {
       sp += __shfl_xor_sync(0xffffffffu, sp, off);

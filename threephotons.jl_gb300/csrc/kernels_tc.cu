@@ -509,7 +509,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
     const int cblk = ew >> 2;               // which 128-column block of each half
     const int r = quarter * 32 + lane;      // row inside the tile
     const int ki = mtile * kBM + r;
-    float sp = 0.f, sq = 0.f;
+    // compensated (Kahan) sums: Sp and Sql are differences of large, nearly equal
+    // energies once combined, so their rounding sets the precision of dE
+    float sp = 0.f, sq = 0.f, csp = 0.f, csq = 0.f;
     for (int h = 0; h < nhalf; ++h) {
       if (!mbar_wait(&hd->tmem_full[h], 0u, abort_flag, err)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -542,16 +544,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
             const int u = col + j;
             if (u < Gu) {
               const float p = fmaxf(v[j], 1e-30f);
-              sp += p;
-              sq = fmaf(qrow[(size_t)u * kBM], __logf(p), sq);
+              const float y1 = p - csp;
+              const float t1 = sp + y1;
+              csp = (t1 - sp) - y1;
+              sp = t1;
+              const float y2 = qrow[(size_t)u * kBM] * __logf(p) - csq;
+              const float t2 = sq + y2;
+              csq = (t2 - sq) - y2;
+              sq = t2;
             }
           }
         }
       }
     }
     if (!STORE) {
-      hd->part_sp[cblk][r] = sp;
-      hd->part_sq[cblk][r] = sq;
+      hd->part_sp[cblk][r] = sp - csp;
+      hd->part_sq[cblk][r] = sq - csq;
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
