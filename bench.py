@@ -200,6 +200,7 @@ def main():
     ap.add_argument("--mode", default="auto", choices=["auto", "plain", "tc"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-chains", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -277,8 +278,9 @@ def main():
     for _ in range(e2e_steps):
         E_host = basis.energy_batch(host_props)
     e2e_dt = time.perf_counter() - t0
+    # the host API packs the even-l <= L block of each shell (nc complex doubles) before the copy
     e2e = {"value": ws * B * e2e_steps / e2e_dt, "unit": UNIT,
-           "h2d_bytes_per_step": int(host_props.nbytes), "d2h_bytes_per_step": int(E_host.nbytes)}
+           "h2d_bytes_per_step": int(B * K * basis.nc * 16), "d2h_bytes_per_step": int(E_host.nbytes)}
     if not np.allclose(E_host, E_dev, rtol=0, atol=0):
         raise SystemExit("device-resident and host-API energies differ")
 
@@ -302,6 +304,34 @@ def main():
                 "kernel": "angular contraction + fused Bayes", "kernel_ms_per_launch": per_launch_ms,
                 "algorithmic_flop_per_proposal": W_b}
 
+    # device-resident annealing chains: 64 chains x 16 speculative candidates per graph replay
+    chains_info = None
+    if not args.no_chains:
+        from tp3.chains import Chains
+        basis.set_stream(None)
+        nch, ncand = 64, 16
+        T0 = np.full(nch, 0.1 * float(np.std(E_dev)))
+        ch = Chains(basis, np.repeat(base[None, :K], nch, axis=0), T0, math.pi / 4, 1.02, 0.99998, 12345,
+                    ncand=ncand)
+        ch.run(2)
+        s0 = ch.state()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        reps = max(3, args.steps // 2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ch.run(reps)
+        s1 = ch.state()
+        dt = time.perf_counter() - t0
+        chains_info = {"chains": nch, "candidates_per_launch": ncand, "launches": reps,
+                       "graph_captured": ch.graph_captured,
+                       "proposals_per_s": nch * ncand * reps / dt,
+                       "chain_steps_per_s": float((s1["steps"] - s0["steps"]).sum()) / dt,
+                       "ms_per_launch": 1e3 * dt / reps,
+                       "note": "wall clock around graph replays incl. one final synchronise; proposals include "
+                               "device-side move generation and the Metropolis update"}
+        ch.close()
+
     kernels_per_step = 4
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -312,7 +342,7 @@ def main():
                        "L": L, "K": K, "N": N, "LMAX": LMAX, "proposals_per_step": B,
                        "mode": {0: "plain_fp32", 1: "tc_bf16x3"}.get(mode_used, str(mode_used)),
                        "l2": "flushed (512 MB write) between steps, outside the per-step events"},
-            "e2e": e2e, "roofline": roofline, "clocks": clocks,
+            "e2e": e2e, "roofline": roofline, "clocks": clocks, "chains": chains_info,
             "gpu_launches": kernels_per_step * args.steps}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(base, hist)

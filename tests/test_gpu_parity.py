@@ -101,6 +101,18 @@ def test_energy_batch_matches_single(basis1, config1, config1_hist, mode):
         assert e == pytest.approx(e64, rel=1e-6)
 
 
+@pytest.mark.parametrize("mode", MODES)
+def test_energy_batch_chunked(basis1, config1, config1_hist, mode):
+    """Batches of >= 32 are packed and copied in chunks; each energy must not depend on it."""
+    basis1.set_mode(mode)
+    basis1.set_histogram(config1_hist)
+    rng = np.random.default_rng(9)
+    coeffs = np.stack([config1["coeff"] * (1 + 0.02 * rng.normal(size=config1["coeff"].shape)) for _ in range(37)])
+    Eb = basis1.energy_batch(coeffs)
+    Es = np.array([basis1.energy_batch(c[None])[0] for c in coeffs])
+    np.testing.assert_array_equal(Eb, Es)
+
+
 def test_energy_deterministic(basis1, config1, config1_hist):
     basis1.set_histogram(config1_hist)
     E1 = basis1.energy_batch(config1["coeff"][None])

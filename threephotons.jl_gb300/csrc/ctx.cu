@@ -279,17 +279,18 @@ int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) {
 }
 
 // Gather + coupling stage for n proposals whose FP64 coefficients are in d_coeff.
-int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32) {
+int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool compact = false) {
   const auto& t = c->t;
   cudaError_t e;
+  const tp3::CoeffLayout lay = compact ? tp3::CoeffLayout{t.cident, t.nc} : tp3::CoeffLayout{t.csean, t.LMAX * t.LMAX};
   if (c->mode == TP3_MODE_TC_BF16X3) {
-    if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
     if ((e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo,
                                      want_T32 ? c->d_T : nullptr, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "couple_pair");
   } else {
-    if ((e = tp3::launch_gather(t, n, d_coeff, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
+    if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
     if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "couple_direct");
   }
@@ -297,11 +298,11 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32) {
 }
 
 // Score n proposals whose FP64 coefficients are already in d_coeff (device).
-int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E) {
+int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool compact = false) {
   const auto& t = c->t;
   cudaError_t e;
   if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
-  if (int r = run_coupling(c, n, d_coeff, false)) return r;
+  if (int r = run_coupling(c, n, d_coeff, false, compact)) return r;
   cudaEvent_t a, b;
   int pr = prof_begin(c, &a, &b);
   if (c->mode == TP3_MODE_TC_BF16X3) {
@@ -470,7 +471,10 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
     return fail(nullptr, TP3_ERR_CUDA, msg);
   }
   c->stream = c->own;
-  if ((e = upload(c, b.c_sean, &t.csean)) != cudaSuccess || (e = upload(c, w32, &t.w)) != cudaSuccess ||
+  std::vector<int> ident(b.nc);
+  for (int i = 0; i < b.nc; ++i) ident[i] = i;
+  if ((e = upload(c, b.c_sean, &t.csean)) != cudaSuccess || (e = upload(c, ident, &t.cident)) != cudaSuccess ||
+      (e = upload(c, w32, &t.w)) != cudaSuccess ||
       (e = upload(c, idx, &t.idx)) != cudaSuccess || (e = upload(c, lt, &t.lt)) != cudaSuccess ||
       (e = upload(c, kl, &t.kl)) != cudaSuccess || (e = upload(c, b.tf, &t.tf)) != cudaSuccess ||
       (e = upload(c, Ffull, &t.Ffull)) != cudaSuccess || (e = upload(c, b.u_to_g, &t.u_to_g)) != cudaSuccess ||
@@ -636,12 +640,31 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
   if (n < 1 || !coeffs || !E) return fail(c, TP3_ERR_ARG, "bad batch arguments");
   if (int r = ensure_cap(c, n)) return r;
   const auto& t = c->t;
-  const size_t nco = (size_t)n * t.K * t.LMAX * t.LMAX;
-  std::memcpy(c->h_coeff, coeffs, nco * 2 * sizeof(double));
+  const Basis& b = c->b;
+  const size_t ncoef = (size_t)t.LMAX * t.LMAX;
+  // Only the even-l <= L block of each shell reaches the kernels: pack it on the host
+  // (3.3x fewer bytes at L=18, LMAX=25) in chunks, so packing chunk i+1 overlaps the
+  // copy and the kernels of chunk i.
+  const int nchunk = n >= 32 ? 4 : 1;
+  const int per = (n + nchunk - 1) / nchunk;
+  const double2* src = (const double2*)coeffs;
+  double2* pin = (double2*)c->h_coeff;
+  double2* dev = c->d_coeff;
   cudaError_t e;
-  if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
-    return cuda_fail(c, e, "H2D coeff");
-  if (int r = run_energy(c, n, c->d_coeff, c->d_E)) return r;
+  for (int p0 = 0; p0 < n; p0 += per) {
+    const int m = std::min(per, n - p0);
+    for (int p = p0; p < p0 + m; ++p)
+      for (int k = 0; k < t.K; ++k) {
+        const double2* s = src + ((size_t)p * t.K + k) * ncoef;
+        double2* d = pin + ((size_t)p * t.K + k) * t.nc;
+        for (int i = 0; i < t.nc; ++i) d[i] = s[b.c_sean[i]];
+      }
+    const size_t off = (size_t)p0 * t.K * t.nc;
+    if ((e = cudaMemcpyAsync(dev + off, pin + off, (size_t)m * t.K * t.nc * sizeof(double2), cudaMemcpyHostToDevice,
+                             c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "H2D coeff");
+    if (int r = run_energy(c, m, dev + off, c->d_E + p0, true)) return r;
+  }
   if ((e = cudaMemcpyAsync(c->h_E, c->d_E, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "D2H energy");

@@ -15,6 +15,7 @@ struct DevTables {
   int klength, klp;     // shell triples, padded to the TC row tile
   int G, Gu, mult, N;
   const int* csean;     // [nc] compact -> seanindex0
+  const int* cident;    // [nc] identity map (compact input)
   const float* w;       // [basislen]
   const uint32_t* idx;  // [basislen] i1 | i2 << 10 | i3 << 20
   const int2* lt;       // [n_lt] (jstart, jcount)
@@ -26,7 +27,15 @@ struct DevTables {
 };
 
 // Plain path launches (kernels_plain.cu).
-cudaError_t launch_gather(const DevTables& t, int n, const double2* coeff, float2* cc, cudaStream_t s);
+// Input coefficient layouts of the gather kernels: per shell either the full
+// seanindex-ordered LMAX^2 vector (map = csean, stride LMAX^2) or the compact even-l
+// block (map = identity, stride nc).
+struct CoeffLayout {
+  const int* map;
+  int stride;
+};
+cudaError_t launch_gather(const DevTables& t, int n, const double2* coeff, CoeffLayout lay, float2* cc,
+                          cudaStream_t s);
 cudaError_t launch_couple_direct(const DevTables& t, int n, const float2* cc, float* T, cudaStream_t s);
 // Bayes partials: part[prop][cg][klength] (Sp, Sql); ncg column groups over the full grid.
 cudaError_t launch_angular_plain(const DevTables& t, int n, const float* T, const float* q,
@@ -74,8 +83,8 @@ size_t tc_smem_bytes();
 // 227 KB minus its static counters and slack).
 constexpr int kCoupleMaxDynSmem = 227 * 1024 - 2048;
 cudaError_t tc_configure();
-cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, float2* cc,
-                              int* sym, cudaStream_t s);
+cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
+                              float2* cc, int* sym, cudaStream_t s);
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,

@@ -220,12 +220,13 @@ int plain_ncg(const DevTables& t) {
   return ncg < 1 ? 1 : ncg;
 }
 
-cudaError_t launch_gather(const DevTables& t, int n, const double2* coeff, float2* cc, cudaStream_t s) {
+cudaError_t launch_gather(const DevTables& t, int n, const double2* coeff, CoeffLayout lay, float2* cc,
+                          cudaStream_t s) {
   const int64_t total = (int64_t)n * t.K * t.nc;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   if (blocks < 1) blocks = 1;
-  k_gather<<<blocks, 256, 0, s>>>(n, t.K, t.nc, t.LMAX * t.LMAX, t.csean, coeff, cc);
+  k_gather<<<blocks, 256, 0, s>>>(n, t.K, t.nc, lay.stride, lay.map, coeff, cc);
   return cudaGetLastError();
 }
 

@@ -635,9 +635,9 @@ cudaError_t tc_configure() {
   return cudaSuccess;
 }
 
-cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, float2* cc,
-                              int* sym, cudaStream_t s) {
-  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, t.LMAX * t.LMAX, t.csean, tc.cm, tc.cmir, coeff, cc, sym);
+cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
+                              float2* cc, int* sym, cudaStream_t s) {
+  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, lay.stride, lay.map, tc.cm, tc.cmir, coeff, cc, sym);
   return cudaGetLastError();
 }
 

@@ -97,6 +97,7 @@ class BasisTypeGB300:
         check(self._lib.tp3_basis_info(L, LMAX, N, K, self.lambda_, self.dq, info))
         self.basislen, self.n_lt, self.klength = int(info[0]), int(info[1]), int(info[2])
         self.nnz_pi2 = int(info[7])
+        self.nc = int(info[6])
         self.set_mode(mode)
         self._hist_key = None
         self._hist_ref = None
