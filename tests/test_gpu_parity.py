@@ -76,6 +76,16 @@ def test_c3_config1(basis1, config1, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
+def test_c3_matches_reference_cuda_kernel(basis1, config1, mode):
+    """libtp3's c3 vs the reference's own CUDA kernel + SGEMM output (golden fixture)."""
+    import os
+    basis1.set_mode(mode)
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "config1_refcuda.npz"))["c3_refcuda"]
+    c3 = basis1.c3_raw(config1["coeff"]).astype(np.float64)
+    assert rel_l1(c3, ref.astype(np.float64)) <= 1e-5
+
+
+@pytest.mark.parametrize("mode", MODES)
 def test_energy_config1(basis1, config1, config1_hist, mode):
     basis1.set_mode(mode)
     vol = tp3.SphericalHarmonicsVolume(config1["coeff"], 9, 8, 8.0)

@@ -167,3 +167,15 @@ def test_histogram_contract():
     assert h.shape == (4, 8, 3, 3, 3)
     assert h.min() > 0 and abs(h.sum() - 1.0) < 1e-12
     np.testing.assert_allclose(h[:, :4], h[:, 4:])
+
+
+def test_oracle_pinned_to_reference_cuda_kernel(config1):
+    """The reference's own GPU path (src/cuda_kernel.cu + SGEMM, src/cuda.jl:74-108), run on
+    a GB300 on the same coefficients and tables (tests/golden/make_refcuda_golden.py),
+    against the oracle: relative L1 within the reference's own CPU-vs-GPU tolerance
+    (tests/test_cuda.jl:15)."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "config1_refcuda.npz"))
+    ref = d["c3_refcuda"].astype(np.float64)
+    for mine in (config1["c3_refform"], config1["c3_fp64"]):
+        assert np.abs(ref - mine).sum() / np.abs(mine).sum() < 1e-5
