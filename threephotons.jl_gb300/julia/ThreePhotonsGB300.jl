@@ -1,0 +1,146 @@
+# ThreePhotonsGB300 -- binds libtp3 (include/tp3.h) behind ThreePhotons.jl's own calls.
+#
+# Written against the reference's Julia 0.6 API (src/correlations.jl, src/cuda.jl,
+# src/determination.jl).  Not run in this build: neither the build machine nor the GPU
+# machine has Julia.  The same C ABI is exercised from Python by the test suite.
+#
+# Use inside a session that has loaded ThreePhotons:
+#     include("ThreePhotonsGB300.jl"); using ThreePhotonsGB300
+#     ThreePhotons.complexBasis_choice = ThreePhotonsGB300.GB300_calculate_basis
+# after which rotate_all_at_once / calculate_temperature / evaluate_step call
+# FullCorrelation_parallized and energy on a BasisTypeGB300 (methods below).
+module ThreePhotonsGB300
+
+import ThreePhotons: AbstractBasisType, SphericalHarmonicsVolume, FullCorrelation_parallized, energy,
+                     Umat, C3, num_coeff
+
+export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_run, GB300_chains_state
+
+const libtp3 = joinpath(@__DIR__, "..", "lib", "libtp3.so")
+
+const TP3_OK = Int32(0)
+
+function check(status::Int32, ctx::Ptr{Void})
+    if status != TP3_OK
+        msg = unsafe_string(ccall((:tp3_last_error, libtp3), Cstring, (Ptr{Void},), ctx))
+        what = unsafe_string(ccall((:tp3_status_string, libtp3), Cstring, (Int32,), status))
+        error("libtp3 status $status ($what): $msg")   # no CPU fallback
+    end
+end
+
+"""Device-resident basis (role of BasisTypeCuda, src/cuda.jl:24-42): the fields the
+annealing code reads, plus the libtp3 context that owns every device table."""
+type BasisTypeGB300 <: AbstractBasisType
+    ctx::Ptr{Void}
+    basislen::Int64
+    N::Int64
+    L::Int64
+    LMAX::Int64
+    lrange::StepRange
+    ctr::Dict
+    rtc::Dict
+    K::Int64
+    lambda::Float64
+    dq::Float64
+    histogram::Any          # the c3ref last uploaded (compared by identity)
+end
+
+"""complexBasis_choice replacement (src/correlations.jl:87, src/cuda.jl:57-71)."""
+function GB300_calculate_basis(L::Int64, LMAX::Int64, N::Int64, K::Int64, lambda::Float64=0.0,
+                               dq::Float64=0.0, forIntensity=true)
+    forIntensity || error("only the intensity basis (lrange = 0:2:L) is on the GB300 path")
+    ctx = Ref{Ptr{Void}}(C_NULL)
+    check(ccall((:tp3_ctx_create, libtp3), Int32,
+                (Int32, Int32, Int32, Int32, Float64, Float64, Ref{Ptr{Void}}),
+                L, LMAX, N, K, lambda, dq, ctx), C_NULL)
+    info = zeros(Int64, 8)
+    check(ccall((:tp3_basis_info, libtp3), Int32,
+                (Int32, Int32, Int32, Int32, Float64, Float64, Ptr{Int64}),
+                L, LMAX, N, K, lambda, dq, info), C_NULL)
+    lrange = 0:2:L
+    ctr = Dict(l => Umat(l) for l = lrange)
+    rtc = Dict(l => ctranspose(ctr[l]) for l = lrange)
+    b = BasisTypeGB300(ctx[], info[1], N, L, LMAX, lrange, ctr, rtc, K, lambda, dq, nothing)
+    finalizer(b, x -> ccall((:tp3_ctx_destroy, libtp3), Void, (Ptr{Void},), x.ctx))
+    return b
+end
+
+"""First K shells as one contiguous K x LMAX^2 block (the layout cuda.jl:79 builds)."""
+function pack(intensity::SphericalHarmonicsVolume, basis::BasisTypeGB300)
+    n = num_coeff(basis.LMAX)
+    buf = Array{Complex{Float64}}(n, basis.K)
+    for k = 1:basis.K
+        buf[:, k] = intensity.coeff[k][1:n]
+    end
+    return buf
+end
+
+"""src/cuda.jl:74-108 on libtp3 (tp3_c3)."""
+function FullCorrelation_parallized(intensity::SphericalHarmonicsVolume, basis::BasisTypeGB300,
+                                    minimal::Bool=true, normalize::Bool=false, return_raw::Bool=false)
+    klength = div(basis.K * (basis.K + 1) * (basis.K + 2), 6)
+    raw = Array{Float32}(2 * basis.N^2, klength)
+    check(ccall((:tp3_c3, libtp3), Int32, (Ptr{Void}, Ptr{Complex{Float64}}, Ptr{Float32}),
+                basis.ctx, pack(intensity, basis), raw), basis.ctx)
+    res = convert(Array{Float64}, raw)
+    if return_raw return res end
+    t = zeros(Float64, basis.N, 2 * basis.N, basis.K, basis.K, basis.K)
+    i = 1
+    for k1 = 1:basis.K for k2 = 1:k1 for k3 = 1:k2
+        t[:, :, k3, k2, k1] = reshape(res[:, i], basis.N, 2 * basis.N)
+        i += 1
+    end end end
+    return normalize ? t / sum(abs, t) : t
+end
+
+function set_histogram!(basis::BasisTypeGB300, c3ref::C3)
+    if basis.histogram !== c3ref
+        K3 = size(c3ref, 3)
+        check(ccall((:tp3_set_histogram, libtp3), Int32, (Ptr{Void}, Ptr{Float64}, Int32),
+                    basis.ctx, c3ref, K3), basis.ctx)
+        basis.histogram = c3ref
+    end
+end
+
+"""src/correlations.jl:201-226 on libtp3 (tp3_energy)."""
+function energy(intensity::SphericalHarmonicsVolume, basis::BasisTypeGB300, c3ref::C3,
+                K3_range::UnitRange{Int64}, measure::String="Bayes", negativity_factor::Float64=0.0)
+    K3_range == 1:basis.K || error("K3_range must be 1:K")
+    measure == "Bayes" || return 0.0
+    set_histogram!(basis, c3ref)
+    E = Ref{Float64}(0.0)
+    check(ccall((:tp3_energy, libtp3), Int32, (Ptr{Void}, Ptr{Complex{Float64}}, Ref{Float64}),
+                basis.ctx, pack(intensity, basis), E), basis.ctx)
+    return E[]
+end
+
+energy(intensity::SphericalHarmonicsVolume, basis::BasisTypeGB300, c3ref::C3, measure::String="Bayes",
+       negativity_factor::Float64=0.0) = energy(intensity, basis, c3ref, 1:basis.K, measure, negativity_factor)
+
+# ---- device-resident chains (rotate_all_at_once on the GPU) ---------------------------
+function GB300_chains_create(basis::BasisTypeGB300, starts::Vector{SphericalHarmonicsVolume}, T0::Vector{Float64},
+                             initial_stepsize::Float64, stepsizefactor::Float64, temperature_decay::Float64,
+                             seed::UInt64; ncand::Int=16, log_capacity::Int=0)
+    coeff = cat(3, [pack(s, basis) for s in starts]...)
+    h = Ref{Ptr{Void}}(C_NULL)
+    check(ccall((:tp3_chains_create, libtp3), Int32,
+                (Ptr{Void}, Int32, Int32, Ptr{Complex{Float64}}, Ptr{Float64}, Float64, Float64, Float64,
+                 UInt64, Int32, Ref{Ptr{Void}}),
+                basis.ctx, length(starts), ncand, coeff, T0, initial_stepsize, stepsizefactor,
+                temperature_decay, seed, log_capacity, h), basis.ctx)
+    return h[]
+end
+
+GB300_chains_run(basis::BasisTypeGB300, h::Ptr{Void}, launches::Int) =
+    check(ccall((:tp3_chains_run, libtp3), Int32, (Ptr{Void}, Int32), h, launches), basis.ctx)
+
+function GB300_chains_state(basis::BasisTypeGB300, h::Ptr{Void}, n::Int)
+    E = zeros(n); T = zeros(n); steps = zeros(Int64, n); acc = zeros(Int64, n)
+    sigma = zeros(div(basis.L, 2) + 1, n)
+    check(ccall((:tp3_chains_state, libtp3), Int32,
+                (Ptr{Void}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int64}, Ptr{Int64}),
+                h, E, T, sigma, steps, acc), basis.ctx)
+    return E, T, sigma, steps, acc
+end
+
+end # module
