@@ -167,15 +167,102 @@ std::string setup_tc(tp3_ctx* c) {
   if (need(pmax, tc.w_smem) > limit) return "coupling tile exceeds shared memory";
   tc.pmax = pmax;
   tc.couple_smem = need(pmax, tc.w_smem);
-  // chunks of whole k1 values, largest shells first, at most pmax shell pairs each
-  std::vector<int2> chunks;
-  for (int k1 = b.K - 1; k1 >= 0;) {
-    int hi = k1, cnt = 0;
-    while (k1 >= 0 && cnt + k1 + 1 <= pmax) { cnt += k1 + 1; --k1; }
-    chunks.push_back(make_int2(hi, k1 + 1));
+  // real-function path: D rows hold m3 = 0..l3 only, so the same bytes hold more pairs
+  int SDh = 0;
+  for (const auto& pb : pbs) {
+    int h = 0;
+    for (int s3 = 0; s3 < pb.nl3; ++s3) h += pb.l3min + 2 * s3 + 1;
+    SDh = std::max(SDh, h);
   }
+  tc.SDhp = SDh | 1;
+  tc.pmax_sym = (int)((2 * (size_t)pmax * tc.SDp) / (2 * (size_t)tc.SDhp));
+  // chunks of whole k1 values, largest shells first, at most pmax shell pairs each
+  auto make_chunks = [&](int pm) {
+    std::vector<int2> ch;
+    for (int k1 = b.K - 1; k1 >= 0;) {
+      int hi = k1, cnt = 0;
+      while (k1 >= 0 && cnt + k1 + 1 <= pm) { cnt += k1 + 1; --k1; }
+      ch.push_back(make_int2(hi, k1 + 1));
+    }
+    return ch;
+  };
+  std::vector<int2> chunks = make_chunks(pmax), chunks_sym = make_chunks(tc.pmax_sym);
   tc.nchunks = (int)chunks.size();
+  tc.nchunks_sym = (int)chunks_sym.size();
+  if (tc.nchunks_sym > 64) return "too many shell-pair chunks for the coupling kernel";
   if (tc.nchunks > 64) return "too many shell-pair chunks for the coupling kernel";
+  // split coupling: D offsets, L2-sized sub-batches, balanced (pair block, m3 range) units
+  const int npairs = b.K * (b.K + 1) / 2;
+  std::vector<long long> doff(pbs.size());
+  long long dst = 0;
+  tc.dmax = 0;
+  for (size_t i = 0; i < pbs.size(); ++i) {
+    doff[i] = dst;
+    dst += (long long)npairs * pbs[i].SD;
+    tc.dmax = std::max(tc.dmax, std::max(pbs[i].l1, pbs[i].l2));
+  }
+  tc.dstride = dst;
+  tc.dsub = (int)std::max<long long>(1, (72LL << 20) / (dst * (long long)sizeof(float2)));
+  auto m3work = [&](const PairBlock& pb, int m3) {
+    const int n = std::min(pb.l1, pb.l2 - m3) - std::max(-pb.l1, -pb.l2 - m3) + 1;
+    return (double)std::max(n, 0) * (4 + 2 * pb.nl3p);
+  };
+  double target = 0;
+  for (const auto& pb : pbs)
+    for (int m3 = 0; m3 <= pb.M; ++m3) target = std::max(target, m3work(pb, m3));
+  struct U { int4 u; double w; };
+  std::vector<U> us, ug;
+  auto cut = [&](std::vector<U>& out, int pbi, int from, int to, int step) {  // m3 = from .. to by step
+    const PairBlock& pb = pbs[pbi];
+    int lo = from;
+    double w = 0;
+    for (int m3 = from;; m3 += step) {
+      w += m3work(pb, m3);
+      const bool last = m3 == to;
+      if (w >= target || last) {
+        const int a = std::min(lo, m3), z = std::max(lo, m3);
+        out.push_back({make_int4(pbi, a, z, 0), w});
+        lo = m3 + step;
+        w = 0;
+      }
+      if (last) break;
+    }
+  };
+  for (int i = 0; i < (int)pbs.size(); ++i) {
+    cut(us, i, 0, pbs[i].M, 1);
+    cut(ug, i, 0, pbs[i].M, 1);
+    if (pbs[i].M > 0) cut(ug, i, -1, -pbs[i].M, -1);
+  }
+  auto heavy_first = [](const U& a, const U& c) { return a.w > c.w; };
+  std::sort(us.begin(), us.end(), heavy_first);
+  std::sort(ug.begin(), ug.end(), heavy_first);
+  std::vector<int4> units_sym, units_gen;
+  tc.unit_wmax = 0;
+  for (const auto* lst : {&us, &ug})
+    for (const auto& x : *lst) {
+      const PairBlock& pb = pbs[x.u.x];
+      if (x.u.y < 0 && x.u.z > 0) return "work unit straddles m3 = 0";
+      const int wb = eofs[pb.eofs + x.u.y + pb.M];
+      const int we = (x.u.z + pb.M + 1 <= 2 * pb.M) ? eofs[pb.eofs + x.u.z + pb.M + 1] : pb.wcount;
+      tc.unit_wmax = std::max(tc.unit_wmax, we - wb);
+    }
+  for (const auto& x : us) units_sym.push_back(x.u);
+  for (const auto& x : ug) units_gen.push_back(x.u);
+  // every (pair block, m3) is covered exactly once: m3 >= 0 by the real-function units,
+  // -M..M by the general ones
+  for (int pass = 0; pass < 2; ++pass) {
+    const auto& lst = pass == 0 ? units_sym : units_gen;
+    for (int i = 0; i < (int)pbs.size(); ++i) {
+      std::vector<int> cover(2 * pbs[i].M + 1, 0);
+      for (const auto& u : lst)
+        if (u.x == i)
+          for (int m3 = u.y; m3 <= u.z; ++m3) cover[m3 + pbs[i].M]++;
+      for (int m3 = -pbs[i].M; m3 <= pbs[i].M; ++m3)
+        if (cover[m3 + pbs[i].M] != ((pass == 0 && m3 < 0) ? 0 : 1)) return "coupling work units do not cover m3";
+    }
+  }
+  tc.n_units_sym = (int)units_sym.size();
+  tc.n_units_gen = (int)units_gen.size();
   std::vector<int> cmir(b.nc);
   for (int i = 0; i < b.nc; ++i) cmir[i] = b.coff[b.c_l[i] / 2] + b.c_l[i] - b.c_m[i];
   tc.KP = (b.n_lt() + 31) / 32 * 32;
@@ -201,11 +288,19 @@ std::string setup_tc(tp3_ctx* c) {
   cudaError_t e;
   if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
       (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
-      (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
-      (e = upload(c, cmir, &tc.cmir)) != cudaSuccess ||
+      (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, chunks_sym, &tc.chunks_sym)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
+      (e = upload(c, cmir, &tc.cmir)) != cudaSuccess || (e = upload(c, doff, &tc.doff)) != cudaSuccess ||
+      (e = upload(c, units_sym, &tc.units_sym)) != cudaSuccess ||
+      (e = upload(c, units_gen, &tc.units_gen)) != cudaSuccess ||
       (e = upload(c, Fhi, &tc.Fhi)) != cudaSuccess || (e = upload(c, Flo, &tc.Flo)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
+  // the split coupling is kept for the autotuner; the fused kernel is the default
+  tc.split = false;
+  tc.split_ok = tp3::couple_split_smem_d(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
+             tp3::couple_split_smem_t(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
+             tp3::couple_split_configure(t, tc) == cudaSuccess;
+  cudaGetLastError();
   if ((e = encode_2d_bf16(c, &c->maps.b_hi, (void*)tc.Fhi, tc.KP, tc.NP, 32, 256)) != cudaSuccess ||
       (e = encode_2d_bf16(c, &c->maps.b_lo, (void*)tc.Flo, tc.KP, tc.NP, 32, 256)) != cudaSuccess)
     return "tensor map encoding of F failed";
@@ -216,7 +311,8 @@ std::string setup_tc(tp3_ctx* c) {
 // ---- scratch ------------------------------------------------------------------
 void free_scratch(tp3_ctx* c) {
   cudaFree(c->d_coeff); cudaFree(c->d_cc); cudaFree(c->d_T); cudaFree(c->d_part); cudaFree(c->d_E);
-  cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab); cudaFree(c->d_sym);
+  cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab); cudaFree(c->d_sym); cudaFree(c->d_D);
+  c->d_D = nullptr;
   cudaFreeHost(c->h_coeff); cudaFreeHost(c->h_E);
   c->d_sym = nullptr;
   c->d_coeff = nullptr; c->d_cc = nullptr; c->d_T = nullptr; c->d_part = nullptr; c->d_E = nullptr;
@@ -243,6 +339,8 @@ int ensure_cap(tp3_ctx* c, int n) {
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * t.klength * sizeof(double))) != cudaSuccess) ||
       (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
+      (c->tc_ok && c->tc.split_ok &&
+       (e = cudaMalloc(&c->d_D, (size_t)c->tc.dsub * c->tc.dstride * sizeof(float2))) != cudaSuccess) ||
       (e = cudaMallocHost(&c->h_coeff, (size_t)n * t.K * ncoef * 2 * sizeof(double))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_E, (size_t)n * sizeof(double))) != cudaSuccess) {
     free_scratch(c);
@@ -286,9 +384,13 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
   if (c->mode == TP3_MODE_TC_BF16X3) {
     if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
-    if ((e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo,
-                                     want_T32 ? c->d_T : nullptr, c->stream)) != cudaSuccess)
-      return cuda_fail(c, e, "couple_pair");
+    if (c->tc.split)
+      e = tp3::launch_couple_split(t, c->tc, n, c->d_cc, c->d_sym, c->d_D, c->d_Thi, c->d_Tlo,
+                                   want_T32 ? c->d_T : nullptr, c->stream);
+    else
+      e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, want_T32 ? c->d_T : nullptr,
+                                  c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "coupling");
   } else {
     if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
     if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)

@@ -54,6 +54,7 @@ struct tp3_ctx {
   float* d_c3 = nullptr;       // [klength][G] (one proposal)
   int* d_err = nullptr;        // device error flag (timeouts)
   int* d_sym = nullptr;        // [cap] real-function symmetry flag per proposal
+  float2* d_D = nullptr;       // [dsub][dstride] pair-coupled D of the split coupling
   double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
   double* h_E = nullptr;       // pinned [cap]
   int* h_err = nullptr;        // pinned

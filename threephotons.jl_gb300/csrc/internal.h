@@ -62,6 +62,19 @@ struct TcTables {
   bool w_smem = false;
   size_t couple_smem = 0;
   const int2* chunks = nullptr;  // (k1 high, k1 low) runs of shells, pairs per run <= pmax
+  const int2* chunks_sym = nullptr;  // same for the real-function path (rows of SDhp)
+  int nchunks_sym = 0, pmax_sym = 0, SDhp = 0;
+  // split coupling (kernels_couple.cu)
+  bool split = false;            // use the two-kernel coupling
+  bool split_ok = false;         // the two-kernel coupling fits this shape
+  const long long* doff = nullptr;  // [n_pb] offset of each pair block's D rows in one proposal's D
+  long long dstride = 0;         // float2 per proposal of D
+  int dsub = 1;                  // proposals per (D, T) kernel pair, sized so D stays in L2
+  const int4* units_sym = nullptr;  // (pair block, m3 lo, m3 hi) work units, real-function path
+  const int4* units_gen = nullptr;  // same for the general path
+  int n_units_sym = 0, n_units_gen = 0;
+  int dmax = 0;                  // largest l1 (or l2) of any block
+  int unit_wmax = 0;             // largest 3j row range of any unit (floats)
   const int* cm = nullptr;       // [nc] m of each compact coefficient
   const int* cmir = nullptr;     // [nc] compact index of (l, -m)
   int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
@@ -90,6 +103,11 @@ cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, co
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
                               const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s);
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s);
+size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
+size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
+cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);
+cudaError_t launch_couple_split(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
+                                float2* Dg, __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
 
 int plain_ncg(const DevTables& t);
 // Detail text returned by tp3_last_error(NULL) on this thread.

@@ -112,18 +112,24 @@ template <int MAXS, bool W_SMEM>
 __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
     const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
     const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
-    const int2* __restrict__ chunks, int nchunks, int pmax, int SDp, int wsmem, int klp, int KP,
+    const int2* __restrict__ chunks_gen, int nchunks_gen, int pmax_gen, int SDp,
+    const int2* __restrict__ chunks_sym, int nchunks_sym, int pmax_sym, int SDhp, int wsmem, int klp, int KP,
     const int* __restrict__ symflags, __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo,
     float* __restrict__ T32, int ldT32) {
   extern __shared__ __align__(16) float smf[];
   const int prop = blockIdx.y;
   // real-function coefficients: only m3 >= 0 of D is formed, D[-m3] = (-1)^m3 conj(D[m3])
-  // and T = Re(D[0] c[0]) + 2 sum_{m3 > 0} Re(D[m3] c[m3])
+  // and T = Re(D[0] c[0]) + 2 sum_{m3 > 0} Re(D[m3] c[m3]); D rows then hold m3 = 0..l3
+  // only (row length SDhp instead of SDp), so a chunk holds about twice the shell pairs.
   const bool sym = symflags[prop] != 0;
+  const int2* chunks = sym ? chunks_sym : chunks_gen;
+  const int nchunks = sym ? nchunks_sym : nchunks_gen;
+  const int pmax = sym ? pmax_sym : pmax_gen;
+  const int rowD = sym ? SDhp : SDp;
   const PairBlock pb = pbs[blockIdx.x];
   float2* sc = reinterpret_cast<float2*>(smf);                 // [K][ncp]
   float* sw = smf + (2 * (size_t)K * ncp + 3) / 4 * 4;          // [wsmem], 16-byte aligned
-  float2* sD = reinterpret_cast<float2*>(sw + (W_SMEM ? wsmem : 0));  // [pmax][SDp]
+  float2* sD = reinterpret_cast<float2*>(sw + (W_SMEM ? wsmem : 0));  // [2][pmax][rowD]
   const float2* src = cc + (size_t)prop * K * nc;
   for (int i = threadIdx.x; i < K * nc; i += blockDim.x) {
     const int k = i / nc, c = i - k * nc;
@@ -148,7 +154,7 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
   // of the two phases overlap across warps.
   for (int ch = 0; ch < nchunks; ++ch) {
     const int k1hi = chunks[ch].x, k1lo = chunks[ch].y;
-    float2* Dbuf = sD + (size_t)(ch & 1) * pmax * SDp;
+    float2* Dbuf = sD + (size_t)(ch & 1) * pmax * rowD;
     int npairs = 0;
     for (int k1 = k1hi; k1 >= k1lo; --k1) npairs += k1 + 1;
     // ---- phase 1: longest diagonals (small |m3|) first ----
@@ -186,14 +192,19 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
           }
         }
       }
-      float2* d = Dbuf + (size_t)p * SDp;
+      float2* d = Dbuf + (size_t)p * rowD;
       int dofs = 0;
 #pragma unroll
       for (int s = 0; s < MAXS; ++s) {
         if (s < nl3) {
           const int l3 = l3min + 2 * s;
-          if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
-          dofs += 2 * l3 + 1;
+          if (sym) {
+            if (m3 <= l3) d[dofs + m3] = make_float2(ar[s], ai[s]);
+            dofs += l3 + 1;
+          } else {
+            if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
+            dofs += 2 * l3 + 1;
+          }
         }
       }
     }
@@ -222,7 +233,8 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
       while (t > ra) { t -= ra + 1; ++ra; }
       const int rb = t;  // k2 quad ra, k3 quad rb <= ra
       const int l3 = l3min + 2 * s;
-      const int dofs = s * (2 * l3min + 2 * s - 1);  // sum_{j<s} (2 (l3min + 2j) + 1)
+      // row offset of l3: sum_{j<s} (l3_j + 1) (m3 >= 0 rows) or sum_{j<s} (2 l3_j + 1), centred
+      const int dofs = sym ? s * (l3min + s) : s * (2 * l3min + 2 * s - 1) + l3min + 2 * s;
       const int off3 = coff[l3 >> 1] + l3;
       const float2* drow[4];
       const float2* crow[4];
@@ -230,7 +242,7 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
       for (int i = 0; i < 4; ++i) {
         const int k2 = min(4 * ra + i, k1);
         const int k3 = min(4 * rb + i, k1);
-        drow[i] = Dbuf + (size_t)(pbase + k2) * SDp + dofs + l3;
+        drow[i] = Dbuf + (size_t)(pbase + k2) * rowD + dofs;
         crow[i] = sc + k3 * ncp + off3;
       }
       float acc[4][4];
@@ -629,8 +641,9 @@ cudaError_t tc_configure() {
   if ((e = cudaFuncSetAttribute(k_couple_pair<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
       cudaSuccess)                                                                                     \
     return e;
-  TP3_CP_ATTR(4, true) TP3_CP_ATTR(8, true) TP3_CP_ATTR(12, true) TP3_CP_ATTR(16, true)
-  TP3_CP_ATTR(4, false) TP3_CP_ATTR(8, false) TP3_CP_ATTR(12, false) TP3_CP_ATTR(16, false)
+  TP3_CP_ATTR(4, true) TP3_CP_ATTR(8, true) TP3_CP_ATTR(10, true) TP3_CP_ATTR(12, true) TP3_CP_ATTR(16, true)
+  TP3_CP_ATTR(4, false) TP3_CP_ATTR(8, false) TP3_CP_ATTR(10, false) TP3_CP_ATTR(12, false)
+  TP3_CP_ATTR(16, false)
 #undef TP3_CP_ATTR
   return cudaSuccess;
 }
@@ -646,17 +659,19 @@ cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, co
   dim3 grid(tc.n_pb, n);
   const size_t smem = tc.couple_smem;
 #define TP3_CP_LAUNCH(S, W)                                                                                \
-  k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, \
-                                                        tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,   \
-                                                        tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, T32, t.n_ltp)
+  k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(                                                  \
+      cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,         \
+      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, T32, t.n_ltp)
   if (tc.w_smem) {
     if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true);
     else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true);
+    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, true);
     else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, true);
     else TP3_CP_LAUNCH(16, true);
   } else {
     if (tc.maxs <= 4) TP3_CP_LAUNCH(4, false);
     else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, false);
+    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, false);
     else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, false);
     else TP3_CP_LAUNCH(16, false);
   }
