@@ -125,3 +125,39 @@ def c3_to_5d(c3: np.ndarray, K: int, N: int) -> np.ndarray:
                 t[:, :, k3 - 1, k2 - 1, k1 - 1] = c3[:, i].reshape(N, 2 * N, order="F")
                 i += 1
     return t
+
+
+def c3_pair_form(b: OracleBasis, coeff: np.ndarray) -> np.ndarray:
+    """c3 for any lambda in FP64, grouped by Fourier pair (m2, m3) up to sign:
+    c3[g, ki] = sum_q cos(m2 a + m3 b) H[q, ki],  H[q, ki] = sum_{j in q} P_j(ki) T[ki, lt(j)],
+    P_j(ki) = w_j sphPlm(l1,m1,th_k1) sphPlm(l2,m2,th_k2) sphPlm(l3,m3,th_k3) with
+    th_k = acos(k lambda dq / 4pi) (correlations.jl:94, 137-148)."""
+    from .basis import qlist
+    from .sh import sphPlm, alpharange, alpharange_2pi
+    T = triple_products(b, coeff)
+    lt = lt_of_entry(b)
+    th = qlist(b)
+    Y = {(k, l, m): sphPlm(l, m, th[k]) for k in range(b.K) for l in b.lrange for m in range(-l, l + 1)}
+    ks = b.klist - 1
+    l1, m1, l2, m2, l3, m3 = (b.indices[r] for r in range(3, 9))
+    qid = {}
+    Hrows = []
+    for j in range(b.basislen):
+        key = (int(m2[j]), int(m3[j]))
+        if key[0] < 0 or (key[0] == 0 and key[1] < 0):
+            key = (-key[0], -key[1])
+        if key not in qid:
+            qid[key] = len(Hrows)
+            Hrows.append(np.zeros(b.klength))
+        y1 = np.array([Y[(k, l1[j], m1[j])] for k in range(b.K)])
+        y2 = np.array([Y[(k, l2[j], m2[j])] for k in range(b.K)])
+        y3 = np.array([Y[(k, l3[j], m3[j])] for k in range(b.K)])
+        P = b.wignerlist[j] * y1[ks[:, 0]] * y2[ks[:, 1]] * y3[ks[:, 2]]
+        Hrows[qid[key]] += P * T[:, lt[j]]
+    N = b.N
+    A, Bg = np.meshgrid(alpharange(N), alpharange_2pi(2 * N), indexing="ij")
+    a = A.reshape(-1, order="F")
+    be = Bg.reshape(-1, order="F")
+    keys = sorted(qid, key=qid.get)
+    Cq = np.cos(np.outer(a, [k[0] for k in keys]) + np.outer(be, [k[1] for k in keys]))
+    return Cq @ np.stack(Hrows)

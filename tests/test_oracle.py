@@ -179,3 +179,16 @@ def test_oracle_pinned_to_reference_cuda_kernel(config1):
     ref = d["c3_refcuda"].astype(np.float64)
     for mine in (config1["c3_refform"], config1["c3_fp64"]):
         assert np.abs(ref - mine).sum() / np.abs(mine).sum() < 1e-5
+
+
+def test_kat6_lambda_forms_agree(config1):
+    """KAT-6: at lambda = 2.5 (tests/test_cuda.jl:2) the reference's B * PA form and the
+    Fourier-pair form agree."""
+    import math
+    from oracle.c3 import c3_pair_form
+    p = config1["params"]
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"], lam=2.5, dq=math.pi / 8)
+    B32, P32 = reference_tables(b)
+    c3r = c3_reference_form(b, config1["coeff"], B32, P32)
+    c3q = c3_pair_form(b, config1["coeff"])
+    assert np.abs(c3r - c3q).sum() / np.abs(c3q).sum() < 1e-6

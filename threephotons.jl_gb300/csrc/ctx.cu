@@ -312,7 +312,9 @@ std::string setup_tc(tp3_ctx* c) {
 void free_scratch(tp3_ctx* c) {
   cudaFree(c->d_coeff); cudaFree(c->d_cc); cudaFree(c->d_T); cudaFree(c->d_part); cudaFree(c->d_E);
   cudaFree(c->d_Thi); cudaFree(c->d_Tlo); cudaFree(c->d_Eslab); cudaFree(c->d_sym); cudaFree(c->d_D);
+  cudaFree(c->d_H);
   c->d_D = nullptr;
+  c->d_H = nullptr;
   cudaFreeHost(c->h_coeff); cudaFreeHost(c->h_E);
   c->d_sym = nullptr;
   c->d_coeff = nullptr; c->d_cc = nullptr; c->d_T = nullptr; c->d_part = nullptr; c->d_E = nullptr;
@@ -339,6 +341,7 @@ int ensure_cap(tp3_ctx* c, int n) {
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * t.klength * sizeof(double))) != cudaSuccess) ||
       (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
+      (t.nqp > 0 && (e = cudaMalloc(&c->d_H, (size_t)n * t.klp * t.nqp * sizeof(float))) != cudaSuccess) ||
       (c->tc_ok && c->tc.split_ok &&
        (e = cudaMalloc(&c->d_D, (size_t)c->tc.dsub * c->tc.dstride * sizeof(float2))) != cudaSuccess) ||
       (e = cudaMallocHost(&c->h_coeff, (size_t)n * t.K * ncoef * 2 * sizeof(double))) != cudaSuccess ||
@@ -349,6 +352,8 @@ int ensure_cap(tp3_ctx* c, int n) {
   }
   // padding rows/columns of the coupling outputs stay zero for the lifetime of the buffers
   if ((e = cudaMemset(c->d_T, 0, tbytes)) != cudaSuccess) return cuda_fail(c, e, "cudaMemset T");
+  if (t.nqp > 0 && (e = cudaMemset(c->d_H, 0, (size_t)n * t.klp * t.nqp * sizeof(float))) != cudaSuccess)
+    return cuda_fail(c, e, "cudaMemset H");
   if (c->tc_ok) {
     if ((e = cudaMemset(c->d_Thi, 0, tcb)) != cudaSuccess || (e = cudaMemset(c->d_Tlo, 0, tcb)) != cudaSuccess)
       return cuda_fail(c, e, "cudaMemset T hi/lo");
@@ -395,9 +400,14 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
     if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
     if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "couple_direct");
+    if (t.nqp > 0 && (e = tp3::launch_build_H(t, n, c->d_T, c->d_H, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "build_H");
   }
   return TP3_OK;
 }
+
+// operand of the plain angular kernel: T (lambda = 0) or H (lambda != 0)
+const float* plain_A(tp3_ctx* c) { return c->t.nqp > 0 ? c->d_H : c->d_T; }
 
 // Score n proposals whose FP64 coefficients are already in d_coeff (device).
 int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool compact = false) {
@@ -416,7 +426,7 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
       return cuda_fail(c, e, "finalize_slabs");
   } else {
     const int ncg = tp3::plain_ncg(t);
-    if ((e = tp3::launch_angular_plain(t, n, c->d_T, c->d_qfull, c->d_part, ncg, nullptr, c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_angular_plain(t, n, plain_A(c), c->d_qfull, c->d_part, ncg, nullptr, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "angular_plain");
     if (pr) cudaEventRecord(b, c->stream);
     if ((e = tp3::launch_finalize(t, n, c->d_part, ncg, c->d_Qfull, 1, d_E, c->stream)) != cudaSuccess)
@@ -511,12 +521,14 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   std::string m = tp3::build_basis(c->b, L, LMAX, N, K, lambda, dq);
   if (!m.empty()) { delete c; return fail(nullptr, TP3_ERR_ARG, m); }
   Basis& b = c->b;
-  if (lambda != 0.0) {
+  if (std::fabs((double)K * lambda * dq / (4.0 * M_PI)) > 1.0) {
     delete c;
-    return fail(nullptr, TP3_ERR_UNSUPPORTED, "lambda != 0 (Ewald curvature) is not supported by this build");
+    return fail(nullptr, TP3_ERR_ARG, "K * lambda * dq / (4 pi) exceeds 1: theta_k = acos(k lambda dq / 4pi) undefined");
   }
   if (b.nc > 1024) { delete c; return fail(nullptr, TP3_ERR_UNSUPPORTED, "L too large: more than 1024 coefficients per shell"); }
-  if ((size_t)b.K * b.nc * sizeof(float2) > (size_t)tp3::kPlainMaxSmem) {
+  if ((size_t)b.K * b.nc * sizeof(float2) > (size_t)tp3::kPlainMaxSmem ||
+      (lambda != 0.0 && ((size_t)b.K * b.nc + 32 * ((size_t)(b.n_lt() + 63) / 64 * 64)) * sizeof(float) >
+                            (size_t)tp3::kPlainMaxSmem)) {
     delete c;
     return fail(nullptr, TP3_ERR_UNSUPPORTED, "K x coefficients per shell exceed the coupling kernel's shared memory");
   }
@@ -557,14 +569,54 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   for (int i = 0; i < t.n_lt; ++i) lt[i] = make_int2(b.lt_jstart[i], b.lt_jcount[i]);
   std::vector<int4> kl(b.klength);
   for (int i = 0; i < b.klength; ++i) kl[i] = make_int4(b.k1s[i], b.k2s[i], b.k3s[i], (int)b.tf[i]);
-  // F on the full grid (plain path)
-  Basis bf = b;
-  tp3::fold_grid(bf, false);
-  std::vector<double> F64;
-  tp3::build_F(bf, F64);
-  std::vector<float> Ffull((size_t)t.G * t.n_ltp, 0.f);
-  for (int g = 0; g < t.G; ++g)
-    for (int l = 0; l < t.n_lt; ++l) Ffull[(size_t)g * t.n_ltp + l] = (float)F64[(size_t)g * t.n_lt + l];
+  // F on the full grid (plain path, lambda = 0)
+  std::vector<float> Ffull;
+  // lambda != 0: sphPlm(l, m, theta_k) per shell, basis entries grouped by (m2, m3) up to sign,
+  // and the cosine table of those pairs on the full grid
+  std::vector<float> Ytab, Cq;
+  std::vector<int> lt_of_j, qstart, qlist;
+  if (lambda == 0.0) {
+    Basis bf = b;
+    tp3::fold_grid(bf, false);
+    std::vector<double> F64;
+    tp3::build_F(bf, F64);
+    Ffull.assign((size_t)t.G * t.n_ltp, 0.f);
+    for (int g = 0; g < t.G; ++g)
+      for (int l = 0; l < t.n_lt; ++l) Ffull[(size_t)g * t.n_ltp + l] = (float)F64[(size_t)g * t.n_lt + l];
+  } else {
+    Ytab.resize((size_t)K * b.nc);
+    for (int k = 0; k < K; ++k) {
+      const double x = std::cos(std::acos((k + 1) * lambda * dq / (4.0 * M_PI)));  // as the reference: cos(qlist[k])
+      for (int cix = 0; cix < b.nc; ++cix) Ytab[(size_t)k * b.nc + cix] = (float)tp3::sphPlm_x(b.c_l[cix], b.c_m[cix], x);
+    }
+    lt_of_j.resize(b.basislen());
+    for (int tt = 0; tt < b.n_lt(); ++tt)
+      for (int jj = 0; jj < b.lt_jcount[tt]; ++jj) lt_of_j[b.lt_jstart[tt] + jj] = tt;
+    std::map<std::pair<int, int>, int> qid;
+    std::vector<std::pair<int, int>> qs;
+    std::vector<int> q_of_j(b.basislen());
+    for (int j = 0; j < b.basislen(); ++j) {
+      int m2 = b.m2[j], m3 = b.m3[j];
+      if (m2 < 0 || (m2 == 0 && m3 < 0)) { m2 = -m2; m3 = -m3; }
+      auto f = qid.find({m2, m3});
+      if (f == qid.end()) { f = qid.emplace(std::make_pair(m2, m3), (int)qs.size()).first; qs.push_back({m2, m3}); }
+      q_of_j[j] = f->second;
+    }
+    t.nq = (int)qs.size();
+    t.nqp = (t.nq + 15) / 16 * 16;
+    qstart.assign(t.nq + 1, 0);
+    for (int j = 0; j < b.basislen(); ++j) qstart[q_of_j[j] + 1]++;
+    for (int q = 0; q < t.nq; ++q) qstart[q + 1] += qstart[q];
+    qlist.resize(b.basislen());
+    std::vector<int> fillp(qstart.begin(), qstart.end() - 1);
+    for (int j = 0; j < b.basislen(); ++j) qlist[fillp[q_of_j[j]]++] = j;
+    Cq.assign((size_t)t.G * t.nqp, 0.f);
+    for (int g = 0; g < t.G; ++g) {
+      const int a = g % N, bb = g / N;
+      const double al = (a + 0.5) * M_PI / N, be = (bb + 0.5) * M_PI / N;
+      for (int q = 0; q < t.nq; ++q) Cq[(size_t)g * t.nqp + q] = (float)std::cos(qs[q].first * al + qs[q].second * be);
+    }
+  }
 
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -581,6 +633,9 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
       (e = upload(c, kl, &t.kl)) != cudaSuccess || (e = upload(c, b.tf, &t.tf)) != cudaSuccess ||
       (e = upload(c, Ffull, &t.Ffull)) != cudaSuccess || (e = upload(c, b.u_to_g, &t.u_to_g)) != cudaSuccess ||
       (e = upload(c, b.g_to_u, &t.g_to_u)) != cudaSuccess || (e = tp3::plain_configure()) != cudaSuccess ||
+      (e = upload(c, Ytab, &t.Ytab)) != cudaSuccess || (e = upload(c, lt_of_j, &t.lt_of_j)) != cudaSuccess ||
+      (e = upload(c, qstart, &t.qstart)) != cudaSuccess || (e = upload(c, qlist, &t.qlist)) != cudaSuccess ||
+      (e = upload(c, Cq, &t.Cq)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess || (e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_err, sizeof(int))) != cudaSuccess) {
     std::string msg = std::string("table upload: ") + cudaGetErrorString(e);
@@ -710,7 +765,7 @@ int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {
   if (c->mode == TP3_MODE_TC_BF16X3)
     e = tp3::launch_angular_tc(t, c->tc, c->maps, 1, nullptr, nullptr, nullptr, c->d_c3, c->d_err, c->stream);
   else
-    e = tp3::launch_angular_plain(t, 1, c->d_T, nullptr, nullptr, tp3::plain_ncg(t), c->d_c3, c->stream);
+    e = tp3::launch_angular_plain(t, 1, plain_A(c), nullptr, nullptr, tp3::plain_ncg(t), c->d_c3, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "angular store");
   // device layout [ki][g] is the column-major G x klength layout of the reference
   if ((e = cudaMemcpyAsync(out, c->d_c3, (size_t)t.klength * t.G * sizeof(float), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||

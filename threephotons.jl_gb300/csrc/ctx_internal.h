@@ -55,6 +55,7 @@ struct tp3_ctx {
   int* d_err = nullptr;        // device error flag (timeouts)
   int* d_sym = nullptr;        // [cap] real-function symmetry flag per proposal
   float2* d_D = nullptr;       // [dsub][dstride] pair-coupled D of the split coupling
+  float* d_H = nullptr;        // [cap][klp][nqp] Fourier-pair operand (lambda != 0)
   double* h_coeff = nullptr;   // pinned [cap][K][LMAX^2][2]
   double* h_E = nullptr;       // pinned [cap]
   int* h_err = nullptr;        // pinned

@@ -23,6 +23,13 @@ struct DevTables {
   const double* tf;     // [klength]
   const float* Ffull;   // [G][n_ltp]  fp32, full grid (plain path)
   const int* u_to_g;    // [Gu]
+  // lambda != 0 (shell-dependent Legendre factors): Fourier-pair form of the angular stage
+  int nq = 0, nqp = 0;       // (m2, m3) pairs up to sign, padded to 16 (0 at lambda = 0)
+  const float* Ytab = nullptr;   // [K][nc] sphPlm(l, m, theta_k)
+  const int* lt_of_j = nullptr;  // [basislen]
+  const int* qstart = nullptr;   // [nq + 1] ranges of qlist
+  const int* qlist = nullptr;    // [basislen] basis entries grouped by pair
+  const float* Cq = nullptr;     // [G][nqp] cos(m2 alpha + m3 beta)
   const int* g_to_u;    // [G]
 };
 
@@ -40,6 +47,7 @@ cudaError_t launch_couple_direct(const DevTables& t, int n, const float2* cc, fl
 // Bayes partials: part[prop][cg][klength] (Sp, Sql); ncg column groups over the full grid.
 cudaError_t launch_angular_plain(const DevTables& t, int n, const float* T, const float* q,
                                  double2* part, int ncg, float* c3out, cudaStream_t s);
+cudaError_t launch_build_H(const DevTables& t, int n, const float* T, float* H, cudaStream_t s);
 cudaError_t launch_finalize(const DevTables& t, int n, const double2* part, int ncg,
                             const double* Qs, int mult, double* E, cudaStream_t s);
 

@@ -210,9 +210,6 @@ __global__ void __launch_bounds__(256) k_finalize(const double2* __restrict__ pa
 
 }  // namespace
 
-cudaError_t plain_configure() {
-  return cudaFuncSetAttribute(k_couple_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, kPlainMaxSmem);
-}
 
 int plain_ncg(const DevTables& t) {
   // about 512 grid columns per block, at least one group
@@ -242,13 +239,64 @@ cudaError_t launch_angular_plain(const DevTables& t, int n, const float* T, cons
                                  double2* part, int ncg, float* c3out, cudaStream_t s) {
   const int cpg = ((t.G + ncg - 1) / ncg + 63) / 64 * 64;
   dim3 grid((t.klength + 63) / 64, ncg, n);
-  const int64_t Ts = (int64_t)t.klp * t.n_ltp;
+  // lambda = 0: A = T [klp][n_ltp] against F; otherwise A = H [klp][nqp] against the cosine table
+  const bool hform = t.nqp > 0;
+  const int kd = hform ? t.nqp : t.n_ltp;
+  const float* tab = hform ? t.Cq : t.Ffull;
+  const int64_t Ts = (int64_t)t.klp * kd;
   if (c3out)
-    k_angular_plain<true><<<grid, 256, 0, s>>>(T, t.n_ltp, Ts, t.Ffull, t.n_ltp, t.klength, t.G, cpg,
-                                               nullptr, nullptr, ncg, c3out);
+    k_angular_plain<true><<<grid, 256, 0, s>>>(T, kd, Ts, tab, kd, t.klength, t.G, cpg, nullptr, nullptr, ncg,
+                                               c3out);
   else
-    k_angular_plain<false><<<grid, 256, 0, s>>>(T, t.n_ltp, Ts, t.Ffull, t.n_ltp, t.klength, t.G, cpg,
-                                                q, part, ncg, nullptr);
+    k_angular_plain<false><<<grid, 256, 0, s>>>(T, kd, Ts, tab, kd, t.klength, t.G, cpg, q, part, ncg, nullptr);
+  return cudaGetLastError();
+}
+
+// grid: (ceil(klength/32), ceil(nq/8), n); block 256 (warp w: pair q0 + w; lane: shell triple).
+// H[ki][q] = sum_{j with (m2, m3) = +-q} w_j Y(l1,m1,th_k1) Y(l2,m2,th_k2) Y(l3,m3,th_k3) T[ki][lt(j)]
+// (lambda != 0: the Legendre factors depend on the shells, so the angular stage contracts
+// over Fourier pairs (m2, m3) instead of l-triples; src/correlations.jl:137-148, 182).
+__global__ void __launch_bounds__(256) k_build_H(const float* __restrict__ T, int n_ltp, int64_t T_stride,
+                                                 const float* __restrict__ Ytab, int K, int nc,
+                                                 const float* __restrict__ w, const uint32_t* __restrict__ idx,
+                                                 const int* __restrict__ lt_of_j, const int* __restrict__ qstart,
+                                                 const int* __restrict__ qlist, int nq, const int4* __restrict__ kl,
+                                                 int klength, float* __restrict__ H, int nqp, int64_t H_stride) {
+  extern __shared__ float sm[];
+  float* sY = sm;                      // [K][nc]
+  float* sT = sm + (size_t)K * nc;     // [32][n_ltp]
+  const int prop = blockIdx.z;
+  const int ki0 = blockIdx.x * 32;
+  for (int i = threadIdx.x; i < K * nc; i += blockDim.x) sY[i] = Ytab[i];
+  const float* Tp = T + (int64_t)prop * T_stride;
+  for (int i = threadIdx.x; i < 32 * n_ltp; i += blockDim.x) {
+    const int r = i / n_ltp, c = i - r * n_ltp;
+    sT[i] = ki0 + r < klength ? Tp[(int64_t)(ki0 + r) * n_ltp + c] : 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int q = blockIdx.y * 8 + warp;
+  const int ki = ki0 + lane;
+  if (q >= nq || ki >= klength) return;
+  const int4 k = kl[ki];
+  const float* y1 = sY + k.x * nc;
+  const float* y2 = sY + k.y * nc;
+  const float* y3 = sY + k.z * nc;
+  const float* trow = sT + lane * n_ltp;
+  float acc = 0.f;
+  for (int e = qstart[q]; e < qstart[q + 1]; ++e) {
+    const int j = qlist[e];
+    const uint32_t id = idx[j];
+    acc = fmaf(w[j] * y1[id & 1023u] * y2[(id >> 10) & 1023u] * y3[(id >> 20) & 1023u], trow[lt_of_j[j]], acc);
+  }
+  H[(int64_t)prop * H_stride + (int64_t)ki * nqp + q] = acc;
+}
+
+cudaError_t launch_build_H(const DevTables& t, int n, const float* T, float* H, cudaStream_t s) {
+  const size_t smem = ((size_t)t.K * t.nc + 32 * (size_t)t.n_ltp) * sizeof(float);
+  dim3 grid((t.klength + 31) / 32, (t.nq + 7) / 8, n);
+  k_build_H<<<grid, 256, smem, s>>>(T, t.n_ltp, (int64_t)t.klp * t.n_ltp, t.Ytab, t.K, t.nc, t.w, t.idx, t.lt_of_j,
+                                    t.qstart, t.qlist, t.nq, t.kl, t.klength, H, t.nqp, (int64_t)t.klp * t.nqp);
   return cudaGetLastError();
 }
 
@@ -256,6 +304,12 @@ cudaError_t launch_finalize(const DevTables& t, int n, const double2* part, int 
                             int mult, double* E, cudaStream_t s) {
   k_finalize<<<n, 256, 0, s>>>(part, ncg, t.klength, Qs, t.tf, mult, E);
   return cudaGetLastError();
+}
+
+cudaError_t plain_configure() {
+  cudaError_t e = cudaFuncSetAttribute(k_couple_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, kPlainMaxSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_build_H, cudaFuncAttributeMaxDynamicSharedMemorySize, kPlainMaxSmem);
 }
 
 }  // namespace tp3
