@@ -58,6 +58,7 @@ extern "C" {
 /* Evaluation modes (tp3_set_mode). */
 #define TP3_MODE_PLAIN_FP32 0    /* direct coupling + FP32 SIMT angular contraction, full grid */
 #define TP3_MODE_TC_BF16X3 1     /* pair-factorised coupling + tcgen05 BF16 hi/lo x3 */
+#define TP3_MODE_TC_TF32X3 2     /* pair-factorised coupling + tcgen05 TF32 hi/lo x3 */
 #define TP3_MODE_AUTO (-1)       /* fastest available mode for this shape */
 
 typedef struct tp3_ctx tp3_ctx;

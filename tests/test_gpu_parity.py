@@ -15,7 +15,7 @@ from oracle.c3 import triple_products, c3_lt_form, energy_bayes
 
 pytestmark = pytest.mark.gpu
 
-MODES = [tp3.TP3_MODE_PLAIN_FP32, tp3.TP3_MODE_TC_BF16X3]
+MODES = [tp3.TP3_MODE_PLAIN_FP32, tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3]
 
 
 def rel_l1(a, b):

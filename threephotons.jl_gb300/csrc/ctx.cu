@@ -34,6 +34,8 @@ void tp3::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
 namespace {
 
+bool is_tc(int mode) { return mode == TP3_MODE_TC_BF16X3 || mode == TP3_MODE_TC_TF32X3; }
+
 int fail(tp3_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg; else g_create_error = msg;
   return code;
@@ -113,15 +115,18 @@ std::string build_tc_tables(const Basis& b, std::vector<PairBlock>& pbs, std::ve
   return "";
 }
 
-cudaError_t encode_2d_bf16(tp3_ctx* c, CUtensorMap* m, void* ptr, uint64_t inner, uint64_t rows, uint32_t box_inner,
-                           uint32_t box_rows) {
+// 2-D tensor map over a [rows][inner] K-major operand; the box is one 64-byte row of K
+// (32 bf16 or 16 tf32 elements) by box_rows rows, 64-byte swizzle.
+cudaError_t encode_2d(tp3_ctx* c, CUtensorMap* m, void* ptr, uint64_t inner, uint64_t rows, uint32_t box_rows,
+                      bool f32) {
+  const uint64_t esz = f32 ? 4 : 2;
   cuuint64_t dims[2] = {inner, rows};
-  cuuint64_t strides[1] = {inner * 2};
-  cuuint32_t box[2] = {box_inner, box_rows};
+  cuuint64_t strides[1] = {inner * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(64 / esz), box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, es,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = c->encode(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims,
+                         strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
@@ -164,7 +169,10 @@ std::string setup_tc(tp3_ctx* c) {
   while (need(pmax, true) > limit && pmax > b.K) --pmax;
   if (need(pmax, true) > limit) { tc.w_smem = false; pmax = std::max(b.K, 128); }
   while (need(pmax, false) > limit && pmax > b.K) --pmax;
-  if (need(pmax, tc.w_smem) > limit) return "coupling tile exceeds shared memory";
+  // the fused coupling needs one k1's pairs per chunk in shared memory; when it does not
+  // fit (large K x L) only the split coupling (D through global memory) is used
+  tc.fused_ok = need(pmax, tc.w_smem) <= limit;
+  if (!tc.fused_ok) pmax = b.K;
   tc.pmax = pmax;
   tc.couple_smem = need(pmax, tc.w_smem);
   // real-function path: D rows hold m3 = 0..l3 only, so the same bytes hold more pairs
@@ -189,8 +197,7 @@ std::string setup_tc(tp3_ctx* c) {
   std::vector<int2> chunks = make_chunks(pmax), chunks_sym = make_chunks(tc.pmax_sym);
   tc.nchunks = (int)chunks.size();
   tc.nchunks_sym = (int)chunks_sym.size();
-  if (tc.nchunks_sym > 64) return "too many shell-pair chunks for the coupling kernel";
-  if (tc.nchunks > 64) return "too many shell-pair chunks for the coupling kernel";
+  if (tc.nchunks_sym > 64 || tc.nchunks > 64) tc.fused_ok = false;
   // split coupling: D offsets, L2-sized sub-batches, balanced (pair block, m3 range) units
   const int npairs = b.K * (b.K + 1) / 2;
   std::vector<long long> doff(pbs.size());
@@ -268,16 +275,26 @@ std::string setup_tc(tp3_ctx* c) {
   tc.KP = (b.n_lt() + 31) / 32 * 32;
   tc.nhalf = (b.Gu + 255) / 256;
   tc.NP = 256 * tc.nhalf;
-  // F on the unique grid points, split into bf16 hi + lo
+  // F on the unique grid points, split into bf16 hi + lo and into tf32 hi + fp32 lo
   std::vector<double> F;
   tp3::build_F(b, F);
   std::vector<__nv_bfloat16> Fhi((size_t)tc.NP * tc.KP, __float2bfloat16(0.f)), Flo(Fhi);
+  std::vector<float> Fhi32((size_t)tc.NP * tc.KP, 0.f), Flo32(Fhi32);
   for (int u = 0; u < b.Gu; ++u)
     for (int l = 0; l < b.n_lt(); ++l) {
-      const float v = (float)F[(size_t)u * b.n_lt() + l];
+      const double v64 = F[(size_t)u * b.n_lt() + l];
+      const float v = (float)v64;
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
       Fhi[(size_t)u * tc.KP + l] = hi;
       Flo[(size_t)u * tc.KP + l] = __float2bfloat16_rn(v - __bfloat162float(hi));
+      // tf32: round the fp32 value to 10 explicit mantissa bits (nearest, ties away from zero)
+      uint32_t bits;
+      std::memcpy(&bits, &v, 4);
+      bits = (bits + 0x1000u) & ~0x1FFFu;
+      float h32;
+      std::memcpy(&h32, &bits, 4);
+      Fhi32[(size_t)u * tc.KP + l] = h32;
+      Flo32[(size_t)u * tc.KP + l] = (float)(v64 - (double)h32);
     }
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -293,17 +310,22 @@ std::string setup_tc(tp3_ctx* c) {
       (e = upload(c, units_sym, &tc.units_sym)) != cudaSuccess ||
       (e = upload(c, units_gen, &tc.units_gen)) != cudaSuccess ||
       (e = upload(c, Fhi, &tc.Fhi)) != cudaSuccess || (e = upload(c, Flo, &tc.Flo)) != cudaSuccess ||
+      (e = upload(c, Fhi32, &tc.Fhi32)) != cudaSuccess || (e = upload(c, Flo32, &tc.Flo32)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
-  // the split coupling is kept for the autotuner; the fused kernel is the default
-  tc.split = false;
+  // the split coupling is kept for the autotuner and for shapes the fused kernel cannot hold
   tc.split_ok = tp3::couple_split_smem_d(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
              tp3::couple_split_smem_t(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
              tp3::couple_split_configure(t, tc) == cudaSuccess;
   cudaGetLastError();
-  if ((e = encode_2d_bf16(c, &c->maps.b_hi, (void*)tc.Fhi, tc.KP, tc.NP, 32, 256)) != cudaSuccess ||
-      (e = encode_2d_bf16(c, &c->maps.b_lo, (void*)tc.Flo, tc.KP, tc.NP, 32, 256)) != cudaSuccess)
+  if ((e = encode_2d(c, &c->maps.b_hi, (void*)tc.Fhi, tc.KP, tc.NP, 256, false)) != cudaSuccess ||
+      (e = encode_2d(c, &c->maps.b_lo, (void*)tc.Flo, tc.KP, tc.NP, 256, false)) != cudaSuccess ||
+      (e = encode_2d(c, &c->maps32.b_hi, (void*)tc.Fhi32, tc.KP, tc.NP, 256, true)) != cudaSuccess ||
+      (e = encode_2d(c, &c->maps32.b_lo, (void*)tc.Flo32, tc.KP, tc.NP, 256, true)) != cudaSuccess)
     return "tensor map encoding of F failed";
+  cudaGetLastError();
+  if (!tc.fused_ok && !tc.split_ok) return "coupling tile exceeds shared memory";
+  tc.split = !tc.fused_ok;
   (void)t;
   return "";
 }
@@ -324,14 +346,18 @@ void free_scratch(tp3_ctx* c) {
 }
 
 int ensure_cap(tp3_ctx* c, int n) {
-  if (n <= c->cap) return TP3_OK;
+  const bool need4 = c->mode == TP3_MODE_TC_TF32X3 && c->t_elem != 4;
+  if (n <= c->cap && !need4) return TP3_OK;
+  if (n < c->cap) n = c->cap;
   free_scratch(c);
   const auto& t = c->t;
   const int ncg = tp3::plain_ncg(t);
   const size_t ncoef = (size_t)t.LMAX * t.LMAX;
   cudaError_t e;
   const size_t tbytes = (size_t)n * t.klp * t.n_ltp * sizeof(float);
-  const size_t tcb = c->tc_ok ? (size_t)n * t.klp * c->tc.KP * sizeof(__nv_bfloat16) : 0;
+  // T operands: 2 bytes per element (bf16), 4 once the tf32 mode has been selected
+  const int elem = (c->mode == TP3_MODE_TC_TF32X3 || c->t_elem == 4) ? 4 : 2;
+  const size_t tcb = c->tc_ok ? (size_t)n * t.klp * c->tc.KP * elem : 0;
   if ((e = cudaMalloc(&c->d_coeff, (size_t)n * t.K * ncoef * sizeof(double2))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_cc, (size_t)n * t.K * t.nc * sizeof(float2))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_T, tbytes)) != cudaSuccess ||
@@ -357,11 +383,15 @@ int ensure_cap(tp3_ctx* c, int n) {
   if (c->tc_ok) {
     if ((e = cudaMemset(c->d_Thi, 0, tcb)) != cudaSuccess || (e = cudaMemset(c->d_Tlo, 0, tcb)) != cudaSuccess)
       return cuda_fail(c, e, "cudaMemset T hi/lo");
-    if ((e = encode_2d_bf16(c, &c->maps.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 32, 128)) != cudaSuccess ||
-        (e = encode_2d_bf16(c, &c->maps.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 32, 128)) != cudaSuccess)
+    if ((e = encode_2d(c, &c->maps.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 128, false)) != cudaSuccess ||
+        (e = encode_2d(c, &c->maps.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 128, false)) != cudaSuccess ||
+        (elem == 4 &&
+         ((e = encode_2d(c, &c->maps32.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 128, true)) != cudaSuccess ||
+          (e = encode_2d(c, &c->maps32.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 128, true)) != cudaSuccess)))
       return fail(c, TP3_ERR_CUDA, "tensor map encoding of T failed");
   }
   c->cap = n;
+  c->t_elem = elem;
   ++c->scratch_gen;
   return TP3_OK;
 }
@@ -386,15 +416,15 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
   const auto& t = c->t;
   cudaError_t e;
   const tp3::CoeffLayout lay = compact ? tp3::CoeffLayout{t.cident, t.nc} : tp3::CoeffLayout{t.csean, t.LMAX * t.LMAX};
-  if (c->mode == TP3_MODE_TC_BF16X3) {
+  if (is_tc(c->mode)) {
     if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
     if (c->tc.split)
       e = tp3::launch_couple_split(t, c->tc, n, c->d_cc, c->d_sym, c->d_D, c->d_Thi, c->d_Tlo,
-                                   want_T32 ? c->d_T : nullptr, c->stream);
+                                   c->mode == TP3_MODE_TC_TF32X3, want_T32 ? c->d_T : nullptr, c->stream);
     else
-      e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, want_T32 ? c->d_T : nullptr,
-                                  c->stream);
+      e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, c->mode == TP3_MODE_TC_TF32X3,
+                                  want_T32 ? c->d_T : nullptr, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "coupling");
   } else {
     if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
@@ -417,9 +447,10 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
   if (int r = run_coupling(c, n, d_coeff, false, compact)) return r;
   cudaEvent_t a, b;
   int pr = prof_begin(c, &a, &b);
-  if (c->mode == TP3_MODE_TC_BF16X3) {
-    if ((e = tp3::launch_angular_tc(t, c->tc, c->maps, n, c->d_qt, c->d_Qfold, c->d_Eslab, nullptr, c->d_err,
-                                    c->stream)) != cudaSuccess)
+  if (is_tc(c->mode)) {
+    const bool tf = c->mode == TP3_MODE_TC_TF32X3;
+    if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, c->d_qt, c->d_Qfold, c->d_Eslab, nullptr,
+                                    c->d_err, tf, c->stream)) != cudaSuccess)
       return cuda_fail(c, e, "angular_tc");
     if (pr) cudaEventRecord(b, c->stream);
     if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream)) != cudaSuccess)
@@ -673,9 +704,8 @@ int tp3_set_stream(tp3_ctx* c, void* s) {
 int tp3_set_mode(tp3_ctx* c, int mode) {
   if (int r = check_ctx(c)) return r;
   if (mode == TP3_MODE_AUTO) mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
-  if (mode == TP3_MODE_TC_BF16X3 && !c->tc_ok)
-    return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core mode unavailable: " + c->tc_why);
-  if (mode != TP3_MODE_PLAIN_FP32 && mode != TP3_MODE_TC_BF16X3) return fail(c, TP3_ERR_ARG, "unknown mode");
+  if (is_tc(mode) && !c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core mode unavailable: " + c->tc_why);
+  if (mode != TP3_MODE_PLAIN_FP32 && !is_tc(mode)) return fail(c, TP3_ERR_ARG, "unknown mode");
   c->mode = mode;
   return TP3_OK;
 }
@@ -762,8 +792,9 @@ int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {
   if ((e = cudaMemcpyAsync(c->d_coeff, c->h_coeff, nco * sizeof(double2), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
     return cuda_fail(c, e, "H2D coeff");
   if (int r = run_coupling(c, 1, c->d_coeff, false)) return r;
-  if (c->mode == TP3_MODE_TC_BF16X3)
-    e = tp3::launch_angular_tc(t, c->tc, c->maps, 1, nullptr, nullptr, nullptr, c->d_c3, c->d_err, c->stream);
+  if (is_tc(c->mode))
+    e = tp3::launch_angular_tc(t, c->tc, c->mode == TP3_MODE_TC_TF32X3 ? c->maps32 : c->maps, 1, nullptr, nullptr,
+                               nullptr, c->d_c3, c->d_err, c->mode == TP3_MODE_TC_TF32X3, c->stream);
   else
     e = tp3::launch_angular_plain(t, 1, plain_A(c), nullptr, nullptr, tp3::plain_ncg(t), c->d_c3, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "angular store");

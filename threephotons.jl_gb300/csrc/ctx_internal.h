@@ -31,7 +31,8 @@ struct tp3_ctx {
   std::string err;
   std::vector<void*> allocs;  // table allocations, freed at destroy
   tp3::EncodeTiledFn encode = nullptr;
-  tp3::TcMaps maps{};
+  tp3::TcMaps maps{};    // bf16 operands
+  tp3::TcMaps maps32{};  // tf32 operands
 
   // histogram
   bool has_hist = false;
@@ -43,6 +44,7 @@ struct tp3_ctx {
   // scratch (sized for cap proposals)
   int cap = 0;
   int scratch_gen = 0;         // incremented whenever the scratch below is reallocated
+  int t_elem = 2;              // bytes per element of the T operand buffers (2 bf16, 4 tf32)
   double2* d_coeff = nullptr;  // [cap][K][LMAX^2]
   float2* d_cc = nullptr;      // [cap][K][nc]
   float* d_T = nullptr;        // [cap][klp][n_ltp]      plain path

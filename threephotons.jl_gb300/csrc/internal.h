@@ -75,6 +75,7 @@ struct TcTables {
   // split coupling (kernels_couple.cu)
   bool split = false;            // use the two-kernel coupling
   bool split_ok = false;         // the two-kernel coupling fits this shape
+  bool fused_ok = false;         // the one-kernel coupling fits this shape
   const long long* doff = nullptr;  // [n_pb] offset of each pair block's D rows in one proposal's D
   long long dstride = 0;         // float2 per proposal of D
   int dsub = 1;                  // proposals per (D, T) kernel pair, sized so D stays in L2
@@ -93,6 +94,8 @@ struct TcTables {
   const float* wtab = nullptr;
   const __nv_bfloat16* Fhi = nullptr;  // [NP][KP]
   const __nv_bfloat16* Flo = nullptr;
+  const float* Fhi32 = nullptr;        // [NP][KP] TF32 hi (fp32 with the low 13 bits clear)
+  const float* Flo32 = nullptr;        // [NP][KP] fp32 remainder
 };
 
 struct TcMaps {
@@ -107,15 +110,15 @@ cudaError_t tc_configure();
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
                               float2* cc, int* sym, cudaStream_t s);
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                               __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
+                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s);
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
-                              const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s);
+                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s);
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s);
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
 size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
 cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);
 cudaError_t launch_couple_split(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                                float2* Dg, __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s);
+                                float2* Dg, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s);
 
 int plain_ncg(const DevTables& t);
 // Detail text returned by tp3_last_error(NULL) on this thread.

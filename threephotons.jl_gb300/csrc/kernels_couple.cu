@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kThreadsT, 2) k_couple_t(
     const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
     const PairBlock* __restrict__ pbs, const long long* __restrict__ doff, long long dstride,
     const int* __restrict__ symflags, const float2* __restrict__ Dg, int prop0, int klp, int KP,
-    __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo, float* __restrict__ T32, int ldT32) {
+    void* __restrict__ Thi, void* __restrict__ Tlo, bool tf32, float* __restrict__ T32, int ldT32) {
   extern __shared__ __align__(16) float smf[];
   const int k1 = K - 1 - (int)blockIdx.y;
   const int sub = blockIdx.z;
@@ -146,8 +146,6 @@ __global__ void __launch_bounds__(kThreadsT, 2) k_couple_t(
   const int nq = (k1 + 4) >> 2;
   const int tiles = nq * (nq + 1) / 2;
   const int items = tiles * nl3;
-  __nv_bfloat16* th = Thi + (size_t)prop * klp * KP;
-  __nv_bfloat16* tl = Tlo + (size_t)prop * klp * KP;
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     const int s = nl3 - 1 - it / tiles;  // largest l3 first
     int t = it % tiles;
@@ -197,9 +195,17 @@ __global__ void __launch_bounds__(kThreadsT, 2) k_couple_t(
         if (k2 <= k1 && k3 <= k2) {
           const int ki = ki_of(k1, k2, k3);
           const float v = acc[i][j];
-          const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-          th[(size_t)ki * KP + lt] = hi;
-          tl[(size_t)ki * KP + lt] = __float2bfloat16_rn(v - __bfloat162float(hi));
+          const size_t o = ((size_t)prop * klp + ki) * KP + lt;
+          if (tf32) {
+            uint32_t h;
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+            reinterpret_cast<float*>(Thi)[o] = __uint_as_float(h);
+            reinterpret_cast<float*>(Tlo)[o] = v - __uint_as_float(h);
+          } else {
+            const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+            reinterpret_cast<__nv_bfloat16*>(Thi)[o] = hi;
+            reinterpret_cast<__nv_bfloat16*>(Tlo)[o] = __float2bfloat16_rn(v - __bfloat162float(hi));
+          }
           if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
         }
       }
@@ -231,7 +237,7 @@ cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc) {
 }
 
 cudaError_t launch_couple_split(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                                float2* Dg, __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s) {
+                                float2* Dg, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s) {
   const size_t sd = couple_split_smem_d(t, tc), st = couple_split_smem_t(t, tc);
   for (int p0 = 0; p0 < n; p0 += tc.dsub) {
     const int m = n - p0 < tc.dsub ? n - p0 : tc.dsub;
@@ -247,7 +253,7 @@ cudaError_t launch_couple_split(const DevTables& t, const TcTables& tc, int n, c
 #undef TP3_D
     dim3 gt(tc.n_pb, t.K, m);
     k_couple_t<<<gt, kThreadsT, st, s>>>(cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.doff, tc.dstride, sym, Dg, p0,
-                                         t.klp, tc.KP, Thi, Tlo, T32, t.n_ltp);
+                                         t.klp, tc.KP, Thi, Tlo, tf32, T32, t.n_ltp);
   }
   return cudaGetLastError();
 }

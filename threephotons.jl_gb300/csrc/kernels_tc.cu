@@ -38,6 +38,22 @@ namespace tp3 {
 // ---------------------------------------------------------------------------
 namespace {
 
+// T as an operand pair of the split-precision contraction: BF16 hi + bf16(v - hi), or
+// TF32 hi (round to nearest, ties away) + the FP32 remainder.
+__device__ __forceinline__ void store_split(void* hi, void* lo, size_t i, float v, bool tf32) {
+  if (tf32) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float hf = __uint_as_float(h);
+    reinterpret_cast<float*>(hi)[i] = hf;
+    reinterpret_cast<float*>(lo)[i] = v - hf;
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    reinterpret_cast<__nv_bfloat16*>(hi)[i] = h;
+    reinterpret_cast<__nv_bfloat16*>(lo)[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
 __device__ __forceinline__ int ki_index(int k1, int k2, int k3) {
   return k1 * (k1 + 1) * (k1 + 2) / 6 + k2 * (k2 + 1) / 2 + k3;
 }
@@ -114,7 +130,7 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
     const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
     const int2* __restrict__ chunks_gen, int nchunks_gen, int pmax_gen, int SDp,
     const int2* __restrict__ chunks_sym, int nchunks_sym, int pmax_sym, int SDhp, int wsmem, int klp, int KP,
-    const int* __restrict__ symflags, __nv_bfloat16* __restrict__ Thi, __nv_bfloat16* __restrict__ Tlo,
+    const int* __restrict__ symflags, void* __restrict__ Thi, void* __restrict__ Tlo, bool tf32out,
     float* __restrict__ T32, int ldT32) {
   extern __shared__ __align__(16) float smf[];
   const int prop = blockIdx.y;
@@ -146,9 +162,6 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
 
   const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, nl3p = pb.nl3p, l3min = pb.l3min, M = pb.M;
   const int off1 = coff[l1 >> 1] + l1, off2 = coff[l2 >> 1] + l2;
-  __nv_bfloat16* th = Thi + (size_t)prop * klp * KP;
-  __nv_bfloat16* tl = Tlo + (size_t)prop * klp * KP;
-
   // D is double-buffered: phase 2 of chunk ch and phase 1 of chunk ch+1 need no
   // barrier between them, so one __syncthreads per chunk suffices and uneven items
   // of the two phases overlap across warps.
@@ -278,10 +291,7 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
           if (k2 <= k1 && k3 <= k2) {
             const int ki = ki_index(k1, k2, k3);
             const float v = acc[i][j];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-            const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-            th[(size_t)ki * KP + lt] = hi;
-            tl[(size_t)ki * KP + lt] = lo;
+            store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + lt, v, tf32out);
             if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
           }
         }
@@ -298,7 +308,7 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
 namespace {
 
 constexpr int kStages = 4;
-constexpr int kBK = 32;                       // K elements per stage (64 bytes of bf16)
+constexpr int kBK = 32;                       // K elements per stage: 64 bytes of bf16 (16 of tf32)
 constexpr int kBM = 128;                      // shell triples per CTA (TMEM lanes)
 constexpr int kBN = 256;                      // grid columns per MMA (one TMEM half)
 constexpr int kABytes = kBM * kBK * 2;        // 8 KB
@@ -367,19 +377,29 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
   return d;
 }
 
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both K-major, M = 128, N = 256.
-__host__ __device__ constexpr uint32_t idesc_bf16_m128_n256() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+// Instruction descriptor: F32 accumulator, both operands K-major, M = 128, N = 256;
+// operand format 1 = BF16 (kind::f16), 2 = TF32 (kind::tf32).
+__host__ __device__ constexpr uint32_t idesc_m128_n256(uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+template <bool TF32>
+__device__ __forceinline__ void mma_issue(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  if (TF32)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -415,7 +435,7 @@ struct TcSmemHeader {
 
 // grid: (klp / 128, n); block kThreads; dyn smem = 1 KB alignment slack + stages + header.
 // STORE: write c3 (all four images of every unique point) instead of the Bayes terms.
-template <bool STORE>
+template <bool STORE, bool TF32>
 __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
     const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
     const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
@@ -430,7 +450,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
   const int prop = blockIdx.y;
   const int mtile = blockIdx.x;
   const int row0 = prop * klp + mtile * kBM;  // row coordinate in the A tensor
-  const int nk = KP / kBK;
+  constexpr int kbk = TF32 ? kBK / 2 : kBK;  // K elements in one 64-byte row
+  const int nk = KP / kbk;
   const uint32_t tcols = nhalf == 2 ? 512u : 256u;
 
   if (threadIdx.x == 0) {
@@ -470,10 +491,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
           last[s] = it;
           uint8_t* st = stages + s * kStageBytes;
           mbar_expect_tx(&hd->full[s], kStageBytes);
-          tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kBK, row0);
-          tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kBK, row0);
-          tma_load_2d(st + 2 * kABytes, &tmB_hi, &hd->full[s], kc * kBK, h * kBN);
-          tma_load_2d(st + 2 * kABytes + kBBytes, &tmB_lo, &hd->full[s], kc * kBK, h * kBN);
+          tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kbk, row0);
+          tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kbk, row0);
+          tma_load_2d(st + 2 * kABytes, &tmB_hi, &hd->full[s], kc * kbk, h * kBN);
+          tma_load_2d(st + 2 * kABytes + kBBytes, &tmB_lo, &hd->full[s], kc * kbk, h * kBN);
         }
       }
       if (*abort_flag) {
@@ -490,7 +511,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_m128_n256();
+      const uint32_t idesc = idesc_m128_n256(TF32 ? 2u : 1u);
       int it = 0;
       for (int h = 0; h < nhalf && !*abort_flag; ++h) {
         const uint32_t dt = tmem + (uint32_t)(h * kBN);
@@ -502,12 +523,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
           const uint32_t st = smem_u32(stages + s * kStageBytes);
           const uint64_t ahi = smem_desc_sw64(st), alo = smem_desc_sw64(st + kABytes);
           const uint64_t bhi = smem_desc_sw64(st + 2 * kABytes), blo = smem_desc_sw64(st + 2 * kABytes + kBBytes);
+          // two MMA K-steps of 32 bytes per 64-byte row (K = 16 bf16 or K = 8 tf32 each)
 #pragma unroll
-          for (int ks = 0; ks < kBK / 16; ++ks) {
-            const uint64_t dk = (uint64_t)(ks * 32 / 16);  // +32 bytes per K=16 step, in 16-byte units
-            mma_bf16(dt, ahi + dk, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
-            mma_bf16(dt, ahi + dk, blo + dk, idesc, 1u);
-            mma_bf16(dt, alo + dk, bhi + dk, idesc, 1u);
+          for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t dk = (uint64_t)(ks * 2);  // +32 bytes, in 16-byte descriptor units
+            mma_issue<TF32>(dt, ahi + dk, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+            mma_issue<TF32>(dt, ahi + dk, blo + dk, idesc, 1u);
+            mma_issue<TF32>(dt, alo + dk, bhi + dk, idesc, 1u);
           }
           mma_commit(&hd->empty[s]);
         }
@@ -632,9 +654,14 @@ size_t tc_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(Tc
 cudaError_t tc_configure() {
   cudaError_t e;
   const int smem = (int)tc_smem_bytes();
-  if ((e = cudaFuncSetAttribute(k_angular_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_angular_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(k_angular_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+          cudaSuccess)
     return e;
   const int cs = kCoupleMaxDynSmem;
 #define TP3_CP_ATTR(S, W)                                                                              \
@@ -655,13 +682,13 @@ cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, con
 }
 
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                               __nv_bfloat16* Thi, __nv_bfloat16* Tlo, float* T32, cudaStream_t s) {
+                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s) {
   dim3 grid(tc.n_pb, n);
   const size_t smem = tc.couple_smem;
 #define TP3_CP_LAUNCH(S, W)                                                                                \
   k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(                                                  \
       cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,         \
-      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, T32, t.n_ltp)
+      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, tf32, T32, t.n_ltp)
   if (tc.w_smem) {
     if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true);
     else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true);
@@ -680,17 +707,19 @@ cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, co
 }
 
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
-                              const double* Qs, double* Eslab, float* c3out, int* err, cudaStream_t s) {
+                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s) {
   dim3 grid(t.klp / kBM, n);
   const size_t smem = tc_smem_bytes();
-  if (c3out)
-    k_angular_tc<true><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu,
-                                                    tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out,
-                                                    t.u_to_g, t.N, err);
-  else
-    k_angular_tc<false><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP,
-                                                     t.Gu, tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab,
-                                                     nullptr, t.u_to_g, t.N, err);
+#define TP3_ANG(ST, TF)                                                                                        \
+  k_angular_tc<ST, TF><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, \
+                                                     tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out,      \
+                                                     t.u_to_g, t.N, err)
+  if (c3out) {
+    if (tf32) TP3_ANG(true, true); else TP3_ANG(true, false);
+  } else {
+    if (tf32) TP3_ANG(false, true); else TP3_ANG(false, false);
+  }
+#undef TP3_ANG
   return cudaGetLastError();
 }
 

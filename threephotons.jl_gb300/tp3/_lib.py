@@ -29,6 +29,7 @@ TP3_ERR_ALLOC = 9
 
 TP3_MODE_PLAIN_FP32 = 0
 TP3_MODE_TC_BF16X3 = 1
+TP3_MODE_TC_TF32X3 = 2
 TP3_MODE_AUTO = -1
 
 # name -> (restype, argtypes); every symbol include/tp3.h declares
