@@ -104,6 +104,11 @@ int tp3_set_histogram(tp3_ctx* ctx, const double* c3ref, int K3);
 /* Raw model correlation c3 (2N^2 x klength, column-major float). */
 int tp3_c3(tp3_ctx* ctx, const double* coeff, float* out);
 
+/* Raw c3 of n coefficient sets in device memory (layout of tp3_energy_batch_device)
+ * into d_c3 = n x klength x 2N^2 floats in device memory (per set, the tp3_c3 layout).
+ * Asynchronous on the context stream. */
+int tp3_c3_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_c3);
+
 /* Rotation-invariant triple products T[ki][lt] = sum_{j in lt} w_j Re(c_k1 c_k2 c_k3)
  * (klength x n_lt row-major float) with the current mode's coupling kernel: the
  * As values of calculate_triple_products_fast, src/correlations.jl:157-176. */

@@ -88,3 +88,28 @@ int tp3ref_threads(void) {
   return 1;
 #endif
 }
+
+/* T[ki][lt] = sum_{j in lt} w_j Re(ck1[i1] ck2[i2] ck3[i3]) in FP64 (the As sums of
+ * correlations.jl:157-176), row-major klength x n_lt; lt ranges are 0-based. */
+void tp3ref_T(int ncoef, const double* coeff, const double* w, const int64_t* indices, int n_lt,
+              const int64_t* lt_start, const int64_t* lt_count, int64_t klength, const int64_t* klist, double* T) {
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t ki = 0; ki < klength; ++ki) {
+    const int64_t k1 = klist[3 * ki] - 1, k2 = klist[3 * ki + 1] - 1, k3 = klist[3 * ki + 2] - 1;
+    const double* c1 = coeff + 2 * ncoef * k1;
+    const double* c2 = coeff + 2 * ncoef * k2;
+    const double* c3 = coeff + 2 * ncoef * k3;
+    for (int lt = 0; lt < n_lt; ++lt) {
+      double As = 0.0;
+      for (int64_t j = lt_start[lt]; j < lt_start[lt] + lt_count[lt]; ++j) {
+        const int64_t* ix = indices + 9 * j;
+        const double ar = c1[2 * (ix[0] - 1)], ai = c1[2 * (ix[0] - 1) + 1];
+        const double br = c2[2 * (ix[1] - 1)], bi = c2[2 * (ix[1] - 1) + 1];
+        const double cr = c3[2 * (ix[2] - 1)], ci = c3[2 * (ix[2] - 1) + 1];
+        const double pr = ar * br - ai * bi, pi_ = ar * bi + ai * br;
+        As += w[j] * (pr * cr - pi_ * ci);
+      }
+      T[ki * n_lt + lt] = As;
+    }
+  }
+}

@@ -38,7 +38,23 @@ def load():
         _lib.tp3ref_pa.argtypes = [ci, vp, i64, vp, vp, i64, vp, vp, vp]
         _lib.tp3ref_pa.restype = None
         _lib.tp3ref_threads.restype = ci
+        _lib.tp3ref_T.argtypes = [ci, vp, vp, vp, ci, vp, vp, i64, vp, vp]
+        _lib.tp3ref_T.restype = None
     return _lib
+
+
+def triple_products_fast(b, coeff) -> np.ndarray:
+    """FP64 T[ki, lt] (klength x n_lt) with the C + OpenMP loop (same sums as oracle.c3.triple_products)."""
+    lib = load()
+    c = np.ascontiguousarray(np.asarray(coeff)[: b.K], dtype=np.complex128)
+    indices = np.ascontiguousarray(b.indices.T)
+    starts = np.array([js - 1 for (_, _, _, mc, js) in b.mcombolist], dtype=np.int64)
+    counts = np.array([mc for (_, _, _, mc, js) in b.mcombolist], dtype=np.int64)
+    klist = np.ascontiguousarray(b.klist)
+    T = np.empty((b.klength, b.n_lt), dtype=np.float64)
+    lib.tp3ref_T(b.LMAX * b.LMAX, c.ctypes.data, b.wignerlist.ctypes.data, indices.ctypes.data, b.n_lt,
+                 starts.ctypes.data, counts.ctypes.data, b.klength, klist.ctypes.data, T.ctypes.data)
+    return T
 
 
 def threads() -> int:

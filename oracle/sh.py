@@ -184,3 +184,41 @@ def tripletFactor(k1: int, k2: int, k3: int) -> float:
     if k1 == k2 or k1 == k3 or k2 == k3:
         return 3.0
     return 6.0
+
+
+_WD_CACHE: dict = {}
+
+
+def _Ylm_rows(l: int, dirs: np.ndarray) -> np.ndarray:
+    """Y_lm(dirs[i]) for m = -l..l (any fixed orthonormal complex SH convention works here)."""
+    th = np.arccos(np.clip(dirs[:, 2], -1.0, 1.0))
+    ph = np.arctan2(dirs[:, 1], dirs[:, 0])
+    ms = np.arange(-l, l + 1)
+    try:
+        from scipy.special import sph_harm_y
+        return sph_harm_y(l, ms[None, :], th[:, None], ph[:, None])
+    except ImportError:                      # scipy < 1.15: (m, l, azimuth, polar)
+        from scipy.special import sph_harm
+        return sph_harm(ms[None, :], l, ph[:, None], th[:, None])
+
+
+def wigner_D_sampled(l: int, R: np.ndarray) -> np.ndarray:
+    """Matrix D (2l+1 x 2l+1) with sum_m c_m Y_lm(R^T n) = sum_m' (c D)_m' Y_lm'(n) for every n:
+    the action of the rotation R on SH coefficients of order l, obtained by least squares on
+    fixed random directions (exact up to rounding for a band-limited order-l function)."""
+    if l not in _WD_CACHE:
+        rng = np.random.default_rng(1000 + l)
+        n = rng.normal(size=(4 * (2 * l + 1) + 16, 3))
+        n /= np.linalg.norm(n, axis=1)[:, None]
+        _WD_CACHE[l] = (n, np.linalg.pinv(_Ylm_rows(l, n)))
+    n, pinv = _WD_CACHE[l]
+    return pinv @ _Ylm_rows(l, n @ R)
+
+
+def random_rotation3(rng: np.random.Generator) -> np.ndarray:
+    """Haar-random SO(3) matrix."""
+    Q, Rr = np.linalg.qr(rng.normal(size=(3, 3)))
+    Q = Q * np.sign(np.diag(Rr))
+    if np.linalg.det(Q) < 0:
+        Q[:, 0] *= -1
+    return Q

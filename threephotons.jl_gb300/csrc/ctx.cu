@@ -805,6 +805,22 @@ int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {
   return check_device_error(c);
 }
 
+int tp3_c3_batch_device(tp3_ctx* c, int n, const void* d_coeffs, void* d_c3) {
+  if (int r = check_ctx(c)) return r;
+  if (n < 1 || !d_coeffs || !d_c3) return fail(c, TP3_ERR_ARG, "bad batch arguments");
+  if (int r = ensure_cap(c, n)) return r;
+  const auto& t = c->t;
+  cudaError_t e;
+  if (int r = run_coupling(c, n, (const double2*)d_coeffs, false)) return r;
+  if (is_tc(c->mode))
+    e = tp3::launch_angular_tc(t, c->tc, c->mode == TP3_MODE_TC_TF32X3 ? c->maps32 : c->maps, n, nullptr, nullptr,
+                               nullptr, (float*)d_c3, c->d_err, c->mode == TP3_MODE_TC_TF32X3, c->stream);
+  else
+    e = tp3::launch_angular_plain(t, n, plain_A(c), nullptr, nullptr, tp3::plain_ncg(t), (float*)d_c3, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "angular store");
+  return TP3_OK;
+}
+
 int tp3_triple_products(tp3_ctx* c, const double* coeff, float* out) {
   if (int r = check_ctx(c)) return r;
   if (!coeff || !out) return fail(c, TP3_ERR_ARG, "NULL pointer");

@@ -48,6 +48,7 @@ SIGNATURES = {
     "tp3_reserve": (c_int, [c_void_p, c_int]),
     "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),
     "tp3_c3": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "tp3_c3_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "tp3_triple_products": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tp3_sync": (c_int, [c_void_p]),
     "tp3_energy": (c_int, [c_void_p, c_void_p, P(c_double)]),

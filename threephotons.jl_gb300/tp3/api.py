@@ -192,6 +192,10 @@ class BasisTypeGB300:
         check(self._lib.tp3_energy_batch_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr),
                                                 ctypes.c_void_p(d_E_ptr)), self._ctx)
 
+    def c3_batch_device(self, n: int, d_coeffs_ptr: int, d_c3_ptr: int) -> None:
+        check(self._lib.tp3_c3_batch_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr), ctypes.c_void_p(d_c3_ptr)),
+              self._ctx)
+
     def profile_enable(self, on: bool) -> None:
         check(self._lib.tp3_profile_enable(self._ctx, int(on)), self._ctx)
 
