@@ -62,6 +62,7 @@ extern "C" {
 #define TP3_MODE_AUTO (-1)       /* fastest available mode for this shape */
 
 typedef struct tp3_ctx tp3_ctx;
+typedef struct tp3_mlp tp3_mlp;
 
 /* Text for a status code (static storage). */
 const char* tp3_status_string(int status);
@@ -164,6 +165,34 @@ int tp3_chains_log(tp3_chains* chains, int chain, double* rows, int64_t* nrows);
  * bit-exact; the RNG needs no state beyond the step counters. */
 int tp3_chains_snapshot(tp3_chains* chains, void* buf, size_t capacity, size_t* bytes);
 int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
+/* Move of a chain set.  TP3_MOVE_REFERENCE (default): get_MC_step
+ * (src/determination.jl:232-241).  TP3_MOVE_SHELL_SO3: every shell rotated by its own
+ * exp([v]x), v ~ N(0, sigma^2 I3), with the Wigner-D rotation of rotateStructure
+ * (src/spherical_harmonics.jl:595-603) on every even l; sigma starts at sigma0 and
+ * is multiplied / divided by the step-size factor on accept / reject like the
+ * reference's step sizes.  TP3_MOVE_LEARNED: a candidate comes from the network
+ * (tp3_mlp) with probability p_net and from the isotropic step otherwise; the
+ * Metropolis-Hastings ratio of the mixture density corrects the acceptance.  The
+ * network must have n_in = (L+1)^2 + 9 and max_rows >= chains x candidates x K.
+ * No reference counterpart for the two per-shell kinds. */
+#define TP3_MOVE_REFERENCE 0
+#define TP3_MOVE_SHELL_SO3 1
+#define TP3_MOVE_LEARNED 2
+int tp3_chains_set_move(tp3_chains* chains, int kind, double sigma0, double p_net, tp3_mlp* net);
+
+/* Move log for training the network: a ring of `launches` launches of per-shell
+ * moves; per candidate the state's feature rows, the steps v, and
+ * (dE, T, accepted, drawn-from-network, log q(x|x') - log q(x'|x)) where accepted is
+ * the Metropolis decision with the candidate's own uniform (the chain's actual
+ * decision up to its taken step).  tp3_chains_move_log_count returns the candidates held (synchronising);
+ * tp3_chains_move_log_gather writes, for n candidate positions d_idx (int64, device,
+ * each < count), n x K feature rows (BF16, stride (L+1)^2 + 9 rounded up to 32, the
+ * temperature column set to the candidate's), n x K x 3 steps (float) and n x 5
+ * meta floats in that order into device buffers. */
+int tp3_chains_enable_move_log(tp3_chains* chains, int launches);
+int tp3_chains_move_log_count(tp3_chains* chains, int64_t* candidates);
+int tp3_chains_move_log_gather(tp3_chains* chains, int n, const int64_t* d_idx, void* d_x, float* d_v, float* d_meta);
+
 /* *captured = 1 when launches replay a CUDA graph. */
 int tp3_chains_graph(const tp3_chains* chains, int* captured);
 
@@ -188,6 +217,57 @@ int tp3_chains_graph(const tp3_chains* chains, int* captured);
  * writes every entry it reads, so no clearing is needed.  Asynchronous; errors in
  * the arguments return at once (detail in tp3_last_error(NULL)). */
 int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, int K, int N, double* d_E, void* stream);
+
+/* ---- Wigner-D rotations (src/spherical_harmonics.jl:572-603) --------------- */
+/* rotationMatrix(theta, phi, gamma, l) of src/spherical_harmonics.jl:590-592:
+ * D[m, s] = exp(-i s gamma - i m phi) d^l_{ms}(theta), m, s = -l..l, written
+ * column-major (Julia order) as (2l+1)^2 interleaved (re, im) doubles.  It is the
+ * coefficient action of the rotation R = Rz(phi) Ry(-theta) Rz(gamma) on functions
+ * (f'(n) = f(R^T n)).  Host only, FP64; l <= 62. */
+int tp3_wigner_D(int l, double theta, double phi, double gamma, double* out);
+
+/* Per-shell rotations on the device: every shell k of n coefficient sets
+ * (d_coeffs / d_out: n x K x LMAX^2 complex128, the layout of
+ * tp3_energy_batch_device; d_out may equal d_coeffs) is replaced by
+ * rotateStructure's D c_l (src/spherical_harmonics.jl:595-603) for every
+ * l < LMAX, with its own rotation exp([v]x), v = d_axis_angle[set][k][0..2]
+ * (n x K x 3 doubles, axis times angle in radians): the coefficients of
+ * f'(n) = f(R^T n).  rotationMatrix(theta, phi, gamma) is that action for
+ * R = Rz(phi) Ry(-theta) Rz(gamma); the Euler angles are taken from exp([v]x).
+ * FP64; asynchronous on the context stream.  No reference counterpart as one call:
+ * the reference rotates one volume at a time on the host. */
+int tp3_rotate_shells_device(tp3_ctx* ctx, int n, const void* d_coeffs, const void* d_axis_angle, void* d_out);
+
+/* ---- learned proposal network ------------------------------------------------
+ * No reference counterpart: the network that proposes per-shell rotation steps for
+ * the annealer (a mixture with the isotropic step, Metropolis-Hastings corrected).
+ * Architecture: n_in -> hidden -> hidden -> hidden -> 6, ReLU, BF16 weights and
+ * activations, FP32 accumulation on the tensor cores, FP32 master weights and
+ * Adam.  Rows are shells; input rows are BF16 with a stride of n_in rounded up to
+ * 32 (the padding columns must be zero).  Outputs per row: mu[3] (the mean axis-angle
+ * step, |mu_d| < 0.5) and s[3] (log of its standard deviation, in (-7, 1)).
+ * Parameters are one FP32 vector: W1 (hidden x n_in, row-major), b1, W2, b2, W3, b3,
+ * W4 (6 x hidden), b4. */
+int tp3_mlp_create(tp3_ctx* ctx, int n_in, int hidden, int max_rows, uint64_t seed, tp3_mlp** out);
+void tp3_mlp_destroy(tp3_mlp* net);
+int tp3_mlp_num_params(const tp3_mlp* net, int64_t* count);
+int tp3_mlp_get_params(tp3_mlp* net, float* host, int64_t count);
+int tp3_mlp_set_params(tp3_mlp* net, const float* host, int64_t count);
+/* The network's own input buffer (max_rows x row_stride BF16, device): writing the
+ * features there saves the copy that the calls below make from any other pointer. */
+int tp3_mlp_input_buffer(tp3_mlp* net, void** d_x, int* row_stride);
+/* (mu, s) of rows [0, rows) into d_out = rows x 6 floats (device).  Asynchronous. */
+int tp3_mlp_forward_device(tp3_mlp* net, int rows, const void* d_x, void* d_out);
+/* Loss sum_r w_r NLL(v_r; mu_r, s_r) of axis-angle steps d_v (rows x 3 floats) with
+ * weights d_w (rows floats), and its gradient (FP32, the parameter layout) copied to
+ * grad_host when not NULL.  rows must be a multiple of 128 (pad with w = 0 and zero
+ * features).  Synchronises. */
+int tp3_mlp_loss_grad(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w, double* loss,
+                      float* grad_host);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss; the loss is returned
+ * (synchronising) when loss is not NULL, else the call stays asynchronous. */
+int tp3_mlp_train_step(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w, float lr,
+                       double* loss);
 
 /* ---- per-launch timing of the dominant kernel ----------------------------- */
 /* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on

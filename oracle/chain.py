@@ -116,3 +116,94 @@ def run_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, initi
                 sigma[l] /= stepsizefactor
         rows.append([s + 1, sign, En, E, dE, T, ap, sigma[max(sigma)] if sigma else 0.0])
     return state, E, T, sigma, np.array(rows)
+
+
+# ---------------------------------------------------------------------------
+# Per-shell SO(3) moves (no reference counterpart: the learned-proposal experiment).
+# Stream: purpose 3 index 0 = component uniform, purpose 4 index k = the three
+# normals of shell k's axis-angle step.
+# ---------------------------------------------------------------------------
+
+def rodrigues(v) -> np.ndarray:
+    v = np.asarray(v, dtype=np.float64)
+    a = float(np.linalg.norm(v))
+    if a == 0.0:
+        return np.eye(3)
+    u = v / a
+    Kx = np.array([[0, -u[2], u[1]], [u[2], 0, -u[0]], [-u[1], u[0], 0]])
+    return math.cos(a) * np.eye(3) + math.sin(a) * Kx + 2.0 * math.sin(0.5 * a) ** 2 * np.outer(u, u)
+
+
+def rotate_shells(coeff: np.ndarray, v: np.ndarray, L: int, LMAX: int) -> np.ndarray:
+    """Shell k's even orders l = 2..L rotated by exp([v_k]x) (action on functions)."""
+    from .sh import wigner_D_sampled
+    out = coeff.copy()
+    for k in range(coeff.shape[0]):
+        R = rodrigues(v[k])
+        for l in range(2, L + 1, 2):
+            idx = [seanindex(l, m, LMAX) - 1 for m in range(-l, l + 1)]
+            out[k, idx] = wigner_D_sampled(l, R) @ coeff[k, idx]
+    return out
+
+
+def shell_steps(seed: int, step: int, chain: int, K: int):
+    """Unit normals z[K][3] and the component uniform of one candidate."""
+    z = np.array([normals4(seed, step, chain, 4, k)[:3] for k in range(K)])
+    u = u01(philox4x32_10((step & M32, chain, 3, 0), _key(seed))[0])
+    return z, u
+
+
+def rot_logdens(v, mu, s) -> float:
+    """log density of the rotation exp([v]x) under N(mu, diag(exp(2 s))) up to the Haar
+    factor common to a move and its reverse (preimages |v| + 2 pi n, n = -1, 0, 1)."""
+    v, mu, s = (np.asarray(x, dtype=np.float64) for x in (v, mu, s))
+    th = float(np.linalg.norm(v))
+    terms = []
+    for n in ((-1, 0, 1) if th > 0 else (0,)):
+        f = (th + 2 * math.pi * n) / th if th > 0 else 1.0
+        z = (v * f - mu) * np.exp(-s)
+        terms.append(-0.5 * float(z @ z) - float(s.sum()) - 1.5 * math.log(2 * math.pi)
+                     + 2.0 * math.log(abs(f) if f != 0 else 1e-300))
+    m = max(terms)
+    return m + math.log(sum(math.exp(t - m) for t in terms))
+
+
+def mixture_log_ratio(v, mu, s, mu2, s2, sigma: float, p_net: float) -> float:
+    """log q(x|x') - log q(x'|x) of the mixture p q_net + (1 - p) q_iso over all shells."""
+    K = v.shape[0]
+    ls = np.full(3, math.log(sigma))
+    fnet = sum(rot_logdens(v[k], mu[k], s[k]) for k in range(K))
+    rnet = sum(rot_logdens(-v[k], mu2[k], s2[k]) for k in range(K))
+    fiso = sum(rot_logdens(v[k], np.zeros(3), ls) for k in range(K))
+    lp = math.log(p_net)
+    lq = math.log1p(-p_net) if p_net < 1 else -math.inf
+    return float(np.logaddexp(lp + rnet, lq + fiso) - np.logaddexp(lp + fnet, lq + fiso))
+
+
+def run_shell_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, sigma0: float,
+                    stepsizefactor: float, temperature_decay: float, seed: int, chain: int, nsteps: int):
+    """Sequential chain with the isotropic per-shell move; rows as run_chain."""
+    state = coeff0.copy()
+    E = energy_fn(state)
+    T, sigma = T0, sigma0
+    rows = []
+    K = coeff0.shape[0]
+    for s in range(nsteps):
+        T *= temperature_decay
+        z, _ = shell_steps(seed, s, chain, K)
+        cand = rotate_shells(state, sigma * z, L, LMAX)
+        En = energy_fn(cand)
+        dE = En - E
+        ap = math.exp(-dE / T) if -dE / T < 700 else float("inf")
+        u = u01(philox4x32_10((s & M32, chain, 2, 0), _key(seed))[0])
+        acc = dE < 0.0 or (dE > 0.0 and u < ap)
+        sign = 0.0
+        if acc:
+            sign = 1.0 if dE < 0.0 else -1.0
+            sigma *= stepsizefactor
+            E = En
+            state = cand
+        else:
+            sigma /= stepsizefactor
+        rows.append([s + 1, sign, En, E, dE, T, ap, sigma])
+    return state, E, T, sigma, np.array(rows)

@@ -1,0 +1,124 @@
+"""FP64 restatement of the learned-proposal network and its gradient (oracle).
+
+TEST INFRASTRUCTURE ONLY (see oracle/sh.py).  The network has no counterpart in
+the reference; this module is the CPU checker of the library's forward and
+backward kernels.  It reproduces every BF16 rounding the device makes (weights,
+hidden activations, output gradient dO, gated gradients dZ) and accumulates in
+FP64, so the device (FP32 accumulation on the tensor cores) agrees with it to
+accumulation rounding.
+
+Parameter vector (FP32): W1 (H x n_in), b1, W2 (H x H), b2, W3, b3, W4 (6 x H), b4.
+Head: mu = 0.5 tanh(o[0:3]), s = -3 + 4 tanh(o[3:6]).
+Loss: sum_r w_r sum_d [s_d + (v_d - mu_d)^2 exp(-2 s_d) / 2 + log(2 pi) / 2].
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+MU_SCALE, S_MID, S_HALF = 0.5, -3.0, 4.0
+
+
+def bf16(x) -> np.ndarray:
+    """Round to the nearest BF16 (ties to even), returned as float64."""
+    f = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    u = f.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def f32(x) -> np.ndarray:
+    """Round to FP32 (the device's bias precision), returned as float64."""
+    return np.asarray(x, dtype=np.float32).astype(np.float64)
+
+
+def split_params(p: np.ndarray, n_in: int, H: int):
+    p = np.asarray(p, dtype=np.float64)
+    shapes = [(H, n_in), (H, H), (H, H), (6, H)]
+    out, o = [], 0
+    for (a, b) in shapes:
+        W = p[o:o + a * b].reshape(a, b); o += a * b
+        bb = p[o:o + a]; o += a
+        out.append((W, bb))
+    assert o == p.size
+    return out
+
+
+def forward(p, X, n_in: int, H: int):
+    """Raw outputs O (R x 6) and the cached BF16 activations."""
+    layers = split_params(p, n_in, H)
+    A = [bf16(X[:, :n_in])]
+    for l in range(3):
+        W, b = layers[l]
+        A.append(bf16(np.maximum(A[-1] @ bf16(W).T + f32(b), 0.0)))
+    W, b = layers[3]
+    O = A[-1] @ bf16(W).T + f32(b)
+    return O, A
+
+
+def head(O):
+    return MU_SCALE * np.tanh(O[:, :3]), S_MID + S_HALF * np.tanh(O[:, 3:6])
+
+
+def loss_grad(p, X, v, w, n_in: int, H: int):
+    """(loss, gradient vector in the parameter layout)."""
+    layers = split_params(p, n_in, H)
+    O, A = forward(p, X, n_in, H)
+    tm, ts = np.tanh(O[:, :3]), np.tanh(O[:, 3:6])
+    mu, s = MU_SCALE * tm, S_MID + S_HALF * ts
+    e = v - mu
+    is2 = np.exp(-2.0 * s)
+    loss = float(np.sum(w[:, None] * (s + 0.5 * e * e * is2 + 0.5 * math.log(2 * math.pi))))
+    dmu = -e * is2
+    ds = 1.0 - e * e * is2
+    dO = bf16(np.concatenate([w[:, None] * dmu * MU_SCALE * (1 - tm * tm),
+                              w[:, None] * ds * S_HALF * (1 - ts * ts)], axis=1))
+    grads = []
+    W4, _ = layers[3]
+    gW = dO.T @ A[3]
+    gb = dO.sum(axis=0)
+    grads.append((gW, gb))
+    dZ = bf16((dO @ bf16(W4)) * (A[3] > 0))
+    for l in (2, 1, 0):
+        gW = dZ.T @ A[l]
+        gb = dZ.sum(axis=0)
+        grads.append((gW, gb))
+        if l > 0:
+            W, _ = layers[l]
+            dZ = bf16((dZ @ bf16(W)) * (A[l] > 0))
+    grads = grads[::-1]
+    flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
+    return loss, flat
+
+
+def init_params(n_in: int, H: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    parts = []
+    for (a, b, sc) in [(H, n_in, 1.0), (H, H, 1.0), (H, H, 1.0), (6, H, 0.05)]:
+        lim = math.sqrt(6.0 / b) * sc
+        parts.append(rng.uniform(-lim, lim, size=a * b))
+        parts.append(rng.uniform(-0.1, 0.1, size=a))
+    return np.concatenate(parts).astype(np.float32)
+
+
+def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride: int) -> np.ndarray:
+    """Feature rows (K x stride, BF16 values) of a state's shells: (L+1)^2 real SH
+    coefficients x = Umat(l) c_l scaled to norm 8, the 8 history values dE/T clipped to
+    +-10 and divided by 10, log10(T)/4, zeros."""
+    from .sh import Umat, seanindex
+    K = coeff.shape[0]
+    nf = (L + 1) ** 2
+    out = np.zeros((K, stride))
+    h = np.clip(np.nan_to_num(np.asarray(hist, dtype=np.float64), nan=10.0), -10, 10) / 10.0
+    for k in range(K):
+        x = []
+        for l in range(L + 1):
+            idx = [seanindex(l, m, LMAX) - 1 for m in range(-l, l + 1)]
+            x.extend((Umat(l) @ coeff[k, idx]).real)
+        x = np.asarray(x, dtype=np.float32).astype(np.float64)
+        nrm = math.sqrt(float(np.sum(x * x)))
+        out[k, :nf] = x * (8.0 / nrm) if nrm > 0 else 0.0
+        out[k, nf:nf + 8] = h
+        out[k, nf + 8] = math.log10(T) / 4.0
+    return bf16(out)

@@ -20,6 +20,9 @@ code relies on:
   by (-1)^|m|.  Evaluated with the standard three-term recurrence in FP64.
 * ``Umat``       -- src/spherical_harmonics.jl:445-457, complex -> real SH
   transformation matrix of order l.
+* ``d_work`` / ``rotation_matrix`` / ``rotate_structure`` -- src/spherical_harmonics.jl:
+  572-603, the Wigner-D rotation of coefficients (factorial sum evaluated in 60-digit
+  mpmath arithmetic, so the oracle is free of the sum's cancellation).
 """
 from __future__ import annotations
 
@@ -186,6 +189,64 @@ def tripletFactor(k1: int, k2: int, k3: int) -> float:
     return 6.0
 
 
+def d_work(l: int, m1: int, m2: int, beta: float) -> float:
+    """Wigner small-d d^l_{m1 m2}(beta) (spherical_harmonics.jl:572-586), 60 digits."""
+    import mpmath
+    with mpmath.workdps(60):
+        b = mpmath.mpf(beta) / 2
+        cb, sb = mpmath.cos(b), mpmath.sin(b)
+        f = mpmath.factorial
+        val = mpmath.mpf(0)
+        for s in range(max(0, m1 - m2), min(l - m2, l + m1) + 1):
+            val += (cb ** (2 * l + m1 - m2 - 2 * s) * sb ** (m2 - m1 + 2 * s) * (-1) ** (s + m2 - m1)
+                    / (f(l + m1 - s) * f(s) * f(m2 - m1 + s) * f(l - m2 - s)))
+        val *= mpmath.sqrt(f(l + m1) * f(l - m1) * f(l + m2) * f(l - m2))
+        return float(val)
+
+
+def rotation_matrix(theta: float, phi: float, gamma: float, l: int) -> np.ndarray:
+    """rotationMatrix (spherical_harmonics.jl:588-592): D[m, s] = e^{-i s gamma - i m phi} d_ms(theta)."""
+    d = 2 * l + 1
+    D = np.empty((d, d), dtype=np.complex128)
+    for im, m in enumerate(range(-l, l + 1)):
+        for js, s_ in enumerate(range(-l, l + 1)):
+            D[im, js] = np.exp(-1j * s_ * gamma - 1j * m * phi) * d_work(l, m, s_, theta)
+    return D
+
+
+def rotate_structure(coeff: np.ndarray, theta: float, phi: float, gamma: float, K: int, lrange, LMAX: int) -> np.ndarray:
+    """rotateStructure (spherical_harmonics.jl:595-603) on coeff[K', LMAX^2] (seanindex order)."""
+    out = np.array(coeff, dtype=np.complex128, copy=True)
+    for l in lrange:
+        D = rotation_matrix(theta, phi, gamma, l)
+        idx = [seanindex(l, m, LMAX) - 1 for m in range(-l, l + 1)]
+        for k in range(K):
+            out[k, idx] = D @ coeff[k, idx]
+    return out
+
+
+def axis_angle_euler(v) -> tuple:
+    """(theta, phi, gamma) with rotation_matrix(theta, phi, gamma, l) = the coefficient action of the
+    rotation R = exp([v]x) on functions (f'(n) = f(R^T n)).  rotationMatrix(theta, phi, gamma) is that
+    action for R = Rz(phi) Ry(-theta) Rz(gamma), so with R = Rz(a) Ry(b) Rz(c), b in [0, pi]:
+    theta = -b, phi = a, gamma = c."""
+    v = np.asarray(v, dtype=np.float64)
+    a = float(np.linalg.norm(v))
+    if a == 0.0:
+        R = np.eye(3)
+    else:
+        u = v / a
+        Kx = np.array([[0, -u[2], u[1]], [u[2], 0, -u[0]], [-u[1], u[0], 0]])
+        R = math.cos(a) * np.eye(3) + math.sin(a) * Kx + 2.0 * math.sin(0.5 * a) ** 2 * np.outer(u, u)
+    sb = math.hypot(R[0, 2], R[1, 2])
+    b = math.atan2(sb, R[2, 2])
+    if sb > 1e-12:
+        return -b, math.atan2(R[1, 2], R[0, 2]), math.atan2(R[2, 1], -R[2, 0])
+    if R[2, 2] > 0:                      # b = 0: R = Rz(phi)
+        return 0.0, math.atan2(R[1, 0], R[0, 0]), 0.0
+    return -math.pi, math.atan2(-R[1, 0], -R[0, 0]), 0.0   # b = pi: R = Rz(phi) Ry(pi)
+
+
 _WD_CACHE: dict = {}
 
 
@@ -203,9 +264,10 @@ def _Ylm_rows(l: int, dirs: np.ndarray) -> np.ndarray:
 
 
 def wigner_D_sampled(l: int, R: np.ndarray) -> np.ndarray:
-    """Matrix D (2l+1 x 2l+1) with sum_m c_m Y_lm(R^T n) = sum_m' (c D)_m' Y_lm'(n) for every n:
-    the action of the rotation R on SH coefficients of order l, obtained by least squares on
-    fixed random directions (exact up to rounding for a band-limited order-l function)."""
+    """Matrix S (2l+1 x 2l+1) with sum_m c_m Y_lm(R^T n) = sum_m' (S c)_m' Y_lm'(n) for every n:
+    the action of the rotation R on the order-l coefficients of a function (f'(n) = f(R^T n)),
+    a homomorphism S(R1 R2) = S(R1) S(R2).  Obtained by least squares on fixed random
+    directions (exact up to rounding for a band-limited order-l function)."""
     if l not in _WD_CACHE:
         rng = np.random.default_rng(1000 + l)
         n = rng.normal(size=(4 * (2 * l + 1) + 16, 3))

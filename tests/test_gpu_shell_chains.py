@@ -1,0 +1,178 @@
+"""Per-shell SO(3) chain moves and the learned (network) proposal on the device
+against the oracle: the isotropic chain's trajectory, the network proposal with a
+constant head reducing to the isotropic one, and the logged features, steps and
+Metropolis-Hastings ratios of a random network recomputed on the CPU."""
+import math
+
+import numpy as np
+import pytest
+
+import tp3
+from tp3.chains import Chains
+from tp3.learned import ProposalMLP, n_in_for
+from oracle import chain as oc
+from oracle import mlp as om
+from oracle.basis import enumerate_basis, lt_form_F
+from oracle.c3 import triple_products, c3_lt_form, energy_bayes
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5EEDC0FFEE12
+DE_TOL = 2e-7
+
+
+@pytest.fixture(scope="module")
+def setup(config1, config1_hist):
+    p = config1["params"]
+    basis = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    basis.set_histogram(config1_hist)
+    ob = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    F = lt_form_F(ob)
+
+    def e64(c):
+        return energy_bayes(c3_lt_form(F, triple_products(ob, c)), config1_hist, p["K"], p["N"])
+
+    coeff = np.ascontiguousarray(config1["coeff"][: p["K"]])
+    # start: the true structure with every shell turned by its own rotation
+    rng = np.random.default_rng(4)
+    start = oc.rotate_shells(coeff, rng.normal(size=(p["K"], 3)) * 0.6, p["L"], p["LMAX"])
+    yield basis, e64, start, p
+    basis.close()
+
+
+def _agree(dev_rows, ref_rows, E0, chain):
+    tol = DE_TOL * abs(E0)
+    compared = 0
+    for d, r in zip(dev_rows, ref_rows):
+        s = int(r[0]) - 1
+        dE, T = r[4], r[5]
+        u = oc.u01(oc.philox4x32_10((s, chain, 2, 0), (SEED & oc.M32, SEED >> 32))[0])
+        ambiguous = abs(dE) <= tol or abs(dE + T * math.log(u)) <= tol
+        if d[1] != r[1]:
+            assert ambiguous, f"decision differs at step {s + 1}: dev {d} ref {r}"
+            break
+        assert d[2] == pytest.approx(r[2], rel=2e-6)
+        compared += 1
+    return compared
+
+
+def test_isotropic_shell_chain_matches_oracle(setup):
+    basis, e64, start, p = setup
+    nch, B, launches = 2, 4, 4
+    T0, sigma0, f, decay = 2.0, 0.25, 1.05, 0.995
+    ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, f, decay, SEED, ncand=B, log_capacity=64)
+    ch.set_move(tp3.TP3_MOVE_SHELL_SO3, sigma0)
+    ch.run(launches)
+    assert all(ch.state()["steps"] > 0)
+    for c in range(nch):
+        rows = ch.log(c)
+        _, _, _, _, ref = oc.run_shell_chain(e64, start, p["L"], p["LMAX"], T0, sigma0, f, decay, SEED, c, len(rows))
+        assert _agree(rows, ref, ref[0][3], c) >= min(len(rows), 3)
+    ch.close()
+
+
+def _constant_head_params(net, s_const):
+    P = np.zeros(net.n_params, dtype=np.float32)
+    P[-3:] = math.atanh((s_const - om.S_MID) / om.S_HALF)  # b4[3:6]: s = s_const, mu = 0
+    return P
+
+
+def test_constant_network_reduces_to_isotropic(setup):
+    basis, e64, start, p = setup
+    nch, B, launches = 4, 4, 6
+    L, K = p["L"], p["K"]
+    s_const = math.log(0.2)
+    net = ProposalMLP(basis, n_in_for(L), hidden=64, max_rows=((nch * B * K + 127) // 128) * 128, seed=1)
+    P = _constant_head_params(net, s_const)
+    net.set_params(P)
+    sigma_dev = math.exp(om.S_MID + om.S_HALF * math.tanh(float(P[-1])))  # the step size the head gives
+    runs = []
+    for kind in (tp3.TP3_MOVE_SHELL_SO3, tp3.TP3_MOVE_LEARNED):
+        ch = Chains(basis, np.repeat(start[None], nch, axis=0), 2.0, 0.1, 1.0, 0.995, SEED, ncand=B,
+                    log_capacity=64)
+        ch.set_move(kind, sigma_dev, 1.0, net if kind == tp3.TP3_MOVE_LEARNED else None)
+        ch.run(launches)
+        runs.append([ch.log(c) for c in range(nch)])
+        ch.close()
+    for c in range(nch):
+        a, b = runs[0][c], runs[1][c]
+        n = min(len(a), len(b))
+        assert n >= launches
+        np.testing.assert_array_equal(a[:n, 1], b[:n, 1])
+        np.testing.assert_allclose(a[:n, 2], b[:n, 2], rtol=1e-9)
+    net.close()
+
+
+def test_learned_moves_match_oracle(setup):
+    import torch
+    basis, e64, start, p = setup
+    nch, B = 2, 8
+    L, LMAX, K = p["L"], p["LMAX"], p["K"]
+    n_in = n_in_for(L)
+    net = ProposalMLP(basis, n_in, hidden=128, max_rows=((nch * B * K + 127) // 128) * 128, seed=2)
+    params = om.init_params(n_in, 128, 11)
+    # moderate steps (sigma ~ 0.3 rad, |mu| small): the reverse density stays well
+    # conditioned, so one-ulp BF16 differences between the device's and the oracle's
+    # features of x' move the ratio by far less than the tolerance
+    nW4 = 6 * 128
+    params[-6 - nW4:-6] *= 0.3
+    params[-6:-3] = 0.0
+    params[-3:] = math.atanh((math.log(0.3) - om.S_MID) / om.S_HALF)
+    net.set_params(params)
+    T0, sigma0, decay, p_net = 2.0, 0.3, 0.995, 0.8
+    ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, 1.05, decay, SEED, ncand=B)
+    ch.set_move(tp3.TP3_MOVE_LEARNED, sigma0, p_net, net)
+    ch.enable_move_log(4)
+    ch.run(1)
+    n = ch.move_log_count()
+    assert n == nch * B
+    dev = torch.device("cuda")
+    idx = torch.arange(n, dtype=torch.int64, device=dev)
+    stride = (n_in + 31) // 32 * 32
+    X = torch.empty((n * K, stride), dtype=torch.bfloat16, device=dev)
+    V = torch.empty((n * K, 3), dtype=torch.float32, device=dev)
+    M = torch.empty((n, 5), dtype=torch.float32, device=dev)
+    ch.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
+    torch.cuda.synchronize()
+    X, V, M = X.float().cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64), M.cpu().numpy()
+    hist = np.zeros(8)
+    P64 = params.astype(np.float64)
+    E0 = e64(start)
+
+    def dev_head(feats):  # the device network on given feature rows
+        d_x = torch.tensor(feats, dtype=torch.bfloat16, device=dev)
+        out = torch.empty((feats.shape[0], 6), dtype=torch.float32, device=dev)
+        net.forward_device(feats.shape[0], d_x.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        o = out.cpu().numpy().astype(np.float64)
+        return o[:, :3], o[:, 3:]
+
+    for c in range(nch):
+        for i in range(B):
+            j = c * B + i
+            T = T0
+            for _ in range(i + 1):
+                T *= decay
+            feats = om.shell_features(start, L, LMAX, hist, T, stride)
+            Xd = X[j * K:(j + 1) * K]
+            # features agree to one BF16 rounding
+            assert np.all(np.abs(Xd - feats) <= 2 ** -7 * np.abs(feats) + 1e-30)
+            z, u = oc.shell_steps(SEED, i, c, K)
+            comp = 1.0 if u < p_net else 0.0
+            assert M[j, 3] == comp
+            v = V[j * K:(j + 1) * K]
+            # network vs oracle network (FP64 accumulation, same BF16 roundings)
+            mu_o, s_o = om.head(om.forward(P64, feats, n_in, 128)[0])
+            mu, s = dev_head(Xd)  # the rows the chain used
+            np.testing.assert_allclose(mu, mu_o, atol=3e-3)
+            np.testing.assert_allclose(s, s_o, atol=3e-3)
+            vref = mu + np.exp(s) * z if comp else sigma0 * z
+            np.testing.assert_allclose(v, vref, rtol=1e-5, atol=1e-6)
+            # Metropolis-Hastings ratio of the mixture, reverse density at x'
+            x2 = oc.rotate_shells(start, v, L, LMAX)
+            mu2, s2 = dev_head(om.shell_features(x2, L, LMAX, hist, T, stride))
+            lr = oc.mixture_log_ratio(v, mu, s, mu2, s2, sigma0, p_net)
+            assert M[j, 4] == pytest.approx(lr, abs=0.05 + 0.01 * abs(lr))
+            assert M[j, 0] == pytest.approx(e64(x2) - E0, abs=5e-7 * abs(E0))
+    ch.close()
+    net.close()

@@ -22,6 +22,20 @@
 // (step, chain, purpose, index), so a step's draws do not depend on the batching.
 // All of it (proposal, scoring, Metropolis test, state update) runs on the device
 // from one captured CUDA graph per launch.
+//
+// Per-shell moves (no reference counterpart; the learned-proposal experiment).
+// TP3_MOVE_SHELL_SO3 rotates every shell k by its own exp([v_k]x) with the isotropic
+// axis-angle step v_k ~ N(0, sigma^2 I3) (sigma adapted like the reference's step
+// sizes), applied with the Wigner-D rotation of rotateStructure
+// (src/spherical_harmonics.jl:572-603) to every even l.  TP3_MOVE_LEARNED draws a
+// candidate from the mixture p * q_net + (1 - p) * q_iso, where q_net samples
+// v_k ~ N(mu_k, diag(exp(2 s_k))) with (mu_k, s_k) the proposal network's output for
+// shell k's features at the current state, and accepts it with the
+// Metropolis-Hastings rule u < exp(-dE/T) q(x | x') / q(x' | x): the reverse density
+// evaluates the network at the proposed state x' for the step -v (the rotation
+// densities include the preimages |v| + 2 pi n of the exponential map).  The network
+// sees the chain's recent dE/T history and the candidate's temperature as fixed
+// parameters of the step, so every step is an exact MH step for exp(-E/T).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -31,12 +45,25 @@
 #include <vector>
 
 #include "ctx_internal.h"
+#include "mlp.h"
+#include "shellrot.cuh"
 
 namespace {
+
+using tp3::kFeatScale;
+using tp3::kMlpHist;
+using tp3::kMlpOutPad;
+using tp3::mlp_head;
+using tp3::mlp_hist_feature;
+using tp3::mlp_temp_feature;
+using tp3::rot_logdens;
 
 constexpr int kPurposeAngle = 0;
 constexpr int kPurposePlane = 1;
 constexpr int kPurposeAccept = 2;
+constexpr int kPurposeComponent = 3;
+constexpr int kPurposeShell = 4;
+constexpr int kMaxShells = 64;
 constexpr int kMaxL = 62;  // even l <= 62: 2l+1 <= 125 real coefficients per block
 
 struct ChainState {
@@ -50,6 +77,13 @@ struct ChainState {
 
 struct LogRow {  // one evaluated step (the columns of det.out, src/determination.jl:512-514)
   double step, sign, E_new, E, dE, T, ap, sigma_L;
+};
+
+struct MoveMeta {  // one logged candidate of a per-shell move
+  float dE, T;     // energy change from the launch's start state, candidate temperature
+  float acc;       // Metropolis decision with the candidate's own uniform (1 / 0)
+  float comp;      // 1 = drawn from the network, 0 = isotropic
+  float lr;        // log q(x | x') - log q(x' | x) (0 without the network)
 };
 
 __host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -205,53 +239,277 @@ __global__ void __launch_bounds__(256) k_propose(const double2* __restrict__ sta
 }
 
 // grid: ceil(nch / 128); block 128.  Metropolis over the speculative candidates.
+// lr (per candidate log q(x|x') - log q(x'|x)) switches to the Metropolis-Hastings
+// rule; without it the rule is the reference's (dE < 0, or dE > 0 and u < exp(-dE/T)).
+// hist (nullable): the chain's last kMlpHist values of dE/T, newest last.
+// meta (nullable): per-candidate log row of the launch's ring slot.
+// sig_lo: first step-size index updated on accept/reject (0 for per-shell moves).
 __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma, const double* __restrict__ Ecand,
                          int nch, int nl, int B, double f, double decay, uint64_t seed, LogRow* __restrict__ log,
-                         int logcap, int Lmax_index) {
+                         int logcap, int Lmax_index, const double* __restrict__ lr, float* __restrict__ hist,
+                         const int* __restrict__ comp, MoveMeta* __restrict__ meta,
+                         long long* __restrict__ launch_ctr, int meta_cap, int sig_lo) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nch) return;
-  ChainState st = cs[c];
-  double* sg = sigma + (size_t)c * nl;
-  st.last = -1;
-  for (int i = 0; i < B; ++i) {
-    const long long s = st.step;  // this step's index (0-based)
-    const double T = st.T * decay;
-    const double En = Ecand[(size_t)c * B + i];
-    const double dE = En - st.E;
-    const double ap = exp(-dE / T);
-    uint32_t ctr[4] = {(uint32_t)s, (uint32_t)c, (uint32_t)kPurposeAccept, 0u};
-    philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
-    const double u = u01(ctr[0]);
-    const bool acc = dE < 0.0 || (dE > 0.0 && u < ap);
-    double sign = 0.0;
-    if (acc) {
-      sign = dE < 0.0 ? 1.0 : -1.0;
-      for (int l = 1; l < nl; ++l) sg[l] *= f;
-      st.E = En;
-    } else {
-      for (int l = 1; l < nl; ++l) sg[l] /= f;
+  const long long launch = launch_ctr ? *launch_ctr : 0;
+  if (c < nch) {
+    ChainState st = cs[c];
+    const double E0 = st.E, T0 = st.T;
+    const long long s0 = st.step;
+    double* sg = sigma + (size_t)c * nl;
+    st.last = -1;
+    for (int i = 0; i < B; ++i) {
+      const long long s = s0 + i;  // this step's index (0-based)
+      double T = T0;
+      for (int t = 0; t <= i; ++t) T *= decay;
+      const double En = Ecand[(size_t)c * B + i];
+      const double dE = En - E0;
+      const double ap = exp(-dE / T);
+      uint32_t ctr[4] = {(uint32_t)s, (uint32_t)c, (uint32_t)kPurposeAccept, 0u};
+      philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+      const double u = u01(ctr[0]);
+      bool acc;
+      if (lr) {
+        const double a = -dE / T + lr[(size_t)c * B + i];
+        acc = a > 0.0 || u < exp(a);
+      } else {
+        acc = dE < 0.0 || (dE > 0.0 && u < ap);
+      }
+      if (meta) {
+        MoveMeta mm;
+        mm.dE = (float)dE; mm.T = (float)T; mm.acc = acc ? 1.f : 0.f;
+        mm.comp = comp ? (float)comp[(size_t)c * B + i] : 0.f;
+        mm.lr = lr ? (float)lr[(size_t)c * B + i] : 0.f;
+        meta[((size_t)(launch % meta_cap) * nch + c) * B + i] = mm;
+      }
+      if (st.last >= 0) continue;  // past the taken step: logged only
+      double sign = 0.0;
+      if (acc) {
+        sign = dE < 0.0 ? 1.0 : -1.0;
+        for (int l = sig_lo; l < nl; ++l) sg[l] *= f;
+        st.E = En;
+      } else {
+        for (int l = sig_lo; l < nl; ++l) sg[l] /= f;
+      }
+      if (hist) {
+        float* hc = hist + (size_t)c * kMlpHist;
+        for (int t = 0; t + 1 < kMlpHist; ++t) hc[t] = hc[t + 1];
+        hc[kMlpHist - 1] = (float)(dE / T);
+      }
+      st.T = T;
+      st.step = s + 1;
+      if (log && logcap > 0) {
+        LogRow r;
+        r.step = (double)(s + 1); r.sign = sign; r.E_new = En; r.E = st.E; r.dE = dE; r.T = T; r.ap = ap;
+        r.sigma_L = sg[Lmax_index];
+        log[(size_t)c * logcap + (size_t)(s % logcap)] = r;
+      }
+      if (acc) {
+        st.accepted += 1;
+        st.last = i;
+        if (!meta) break;
+      }
     }
-    st.T = T;
-    st.step = s + 1;
-    if (log && logcap > 0) {
-      LogRow r;
-      r.step = (double)(s + 1); r.sign = sign; r.E_new = En; r.E = st.E; r.dE = dE; r.T = T; r.ap = ap;
-      r.sigma_L = sg[Lmax_index];
-      log[(size_t)c * logcap + (size_t)(s % logcap)] = r;
-    }
-    if (acc) {
-      st.accepted += 1;
-      st.last = i;
-      break;
-    }
+    cs[c] = st;
   }
-  cs[c] = st;
 }
 
-// grid: nch; block 256.  Adopt the accepted candidate.
+// Feature rows of the proposal network (layout in mlp.h).  grid: nch * nb * K blocks
+// (row = (chain, candidate i < nb, shell)), block 128.  coef: per-row source set,
+// src_per_chain ? state[chain] : cand[chain * B + i].  X (nullable): rows of stride
+// xs; logf (nullable): the i = 0 rows also go to the launch's log slot.
+__global__ void __launch_bounds__(128) k_features(const double2* __restrict__ coef, int src_per_chain, int nch, int nb,
+                                                  int B, int K, int LMAX, int L, const ChainState* __restrict__ cs,
+                                                  double decay, const float* __restrict__ hist,
+                                                  __nv_bfloat16* __restrict__ X, int xs,
+                                                  __nv_bfloat16* __restrict__ logf,
+                                                  const long long* __restrict__ launch_ctr, int log_cap) {
+  __shared__ float red[4];
+  __shared__ float sx[(kMaxL + 1) * (kMaxL + 1)];
+  const int row = blockIdx.x;
+  const int k = row % K, ci = row / K, i = ci % nb, c = ci / nb;
+  const int ncoef = LMAX * LMAX;
+  const double2* src = coef + ((size_t)(src_per_chain ? c : c * B + i) * K + k) * ncoef;
+  const int nf = (L + 1) * (L + 1);
+  const double r2 = 0.7071067811865476;
+  float ss = 0.f;
+  for (int t = threadIdx.x; t < nf; t += blockDim.x) {
+    int l = 0;
+    while ((l + 1) * (l + 1) <= t) ++l;
+    const int u = t - l * l - l;  // -l..l
+    double x;
+    if (u == 0) {
+      x = src[tp3::sean0(l, 0, LMAX)].x;
+    } else if (u > 0) {  // (c_u + (-1)^u c_-u) / sqrt2
+      const double2 a = src[tp3::sean0(l, u, LMAX)], b = src[tp3::sean0(l, -u, LMAX)];
+      x = (a.x + ((u & 1) ? -b.x : b.x)) * r2;
+    } else {  // (i (-1)^u c_u - i c_-u) / sqrt2, real part
+      const double2 a = src[tp3::sean0(l, u, LMAX)], b = src[tp3::sean0(l, -u, LMAX)];
+      x = (((u & 1) ? a.y : -a.y) + b.y) * r2;
+    }
+    sx[t] = (float)x;
+    ss += (float)(x * x);
+  }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  const float nrm = red[0] + red[1] + red[2] + red[3];
+  const float scale = nrm > 0.f ? kFeatScale / sqrtf(nrm) : 0.f;
+  double T = cs[c].T;
+  for (int t = 0; t <= i; ++t) T *= decay;
+  const float tf = mlp_temp_feature(T);
+  const float* hc = hist + (size_t)c * kMlpHist;
+  __nv_bfloat16* xr = X ? X + (size_t)row * xs : nullptr;
+  __nv_bfloat16* lr = nullptr;
+  if (logf && i == 0) lr = logf + (((size_t)(*launch_ctr % log_cap) * nch + c) * K + k) * xs;
+  for (int t = threadIdx.x; t < xs; t += blockDim.x) {
+    float v = 0.f;
+    if (t < nf) v = sx[t] * scale;
+    else if (t < nf + kMlpHist) v = mlp_hist_feature((double)hc[t - nf]);
+    else if (t == nf + kMlpHist) v = tf;
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    if (xr) xr[t] = b;
+    if (lr) lr[t] = b;
+  }
+}
+
+// Per-shell proposal.  grid: nch * B (candidate (chain, i)); block 128.
+// O (nullable): raw network outputs at the current state, rows (chain, i, shell).
+// Writes the candidate's coefficients, its steps v [cand][K][3], the component drawn,
+// and lq[cand] = (log q_net(x'|x), log q_iso(x'|x)) summed over shells.
+__global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict__ state, double2* __restrict__ cand,
+                                                       const ChainState* __restrict__ cs,
+                                                       const double* __restrict__ sigma, int nl, int B, int K, int LMAX,
+                                                       int L, double f, uint64_t seed, const float* __restrict__ O,
+                                                       double p_net, double* __restrict__ vout, int* __restrict__ comp,
+                                                       double* __restrict__ lq, const double* __restrict__ delta,
+                                                       const int* __restrict__ doff, float* __restrict__ vlog,
+                                                       const long long* __restrict__ launch_ctr, int log_cap, int nch) {
+  __shared__ double2 xs[4][2 * tp3::kMaxRotL + 1], ys[4][2 * tp3::kMaxRotL + 1];
+  __shared__ double eul[kMaxShells][3];
+  __shared__ double red[2][128];
+  const int cid = blockIdx.x / B, i = blockIdx.x % B;
+  const int ncoef = LMAX * LMAX;
+  const double2* src = state + (size_t)cid * K * ncoef;
+  double2* dst = cand + (size_t)blockIdx.x * K * ncoef;
+  const long long step = cs[cid].step + i;
+  double sg = sigma[(size_t)cid * nl];
+  for (int t = 0; t < i; ++t) sg /= f;
+  uint32_t pc[4] = {(uint32_t)step, (uint32_t)cid, (uint32_t)kPurposeComponent, 0u};
+  philox4x32_10(pc, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const bool use_net = O != nullptr && u01(pc[0]) < p_net;
+  double lnet = 0.0, liso = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double z[4];
+    normals4(seed, step, cid, kPurposeShell, k, z);
+    double mu[3] = {0, 0, 0}, s[3], v[3];
+    if (O) mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, mu, s);
+    const double ls = log(sg);
+    for (int d = 0; d < 3; ++d) v[d] = use_net ? mu[d] + exp(s[d]) * z[d] : sg * z[d];
+    const double si[3] = {ls, ls, ls}, zero[3] = {0, 0, 0};
+    liso += rot_logdens(v, zero, si);
+    if (O) lnet += rot_logdens(v, mu, s);
+    double* vo = vout + ((size_t)blockIdx.x * K + k) * 3;
+    vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
+    if (vlog) {
+      float* vl = vlog + (((size_t)(*launch_ctr % log_cap) * nch * B + blockIdx.x) * K + k) * 3;
+      vl[0] = (float)v[0]; vl[1] = (float)v[1]; vl[2] = (float)v[2];
+    }
+    tp3::axis_angle_euler(v[0], v[1], v[2], eul[k][0], eul[k][1], eul[k][2]);
+  }
+  red[0][threadIdx.x] = lnet;
+  red[1][threadIdx.x] = liso;
+  for (int e = threadIdx.x; e < K * ncoef; e += blockDim.x) dst[e] = src[e];
+  __syncthreads();
+  for (int h = 64; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + h];
+      red[1][threadIdx.x] += red[1][threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    lq[(size_t)blockIdx.x * 2] = red[0][0];
+    lq[(size_t)blockIdx.x * 2 + 1] = red[1][0];
+    comp[blockIdx.x] = use_net ? 1 : 0;
+  }
+  // rotate every even l >= 2 of every shell (l = 0 is invariant)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nord = L / 2;
+  for (int item = warp; item < K * nord; item += nw) {
+    const int k = item / nord, l = L - 2 * (item % nord);
+    tp3::rotate_order_warp(src + (size_t)k * ncoef, dst + (size_t)k * ncoef, l, LMAX, eul[k][0], eul[k][1],
+                           eul[k][2], delta + doff[l], xs[warp], ys[warp], lane);
+  }
+}
+
+__device__ inline double logaddexp(double a, double b) {
+  const double m = a > b ? a : b;
+  if (m == -INFINITY) return m;
+  return m + log(exp(a - m) + exp(b - m));
+}
+
+// grid: nch * B; block 64.  O2: raw network outputs at the proposed states.
+// lr[cand] = log q(x | x') - log q(x' | x) for the mixture p q_net + (1 - p) q_iso.
+__global__ void k_mh_ratio(const float* __restrict__ O2, const double* __restrict__ v, const double* __restrict__ lq,
+                           int K, double p_net, double* __restrict__ lr) {
+  __shared__ double red[64];
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double mu[3], s[3];
+    mlp_head(O2 + ((size_t)blockIdx.x * K + k) * kMlpOutPad, mu, s);
+    const double* vk = v + ((size_t)blockIdx.x * K + k) * 3;
+    const double rv[3] = {-vk[0], -vk[1], -vk[2]};
+    acc += rot_logdens(rv, mu, s);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = 32; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double fnet = lq[(size_t)blockIdx.x * 2], fiso = lq[(size_t)blockIdx.x * 2 + 1], rnet = red[0];
+    const double lp = log(p_net), lq1 = p_net < 1.0 ? log1p(-p_net) : -INFINITY;
+    // the isotropic density is symmetric: q_iso(x | x') = q_iso(x' | x)
+    lr[blockIdx.x] = logaddexp(lp + rnet, lq1 + fiso) - logaddexp(lp + fnet, lq1 + fiso);
+  }
+}
+
+// grid: nch; block 32.  sigma[c][0] = s0 (per-shell step size).
+__global__ void k_set_sigma0(double* sigma, int nl, int nch, double s0) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nch) sigma[(size_t)c * nl] = s0;
+}
+
+// Training rows from the move log.  grid: n * K blocks (row = (pick, shell)), block 128.
+__global__ void k_log_gather(const long long* __restrict__ idx, int K, int nch, int B, int xs, int tcol,
+                             const __nv_bfloat16* __restrict__ logf, const float* __restrict__ vlog,
+                             const MoveMeta* __restrict__ meta, __nv_bfloat16* __restrict__ X, float* __restrict__ V,
+                             float* __restrict__ M) {
+  const int row = blockIdx.x;
+  const int k = row % K, j = row / K;
+  const long long pos = idx[j];                 // candidate position in the ring
+  const long long sc = pos / B;                 // (slot, chain)
+  const __nv_bfloat16* f = logf + ((size_t)sc * K + k) * xs;
+  const MoveMeta mm = meta[pos];
+  const __nv_bfloat16 tb = __float2bfloat16_rn(mlp_temp_feature((double)mm.T));
+  for (int t = threadIdx.x; t < xs; t += blockDim.x) X[(size_t)row * xs + t] = t == tcol ? tb : f[t];
+  if (threadIdx.x < 3) V[(size_t)row * 3 + threadIdx.x] = vlog[((size_t)pos * K + k) * 3 + threadIdx.x];
+  if (k == 0 && threadIdx.x == 0) {
+    M[(size_t)j * 5 + 0] = mm.dE;
+    M[(size_t)j * 5 + 1] = mm.T;
+    M[(size_t)j * 5 + 2] = mm.acc;
+    M[(size_t)j * 5 + 3] = mm.comp;
+    M[(size_t)j * 5 + 4] = mm.lr;
+  }
+}
+
+// grid: nch; block 256.  Adopt the accepted candidate; advance the launch counter
+// of the move log (read by this launch's earlier kernels).
 __global__ void k_commit(double2* __restrict__ state, const double2* __restrict__ cand,
-                         const ChainState* __restrict__ cs, int B, int n) {
+                         const ChainState* __restrict__ cs, int B, int n, long long* __restrict__ launch_ctr) {
   const int c = blockIdx.x;
+  if (launch_ctr && c == 0 && threadIdx.x == 0) *launch_ctr += 1;
   const int sel = cs[c].last;
   if (sel < 0) return;
   const double2* src = cand + ((size_t)c * B + sel) * n;
@@ -272,10 +530,27 @@ struct tp3_chains {
   ChainState* d_cs = nullptr;
   double* d_sigma = nullptr;
   LogRow* d_log = nullptr;
+  float* d_hist = nullptr;      // [nch][kMlpHist] dE/T history, newest last
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_gen = -1;   // context scratch generation the graph was captured against
   int graph_mode = -1;  // evaluation mode baked into the graph
+  bool dirty = false;   // move settings changed since the capture
+  // per-shell moves
+  int kind = TP3_MOVE_REFERENCE;
+  double p_net = 0.0;
+  tp3_mlp* net = nullptr;
+  double* d_v = nullptr;        // [nch*B][K][3] axis-angle steps
+  double* d_lq = nullptr;       // [nch*B][2] forward log densities (network, isotropic)
+  double* d_lr = nullptr;       // [nch*B] log q(x|x') - log q(x'|x)
+  int* d_comp = nullptr;        // [nch*B] component drawn
+  // move log (training data): ring of mlog_cap launches
+  int mlog_cap = 0;
+  int xs = 0;                   // feature row stride (bf16)
+  long long* d_launch = nullptr;
+  __nv_bfloat16* d_lfeat = nullptr;  // [cap][nch][K][xs]
+  float* d_lv = nullptr;             // [cap][nch][B][K][3]
+  MoveMeta* d_lmeta = nullptr;       // [cap][nch][B]
 };
 
 namespace {
@@ -284,21 +559,52 @@ void chains_free(tp3_chains* h) {
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   cudaFree(h->d_state); cudaFree(h->d_cand); cudaFree(h->d_Ecand); cudaFree(h->d_cs); cudaFree(h->d_sigma);
-  cudaFree(h->d_log);
+  cudaFree(h->d_log); cudaFree(h->d_hist); cudaFree(h->d_v); cudaFree(h->d_lq); cudaFree(h->d_lr); cudaFree(h->d_comp);
+  cudaFree(h->d_launch); cudaFree(h->d_lfeat); cudaFree(h->d_lv); cudaFree(h->d_lmeta);
 }
 
 // one launch: propose B candidates per chain, score them, accept/reject, commit
 int chains_enqueue(tp3_chains* h) {
   tp3_ctx* c = h->ctx;
   const int n = h->nch * h->B;
-  k_propose<<<n, 256, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX, h->L,
-                                      h->f, h->seed);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e;
+  const bool shell = h->kind != TP3_MOVE_REFERENCE;
+  const bool net = h->kind == TP3_MOVE_LEARNED;
+  const bool mlog = shell && h->mlog_cap > 0;
+  long long* lctr = h->d_launch;
+  if (!shell) {
+    k_propose<<<n, 256, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX, h->L,
+                                        h->f, h->seed);
+  } else {
+    const float* O = nullptr;
+    __nv_bfloat16* X = net ? tp3::mlp_input(h->net) : nullptr;
+    if (net || mlog)
+      k_features<<<h->nch * (net ? h->B : 1) * h->K, 128, 0, c->stream>>>(
+          h->d_state, 1, h->nch, net ? h->B : 1, h->B, h->K, h->LMAX, h->L, h->d_cs, h->decay, h->d_hist, X, h->xs,
+          mlog ? h->d_lfeat : nullptr, lctr, h->mlog_cap);
+    if (net) {
+      if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
+      if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
+    }
+    k_propose_shell<<<n, 128, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX,
+                                              h->L, h->f, h->seed, O, h->p_net, h->d_v, h->d_comp, h->d_lq, c->d_delta,
+                                              c->d_doff, mlog ? h->d_lv : nullptr, lctr, h->mlog_cap, h->nch);
+    if (net) {
+      k_features<<<n * h->K, 128, 0, c->stream>>>(h->d_cand, 0, h->nch, h->B, h->B, h->K, h->LMAX, h->L, h->d_cs,
+                                                   h->decay, h->d_hist, X, h->xs, nullptr, lctr, h->mlog_cap);
+      if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
+      if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
+      k_mh_ratio<<<n, 64, 0, c->stream>>>(O, h->d_v, h->d_lq, h->K, h->p_net, h->d_lr);
+    }
+  }
+  e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "propose");
   if (int r = tp3::ctx_run_energy(c, n, h->d_cand, h->d_Ecand)) return r;
-  k_select<<<(h->nch + 127) / 128, 128, 0, c->stream>>>(h->d_cs, h->d_sigma, h->d_Ecand, h->nch, h->nl, h->B, h->f,
-                                                          h->decay, h->seed, h->d_log, h->logcap, h->nl - 1);
-  k_commit<<<h->nch, 256, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->B, h->K * h->ncoef);
+  k_select<<<(h->nch + 127) / 128, 128, 0, c->stream>>>(
+      h->d_cs, h->d_sigma, h->d_Ecand, h->nch, h->nl, h->B, h->f, h->decay, h->seed, h->d_log, h->logcap,
+      shell ? 0 : h->nl - 1, net ? h->d_lr : nullptr, h->d_hist, shell ? h->d_comp : nullptr,
+      mlog ? h->d_lmeta : nullptr, lctr, h->mlog_cap, shell ? 0 : 1);
+  k_commit<<<h->nch, 256, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->B, h->K * h->ncoef, mlog ? lctr : nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "select/commit");
   return TP3_OK;
@@ -330,6 +636,7 @@ int capture(tp3_chains* h) {
   cudaGetLastError();
   h->graph_gen = ctx->scratch_gen;
   h->graph_mode = ctx->mode;
+  h->dirty = false;
   return r;
 }
 
@@ -360,6 +667,8 @@ int tp3_chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0
       (e = cudaMalloc(&h->d_Ecand, (size_t)nchains * ncand * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_cs, (size_t)nchains * sizeof(ChainState))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_sigma, (size_t)nchains * h->nl * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_hist, (size_t)nchains * kMlpHist * sizeof(float))) != cudaSuccess ||
+      (e = cudaMemset(h->d_hist, 0, (size_t)nchains * kMlpHist * sizeof(float))) != cudaSuccess ||
       (log_capacity > 0 && (e = cudaMalloc(&h->d_log, (size_t)nchains * log_capacity * sizeof(LogRow))) != cudaSuccess)) {
     chains_free(h);
     delete h;
@@ -416,7 +725,7 @@ int tp3_chains_run(tp3_chains* h, int launches) {
   if (int r = tp3::ctx_check(c)) return r;
   if (launches < 0) return tp3::ctx_fail(c, TP3_ERR_ARG, "launches must be >= 0");
   if (int r = tp3::ctx_ensure_cap(c, h->nch * h->B)) return r;
-  if (h->graph_gen != c->scratch_gen || h->graph_mode != c->mode) {
+  if (h->graph_gen != c->scratch_gen || h->graph_mode != c->mode || h->dirty) {
     if (int r = capture(h)) return r;
   }
   for (int i = 0; i < launches; ++i) {
@@ -493,8 +802,9 @@ int tp3_chains_snapshot(tp3_chains* h, void* buf, size_t capacity, size_t* bytes
   const size_t nst = (size_t)h->nch * h->K * h->ncoef * sizeof(double2);
   const size_t ncs = (size_t)h->nch * sizeof(ChainState);
   const size_t nsg = (size_t)h->nch * h->nl * sizeof(double);
+  const size_t nhs = (size_t)h->nch * kMlpHist * sizeof(float);
   const size_t hdr = 8 * sizeof(int64_t);
-  const size_t need = hdr + nst + ncs + nsg;
+  const size_t need = hdr + nst + ncs + nsg + nhs;
   *bytes = need;
   if (!buf) return TP3_OK;
   if (capacity < need) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot buffer too small");
@@ -507,7 +817,8 @@ int tp3_chains_snapshot(tp3_chains* h, void* buf, size_t capacity, size_t* bytes
   std::memcpy(p, head, hdr);
   if ((e = cudaMemcpy(p + hdr, h->d_state, nst, cudaMemcpyDeviceToHost)) != cudaSuccess ||
       (e = cudaMemcpy(p + hdr + nst, h->d_cs, ncs, cudaMemcpyDeviceToHost)) != cudaSuccess ||
-      (e = cudaMemcpy(p + hdr + nst + ncs, h->d_sigma, nsg, cudaMemcpyDeviceToHost)) != cudaSuccess)
+      (e = cudaMemcpy(p + hdr + nst + ncs, h->d_sigma, nsg, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(p + hdr + nst + ncs + nsg, h->d_hist, nhs, cudaMemcpyDeviceToHost)) != cudaSuccess)
     return tp3::ctx_cuda_fail(c, e, "snapshot copy");
   return TP3_OK;
 }
@@ -519,8 +830,9 @@ int tp3_chains_restore(tp3_chains* h, const void* buf, size_t bytes) {
   const size_t nst = (size_t)h->nch * h->K * h->ncoef * sizeof(double2);
   const size_t ncs = (size_t)h->nch * sizeof(ChainState);
   const size_t nsg = (size_t)h->nch * h->nl * sizeof(double);
+  const size_t nhs = (size_t)h->nch * kMlpHist * sizeof(float);
   const size_t hdr = 8 * sizeof(int64_t);
-  if (bytes != hdr + nst + ncs + nsg) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot size does not match these chains");
+  if (bytes != hdr + nst + ncs + nsg + nhs) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot size does not match these chains");
   int64_t head[8];
   std::memcpy(head, buf, hdr);
   double f, decay;
@@ -534,7 +846,102 @@ int tp3_chains_restore(tp3_chains* h, const void* buf, size_t bytes) {
   if (e == cudaSuccess) e = cudaMemcpy(h->d_state, p + hdr, nst, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(h->d_cs, p + hdr + nst, ncs, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(h->d_sigma, p + hdr + nst + ncs, nsg, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_hist, p + hdr + nst + ncs + nsg, nhs, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "restore copy");
+  return TP3_OK;
+}
+
+int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp3_mlp* net) {
+  if (!h) return TP3_ERR_ARG;
+  tp3_ctx* c = h->ctx;
+  if (int r = tp3::ctx_check(c)) return r;
+  if (kind != TP3_MOVE_REFERENCE && kind != TP3_MOVE_SHELL_SO3 && kind != TP3_MOVE_LEARNED)
+    return tp3::ctx_fail(c, TP3_ERR_ARG, "unknown move kind");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "set move sync");
+  if (kind != TP3_MOVE_REFERENCE) {
+    if (!(sigma0 > 0.0) || !std::isfinite(sigma0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "sigma0 must be positive");
+    if (h->K > kMaxShells) return tp3::ctx_fail(c, TP3_ERR_UNSUPPORTED, "per-shell moves need K <= 64");
+    if (int r = tp3::ctx_ensure_rot_tables(c, h->L)) return r;
+    const size_t nc = (size_t)h->nch * h->B;
+    if (!h->d_v && ((e = cudaMalloc(&h->d_v, nc * h->K * 3 * sizeof(double))) != cudaSuccess ||
+                    (e = cudaMalloc(&h->d_lq, nc * 2 * sizeof(double))) != cudaSuccess ||
+                    (e = cudaMalloc(&h->d_lr, nc * sizeof(double))) != cudaSuccess ||
+                    (e = cudaMalloc(&h->d_comp, nc * sizeof(int))) != cudaSuccess)) {
+      cudaGetLastError();
+      return tp3::ctx_fail(c, TP3_ERR_ALLOC, std::string("move buffers: ") + cudaGetErrorString(e));
+    }
+    k_set_sigma0<<<(h->nch + 31) / 32, 32, 0, c->stream>>>(h->d_sigma, h->nl, h->nch, sigma0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "set sigma0");
+  }
+  if (kind == TP3_MOVE_LEARNED) {
+    if (!net) return tp3::ctx_fail(c, TP3_ERR_ARG, "learned moves need a network");
+    if (!(p_net > 0.0 && p_net <= 1.0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "p_net must be in (0, 1]");
+    if (tp3::mlp_n_in_of(net) != tp3::mlp_n_in(h->L))
+      return tp3::ctx_fail(c, TP3_ERR_ARG, "network input width is not (L+1)^2 + 9");
+    if (tp3::mlp_max_rows(net) < h->nch * h->B * h->K)
+      return tp3::ctx_fail(c, TP3_ERR_ARG, "network max_rows < chains x candidates x shells");
+  }
+  h->kind = kind;
+  h->p_net = kind == TP3_MOVE_LEARNED ? p_net : 0.0;
+  h->net = kind == TP3_MOVE_LEARNED ? net : nullptr;
+  h->xs = tp3::mlp_n_in_pad(h->L);
+  h->dirty = true;
+  return TP3_OK;
+}
+
+int tp3_chains_enable_move_log(tp3_chains* h, int launches) {
+  if (!h) return TP3_ERR_ARG;
+  tp3_ctx* c = h->ctx;
+  if (int r = tp3::ctx_check(c)) return r;
+  if (launches < 1) return tp3::ctx_fail(c, TP3_ERR_ARG, "launch capacity must be >= 1");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "move log sync");
+  cudaFree(h->d_lfeat); cudaFree(h->d_lv); cudaFree(h->d_lmeta);
+  h->d_lfeat = nullptr; h->d_lv = nullptr; h->d_lmeta = nullptr;
+  h->xs = tp3::mlp_n_in_pad(h->L);
+  const size_t slots = (size_t)launches * h->nch;
+  if ((!h->d_launch && (e = cudaMalloc(&h->d_launch, sizeof(long long))) != cudaSuccess) ||
+      (e = cudaMalloc(&h->d_lfeat, slots * h->K * h->xs * sizeof(__nv_bfloat16))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_lv, slots * h->B * h->K * 3 * sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_lmeta, slots * h->B * sizeof(MoveMeta))) != cudaSuccess) {
+    cudaGetLastError();
+    h->mlog_cap = 0;
+    h->dirty = true;
+    return tp3::ctx_fail(c, TP3_ERR_ALLOC, std::string("move log: ") + cudaGetErrorString(e));
+  }
+  if ((e = cudaMemset(h->d_launch, 0, sizeof(long long))) != cudaSuccess)
+    return tp3::ctx_cuda_fail(c, e, "move log reset");
+  h->mlog_cap = launches;
+  h->dirty = true;
+  return TP3_OK;
+}
+
+int tp3_chains_move_log_count(tp3_chains* h, int64_t* candidates) {
+  if (!h || !candidates) return TP3_ERR_ARG;
+  tp3_ctx* c = h->ctx;
+  if (int r = tp3::ctx_check(c)) return r;
+  *candidates = 0;
+  if (h->mlog_cap == 0) return TP3_OK;
+  long long n = 0;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(&n, h->d_launch, sizeof(long long), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "move log count");
+  *candidates = (int64_t)(n < h->mlog_cap ? n : h->mlog_cap) * h->nch * h->B;
+  return TP3_OK;
+}
+
+int tp3_chains_move_log_gather(tp3_chains* h, int n, const int64_t* d_idx, void* d_x, float* d_v, float* d_meta) {
+  if (!h) return TP3_ERR_ARG;
+  tp3_ctx* c = h->ctx;
+  if (int r = tp3::ctx_check(c)) return r;
+  if (h->mlog_cap == 0) return tp3::ctx_fail(c, TP3_ERR_ARG, "move log not enabled");
+  if (n < 1 || !d_idx || !d_x || !d_v || !d_meta) return tp3::ctx_fail(c, TP3_ERR_ARG, "bad gather arguments");
+  const int tcol = (h->L + 1) * (h->L + 1) + kMlpHist;
+  k_log_gather<<<n * h->K, 128, 0, c->stream>>>((const long long*)d_idx, h->K, h->nch, h->B, h->xs, tcol, h->d_lfeat,
+                                                 h->d_lv, h->d_lmeta, (__nv_bfloat16*)d_x, d_v, d_meta);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "move log gather");
   return TP3_OK;
 }
 

@@ -62,6 +62,11 @@ struct tp3_ctx {
   double* h_E = nullptr;       // pinned [cap]
   int* h_err = nullptr;        // pinned
 
+  // Wigner-D tables: Delta^l = d^l(pi/2) row-major for l = 0..rot_lmax, at d_doff[l]
+  int rot_lmax = -1;
+  double* d_delta = nullptr;
+  int* d_doff = nullptr;
+
   // profiling of the angular + Bayes kernel
   bool prof = false;
   std::vector<cudaEvent_t> ev;  // pairs
@@ -78,4 +83,12 @@ int ctx_ensure_cap(tp3_ctx* c, int n);
 // Score n proposals whose FP64 seanindex-ordered coefficients are in device memory.
 int ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E);
 int ctx_check_device_error(tp3_ctx* c);
+// Upload the Wigner-D tables for orders 0..lmax once (shellrot.cu).
+int ctx_ensure_rot_tables(tp3_ctx* c, int lmax);
+// Proposal network hooks (mlp.cu): its input buffer (rows of mlp_n_in_pad bf16),
+// the raw [rows][kMlpOutPad] outputs of a forward pass over rows [0, R).
+__nv_bfloat16* mlp_input(tp3_mlp* n);
+int mlp_max_rows(const tp3_mlp* n);
+int mlp_n_in_of(const tp3_mlp* n);
+int mlp_forward_raw(tp3_mlp* n, int R, const float** out);
 }  // namespace tp3

@@ -179,6 +179,47 @@ double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
   return (double)(phase * sgnS * w);
 }
 
+double wigner_d_half_pi(int l, int m, int s) {
+  if (l < 0 || std::abs(m) > l || std::abs(s) > l) return 0.0;
+  // d^l_{ms}(pi/2) = 2^-l sqrt((l+m)!(l-m)!(l+s)!(l-s)!)
+  //                  * sum_v (-1)^(v+s-m) / [(l+m-v)! v! (s-m+v)! (l-s-v)!]
+  // (the factorial sum of src/spherical_harmonics.jl:572-586 at beta = pi/2, where
+  // cos(beta/2)^a sin(beta/2)^b = 2^-l for every term).  The sum is exact in big
+  // integers over the common denominator M = (l+m-vmin)! vmax! (s-m+vmax)! (l-s-vmin)!.
+  const long a = l + m, c = s - m, e = l - s;
+  const long vmin = std::max(0L, -c), vmax = std::min(e, a);
+  if (vmin > vmax) return 0.0;
+  SBig acc;
+  for (long v = vmin; v <= vmax; ++v) {
+    Big t = range_prod(a - v, a - vmin);
+    t = Big::mul(t, range_prod(v, vmax));
+    t = Big::mul(t, range_prod(c + v, c + vmax));
+    t = Big::mul(t, range_prod(e - v, e - vmin));
+    acc.add(t, (v & 1) != 0);
+  }
+  Big S;
+  const int sgnS = acc.finish(S);
+  if (sgnS == 0) return 0.0;
+  Big M = Big::mul(fact(a - vmin), fact(vmax));
+  M = Big::mul(M, fact(c + vmax));
+  M = Big::mul(M, fact(e - vmin));
+  Big num = Big::mul(fact(l + m), fact(l - m));
+  num = Big::mul(num, fact(l + s));
+  num = Big::mul(num, fact(l - s));
+  num = Big::mul(num, Big::mul(S, S));
+  const Big den = Big::mul(M, M);
+  long double mn, md;
+  long en, ed;
+  num.to_ld(mn, en);
+  den.to_ld(md, ed);
+  long double r = mn / md;
+  long ex = en - ed - 2L * l;  // the 2^-l factor, squared
+  if (ex & 1) { r *= 2.0L; ex -= 1; }
+  const long double w = sqrtl(r) * ldexpl(1.0L, (int)(ex / 2));
+  const int phase = (c % 2 != 0) ? -1 : 1;  // (-1)^(s-m)
+  return (double)(phase * sgnS * w);
+}
+
 double sphPlm_x(int l, int m, double x) {
   int ma = std::abs(m);
   if (ma > l) return 0.0;

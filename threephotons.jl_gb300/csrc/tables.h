@@ -27,6 +27,12 @@ double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);
 // gsl_sf_legendre_sphPlm as wrapped by src/spherical_harmonics.jl:69-76.
 double sphPlm_x(int l, int m, double x);
 
+// Wigner small-d at beta = pi/2, d^l_{ms}(pi/2), in the convention of the
+// reference's d_work (src/spherical_harmonics.jl:572-586); exact big-integer sum.
+// d^l(beta) then factorises as P Delta E(beta) Delta^T P^* with Delta = d^l(pi/2),
+// P = diag(i^m), E = diag(e^{i m beta}).
+double wigner_d_half_pi(int l, int m, int s);
+
 // 0-based seanindex (src/spherical_harmonics.jl:163-170 minus one).
 int seanindex0(int l, int m, int LMAX);
 

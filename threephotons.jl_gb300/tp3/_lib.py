@@ -31,6 +31,9 @@ TP3_MODE_PLAIN_FP32 = 0
 TP3_MODE_TC_BF16X3 = 1
 TP3_MODE_TC_TF32X3 = 2
 TP3_MODE_AUTO = -1
+TP3_MOVE_REFERENCE = 0
+TP3_MOVE_SHELL_SO3 = 1
+TP3_MOVE_LEARNED = 2
 
 # name -> (restype, argtypes); every symbol include/tp3.h declares
 SIGNATURES = {
@@ -64,7 +67,22 @@ SIGNATURES = {
     "tp3_chains_snapshot": (c_int, [c_void_p, c_void_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
     "tp3_chains_restore": (c_int, [c_void_p, c_void_p, ctypes.c_size_t]),
     "tp3_chains_graph": (c_int, [c_void_p, P(c_int)]),
+    "tp3_chains_set_move": (c_int, [c_void_p, c_int, c_double, c_double, c_void_p]),
+    "tp3_chains_enable_move_log": (c_int, [c_void_p, c_int]),
+    "tp3_chains_move_log_count": (c_int, [c_void_p, P(c_int64)]),
+    "tp3_chains_move_log_gather": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tp3_bayes_energy_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
+    "tp3_wigner_D": (c_int, [c_int, c_double, c_double, c_double, c_void_p]),
+    "tp3_rotate_shells_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "tp3_mlp_create": (c_int, [c_void_p, c_int, c_int, c_int, ctypes.c_uint64, P(c_void_p)]),
+    "tp3_mlp_destroy": (None, [c_void_p]),
+    "tp3_mlp_num_params": (c_int, [c_void_p, P(c_int64)]),
+    "tp3_mlp_get_params": (c_int, [c_void_p, c_void_p, c_int64]),
+    "tp3_mlp_set_params": (c_int, [c_void_p, c_void_p, c_int64]),
+    "tp3_mlp_input_buffer": (c_int, [c_void_p, P(c_void_p), P(c_int)]),
+    "tp3_mlp_forward_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_mlp_loss_grad": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, P(c_double), c_void_p]),
+    "tp3_mlp_train_step": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, ctypes.c_float, P(c_double)]),
     "tp3_profile_enable": (c_int, [c_void_p, c_int]),
     "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),
 }

@@ -10,6 +10,7 @@ annealing loop calls:
     energy(intensity, basis, c3ref, K3_range, measure="Bayes", negativity_factor=0.0)
                                                   src/correlations.jl:196-226
     get_MC_step / random_rotation(_step)           src/determination.jl:232-241, src/utilities.jl:165-190
+    rotationMatrix / rotateStructure               src/spherical_harmonics.jl:588-603
 
 Every number that is part of c3 or the energy is computed by libtp3 on the GPU.
 Errors raise ``TP3Error``; a missing library raises ImportError.  Nothing here
@@ -19,6 +20,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -77,6 +79,27 @@ def Umat(l: int) -> np.ndarray:
     return U
 
 
+def rotationMatrix(theta: float, phi: float, gamma: float, l: int) -> np.ndarray:
+    """Wigner D of order l (spherical_harmonics.jl:588-592): D[m, s] = e^{-i s gamma - i m phi} d_ms(theta),
+    m, s = -l..l (libtp3, FP64 on the host)."""
+    d = 2 * l + 1
+    out = np.empty(2 * d * d, dtype=np.float64)
+    check(load().tp3_wigner_D(l, theta, phi, gamma, out.ctypes.data))
+    return out.view(np.complex128).reshape(d, d, order="F")
+
+
+def rotateStructure(volume: SphericalHarmonicsVolume, theta: float, phi: float, gamma: float, K: int,
+                    lrange) -> SphericalHarmonicsVolume:
+    """Rotate every shell 1..K by rotationMatrix for each l in lrange (spherical_harmonics.jl:595-603)."""
+    from .structure import seanindex0
+    new = volume.copy()
+    for l in lrange:
+        D = rotationMatrix(theta, phi, gamma, l)
+        idx = [seanindex0(l, m, volume.LMAX) for m in range(-l, l + 1)]
+        new.coeff[:K, idx] = volume.coeff[:K, idx] @ D.T
+    return new
+
+
 class BasisTypeGB300:
     """Device-resident basis (role of BasisTypeCuda, src/cuda.jl:24-42).
 
@@ -91,6 +114,7 @@ class BasisTypeGB300:
         self.ctr = {l: Umat(l) for l in self.lrange}
         self.rtc = {l: self.ctr[l].conj().T for l in self.lrange}
         self._lib = load()
+        self._dependents = weakref.WeakSet()
         self._ctx = ctypes.c_void_p()
         check(self._lib.tp3_ctx_create(L, LMAX, N, K, self.lambda_, self.dq, ctypes.byref(self._ctx)))
         info = (ctypes.c_int64 * 8)()
@@ -124,7 +148,14 @@ class BasisTypeGB300:
     def reserve(self, n: int) -> None:
         check(self._lib.tp3_reserve(self._ctx, n), self._ctx)
 
+    def _adopt(self, obj) -> None:
+        """Register an object holding library handles on this context (chains, networks);
+        close() releases it first, so no handle outlives its context."""
+        self._dependents.add(obj)
+
     def close(self) -> None:
+        for d in list(getattr(self, "_dependents", ())):
+            d.close()
         if self._ctx:
             self._lib.tp3_ctx_destroy(self._ctx)
             self._ctx = ctypes.c_void_p()
@@ -194,6 +225,12 @@ class BasisTypeGB300:
 
     def c3_batch_device(self, n: int, d_coeffs_ptr: int, d_c3_ptr: int) -> None:
         check(self._lib.tp3_c3_batch_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr), ctypes.c_void_p(d_c3_ptr)),
+              self._ctx)
+
+    def rotate_shells_device(self, n: int, d_coeffs_ptr: int, d_axis_angle_ptr: int, d_out_ptr: int) -> None:
+        """Rotate shell k of each of n device coefficient sets by exp([v]x), v = axis_angle[set][k] (FP64)."""
+        check(self._lib.tp3_rotate_shells_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr),
+                                                 ctypes.c_void_p(d_axis_angle_ptr), ctypes.c_void_p(d_out_ptr)),
               self._ctx)
 
     def profile_enable(self, on: bool) -> None:

@@ -73,6 +73,7 @@ class Chains:
                                           float(initial_stepsize), float(stepsizefactor),
                                           float(temperature_decay), ctypes.c_uint64(seed), log_capacity,
                                           ctypes.byref(self._h)), basis.ctx)
+        basis._adopt(self)
 
     def run(self, launches: int) -> None:
         check(self._lib.tp3_chains_run(self._h, launches), self.basis.ctx)
@@ -105,6 +106,27 @@ class Chains:
 
     def restore(self, blob: bytes) -> None:
         check(self._lib.tp3_chains_restore(self._h, blob, len(blob)), self.basis.ctx)
+
+    def set_move(self, kind: int, sigma0: float = 0.1, p_net: float = 0.0, net=None) -> None:
+        """Move kind: 0 reference get_MC_step, 1 per-shell isotropic SO(3) step with
+        sigma0 (radians), 2 mixture of the network's step (probability p_net) and the
+        isotropic one, Metropolis-Hastings corrected."""
+        check(self._lib.tp3_chains_set_move(self._h, kind, float(sigma0), float(p_net),
+                                            net.handle if net is not None else None), self.basis.ctx)
+
+    def enable_move_log(self, launches: int) -> None:
+        check(self._lib.tp3_chains_enable_move_log(self._h, launches), self.basis.ctx)
+
+    def move_log_count(self) -> int:
+        n = ctypes.c_int64()
+        check(self._lib.tp3_chains_move_log_count(self._h, ctypes.byref(n)), self.basis.ctx)
+        return n.value
+
+    def move_log_gather(self, n: int, d_idx: int, d_x: int, d_v: int, d_meta: int) -> None:
+        """Device pointers: idx int64[n]; x bf16[n*K][stride]; v float[n*K][3]; meta float[n][5]
+        (dE, T, accepted, drawn-from-network, log MH ratio)."""
+        check(self._lib.tp3_chains_move_log_gather(self._h, n, ctypes.c_void_p(d_idx), ctypes.c_void_p(d_x),
+                                                   ctypes.c_void_p(d_v), ctypes.c_void_p(d_meta)), self.basis.ctx)
 
     @property
     def graph_captured(self) -> bool:

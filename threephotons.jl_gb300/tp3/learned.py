@@ -1,0 +1,180 @@
+"""Learned proposal for the annealer: the network handle over libtp3.
+
+No counterpart in the reference.  ``ProposalMLP`` owns a device network
+(tp3_mlp_*): 3 hidden ReLU layers, BF16 weights and activations, FP32
+accumulation, trained by the library's own tcgen05 forward/backward kernels with
+Adam.  Every method takes device pointers (torch tensors' ``data_ptr()``);
+nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import TP3Error, check, load
+
+
+def n_in_for(L: int) -> int:
+    """Feature width per shell: (L+1)^2 real SH coefficients, 8 history values, log T."""
+    return (L + 1) * (L + 1) + 9
+
+
+def n_in_pad(n_in: int) -> int:
+    return (n_in + 31) // 32 * 32
+
+
+class ProposalMLP:
+    def __init__(self, basis, n_in: int, hidden: int = 512, max_rows: int = 32768, seed: int = 0):
+        self._lib = load()
+        self._basis = basis
+        self.n_in, self.hidden, self.max_rows = n_in, hidden, max_rows
+        self.stride = n_in_pad(n_in)
+        h = ctypes.c_void_p()
+        check(self._lib.tp3_mlp_create(basis.ctx, n_in, hidden, max_rows, ctypes.c_uint64(seed), ctypes.byref(h)),
+              basis.ctx)
+        self._h = h
+        basis._adopt(self)
+        n = ctypes.c_int64()
+        check(self._lib.tp3_mlp_num_params(h, ctypes.byref(n)))
+        self.n_params = n.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.tp3_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, dtype=np.float32)
+        check(self._lib.tp3_mlp_get_params(self._h, out.ctypes.data, self.n_params), self._basis.ctx)
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != self.n_params:
+            raise TP3Error(_lib.TP3_ERR_ARG, f"expected {self.n_params} parameters")
+        check(self._lib.tp3_mlp_set_params(self._h, p.ctypes.data, self.n_params), self._basis.ctx)
+
+    def forward_device(self, rows: int, d_x: int, d_out: int) -> None:
+        """(mu, s) per row into d_out (rows x 6 float32)."""
+        check(self._lib.tp3_mlp_forward_device(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_out)),
+              self._basis.ctx)
+
+    def loss_grad(self, rows: int, d_x: int, d_v: int, d_w: int, want_grad: bool = True):
+        loss = ctypes.c_double()
+        g = np.empty(self.n_params, dtype=np.float32) if want_grad else None
+        check(self._lib.tp3_mlp_loss_grad(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_v),
+                                          ctypes.c_void_p(d_w), ctypes.byref(loss),
+                                          g.ctypes.data if g is not None else None), self._basis.ctx)
+        return loss.value, g
+
+    def train_step(self, rows: int, d_x: int, d_v: int, d_w: int, lr: float, want_loss: bool = False):
+        loss = ctypes.c_double()
+        check(self._lib.tp3_mlp_train_step(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_v),
+                                           ctypes.c_void_p(d_w), ctypes.c_float(lr),
+                                           ctypes.byref(loss) if want_loss else None), self._basis.ctx)
+        return loss.value if want_loss else None
+
+
+# ---------------------------------------------------------------------------
+# Training on logged moves and the annealing comparison
+# ---------------------------------------------------------------------------
+
+def move_weights(meta):
+    """Training weight of a logged candidate (torch tensor [n, 5] -> [n]): accepted moves,
+    counted more the more they lowered the energy (1 + min(-dE/T, 5) for dE < 0)."""
+    import torch
+    dE, T, acc = meta[:, 0], meta[:, 1], meta[:, 2]
+    gain = torch.clamp(-dE / T, min=0.0, max=5.0)
+    return acc * (1.0 + gain)
+
+
+def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr: float = 1e-3, seed: int = 0,
+                 holdout: float = 0.05, log_every: int = 0):
+    """Adam steps on the weighted NLL of logged steps, batches of whole candidates
+    (K rows each) drawn uniformly from the move log.  Returns (train losses, held-out
+    loss before, held-out loss after); the held-out candidates are never trained on."""
+    import torch
+    dev = torch.device("cuda")
+    K = chains.basis.K
+    total = chains.move_log_count()
+    if total < 2:
+        raise TP3Error(_lib.TP3_ERR_ARG, "move log is empty")
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    perm = torch.randperm(total, generator=g)
+    nh = max(1, int(total * holdout))
+    hold, train = perm[:nh], perm[nh:]
+    nb = min(batch_candidates, train.numel())
+    rows = (nb * K + 127) // 128 * 128
+    if rows > net.max_rows:
+        raise TP3Error(_lib.TP3_ERR_ARG, "batch exceeds the network's max_rows")
+    X = torch.zeros((rows, net.stride), dtype=torch.bfloat16, device=dev)
+    V = torch.zeros((rows, 3), dtype=torch.float32, device=dev)
+    W = torch.zeros(rows, dtype=torch.float32, device=dev)
+    M = torch.zeros((nb, 5), dtype=torch.float32, device=dev)
+
+    def fill(idx_cpu):
+        n = idx_cpu.numel()
+        idx = idx_cpu.to(dev, dtype=torch.int64)
+        chains.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
+        w = move_weights(M[:n])
+        W.zero_()
+        W[: n * K] = (w / torch.clamp(w.sum(), min=1e-12)).repeat_interleave(K)
+        if n * K < rows:
+            X[n * K:].zero_()
+            V[n * K:].zero_()
+
+    def heldout_loss():
+        tot, wsum = 0.0, 0
+        for a in range(0, nh, nb):
+            part = hold[a:a + nb]
+            fill(part)
+            l, _ = net.loss_grad(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), want_grad=False)
+            tot += l * part.numel()
+            wsum += part.numel()
+        return tot / max(wsum, 1)
+
+    before = heldout_loss()
+    losses = []
+    for it in range(steps):
+        pick = train[torch.randint(0, train.numel(), (nb,), generator=g)]
+        fill(pick)
+        want = log_every and (it % log_every == 0 or it == steps - 1)
+        l = net.train_step(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), lr, want_loss=bool(want))
+        if want:
+            losses.append((it, l))
+    after = heldout_loss()
+    return losses, before, after
+
+
+def time_to_energy(chains, target: float, max_launches: int, chunk: int = 10):
+    """Run launches in chunks until the median chain energy is <= target; returns
+    (seconds of device time, launches, median energy reached, energy trace)."""
+    import time
+    import torch
+    trace = []
+    t0 = time.perf_counter()
+    done = 0
+    med = float("inf")
+    while done < max_launches:
+        n = min(chunk, max_launches - done)
+        chains.run(n)
+        done += n
+        st = chains.state()
+        med = float(np.median(st["E"]))
+        trace.append((done, time.perf_counter() - t0, med))
+        if med <= target:
+            break
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, done, med, trace
