@@ -182,13 +182,15 @@ int tp3_chains_set_move(tp3_chains* chains, int kind, double sigma0, double p_ne
 
 /* Move log for training the network: a ring of `launches` launches of per-shell
  * moves; per candidate the state's feature rows, the steps v, and
- * (dE, T, accepted, drawn-from-network, log q(x|x') - log q(x'|x)) where accepted is
- * the Metropolis decision with the candidate's own uniform (the chain's actual
- * decision up to its taken step).  tp3_chains_move_log_count returns the candidates held (synchronising);
+ * (dE, T, accepted, drawn-from-network, log q(x|x') - log q(x'|x), sigma_i) where
+ * accepted is the Metropolis decision with the candidate's own uniform (the chain's
+ * actual decision up to its taken step) and sigma_i the candidate's isotropic step
+ * size.  The network proposes relative to sigma_i: for its outputs (mu^_k, s^_k),
+ * shell k's step is N(sigma_i mu^_k, exp(2 (log sigma_i + s^_k - mean_k s^_k))).  tp3_chains_move_log_count returns the candidates held (synchronising);
  * tp3_chains_move_log_gather writes, for n candidate positions d_idx (int64, device,
  * each < count), n x K feature rows (BF16, stride (L+1)^2 + 9 rounded up to 32, the
- * temperature column set to the candidate's), n x K x 3 steps (float) and n x 5
- * meta floats in that order into device buffers. */
+ * temperature column set to the candidate's), n x K x 3 steps divided by sigma_i
+ * (float) and n x 6 meta floats in that order into device buffers. */
 int tp3_chains_enable_move_log(tp3_chains* chains, int launches);
 int tp3_chains_move_log_count(tp3_chains* chains, int64_t* candidates);
 int tp3_chains_move_log_gather(tp3_chains* chains, int n, const int64_t* d_idx, void* d_x, float* d_v, float* d_meta);

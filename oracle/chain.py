@@ -168,6 +168,13 @@ def rot_logdens(v, mu, s) -> float:
     return m + math.log(sum(math.exp(t - m) for t in terms))
 
 
+def shell_params(mu_hat, s_hat, sigma: float):
+    """Per-shell step parameters from the network head relative to the isotropic step
+    size: mu = sigma mu^, s = log sigma + s^ - mean over shells of s^."""
+    mu_hat, s_hat = np.asarray(mu_hat, dtype=np.float64), np.asarray(s_hat, dtype=np.float64)
+    return sigma * mu_hat, math.log(sigma) + s_hat - s_hat.mean(axis=0, keepdims=True)
+
+
 def mixture_log_ratio(v, mu, s, mu2, s2, sigma: float, p_net: float) -> float:
     """log q(x|x') - log q(x'|x) of the mixture p q_net + (1 - p) q_iso over all shells."""
     K = v.shape[0]

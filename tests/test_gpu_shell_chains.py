@@ -111,13 +111,13 @@ def test_learned_moves_match_oracle(setup):
     n_in = n_in_for(L)
     net = ProposalMLP(basis, n_in, hidden=128, max_rows=((nch * B * K + 127) // 128) * 128, seed=2)
     params = om.init_params(n_in, 128, 11)
-    # moderate steps (sigma ~ 0.3 rad, |mu| small): the reverse density stays well
+    # moderate relative steps (|mu^| small, s^ near 0): the reverse density stays well
     # conditioned, so one-ulp BF16 differences between the device's and the oracle's
     # features of x' move the ratio by far less than the tolerance
     nW4 = 6 * 128
     params[-6 - nW4:-6] *= 0.3
     params[-6:-3] = 0.0
-    params[-3:] = math.atanh((math.log(0.3) - om.S_MID) / om.S_HALF)
+    params[-3:] = math.atanh((0.0 - om.S_MID) / om.S_HALF)
     net.set_params(params)
     T0, sigma0, decay, p_net = 2.0, 0.3, 0.995, 0.8
     ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, 1.05, decay, SEED, ncand=B)
@@ -131,7 +131,7 @@ def test_learned_moves_match_oracle(setup):
     stride = (n_in + 31) // 32 * 32
     X = torch.empty((n * K, stride), dtype=torch.bfloat16, device=dev)
     V = torch.empty((n * K, 3), dtype=torch.float32, device=dev)
-    M = torch.empty((n, 5), dtype=torch.float32, device=dev)
+    M = torch.empty((n, 6), dtype=torch.float32, device=dev)
     ch.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
     torch.cuda.synchronize()
     X, V, M = X.float().cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64), M.cpu().numpy()
@@ -166,13 +166,43 @@ def test_learned_moves_match_oracle(setup):
             mu, s = dev_head(Xd)  # the rows the chain used
             np.testing.assert_allclose(mu, mu_o, atol=3e-3)
             np.testing.assert_allclose(s, s_o, atol=3e-3)
-            vref = mu + np.exp(s) * z if comp else sigma0 * z
+            sig_i = sigma0
+            for _ in range(i):  # candidate i assumes i rejections: sigma / f^i
+                sig_i /= 1.05
+            assert M[j, 5] == pytest.approx(sig_i, rel=1e-6)
+            v = v * M[j, 5]  # the log holds v / sigma_i
+            mu, s = oc.shell_params(mu, s, sig_i)
+            vref = mu + np.exp(s) * z if comp else sig_i * z
             np.testing.assert_allclose(v, vref, rtol=1e-5, atol=1e-6)
             # Metropolis-Hastings ratio of the mixture, reverse density at x'
             x2 = oc.rotate_shells(start, v, L, LMAX)
-            mu2, s2 = dev_head(om.shell_features(x2, L, LMAX, hist, T, stride))
-            lr = oc.mixture_log_ratio(v, mu, s, mu2, s2, sigma0, p_net)
+            mu2, s2 = oc.shell_params(*dev_head(om.shell_features(x2, L, LMAX, hist, T, stride)), sig_i)
+            lr = oc.mixture_log_ratio(v, mu, s, mu2, s2, sig_i, p_net)
             assert M[j, 4] == pytest.approx(lr, abs=0.05 + 0.01 * abs(lr))
             assert M[j, 0] == pytest.approx(e64(x2) - E0, abs=5e-7 * abs(E0))
     ch.close()
     net.close()
+
+
+def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
+    """The full learned-proposal protocol at the small configuration: the plain
+    annealer's logged moves train the network on the device (held-out NLL falls), and
+    the learned annealer's time to the plain annealer's final median energy is measured
+    and reported (the gain itself is a measured quantity, not asserted)."""
+    from tp3.learned import learned_vs_plain
+    p = config1["params"]
+    basis = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    basis.set_histogram(config1_hist)
+    res = learned_vs_plain(basis, config1["coeff"], nchains=16, ncand=8, collect_launches=200, train_steps=200,
+                           batch_candidates=256, eval_launches=120, seed=7)
+    basis.close()
+    assert res["collect"]["moves"] == 16 * 8 * 200
+    assert res["train"]["heldout_nll_after"] < res["train"]["heldout_nll_before"]
+    assert math.isfinite(res["learned"]["median_E"]) and math.isfinite(res["plain"]["final_median_E"])
+    assert 0.05 < res["learned"]["accept_rate"] < 0.95
+    with capsys.disabled():
+        print(f"\n[learned proposal, L8 K8 N16] plain: {res['plain']['launches']} launches "
+              f"{res['plain']['seconds']:.3f} s -> median E {res['plain']['final_median_E']:.4f}; learned: "
+              f"{res['learned']['launches']} launches {res['learned']['seconds_to_target']:.3f} s -> "
+              f"{res['learned']['median_E']:.4f} (reached={res['learned']['reached']}, "
+              f"time ratio={res['time_ratio']})")

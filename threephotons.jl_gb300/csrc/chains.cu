@@ -84,6 +84,7 @@ struct MoveMeta {  // one logged candidate of a per-shell move
   float acc;       // Metropolis decision with the candidate's own uniform (1 / 0)
   float comp;      // 1 = drawn from the network, 0 = isotropic
   float lr;        // log q(x | x') - log q(x' | x) (0 without the network)
+  float sig;       // the candidate's isotropic step size sigma_i
 };
 
 __host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -256,8 +257,10 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
     const double E0 = st.E, T0 = st.T;
     const long long s0 = st.step;
     double* sg = sigma + (size_t)c * nl;
+    double sig_i = sg[0];  // sigma_0 / f^i of candidate i (per-shell moves)
     st.last = -1;
     for (int i = 0; i < B; ++i) {
+      if (i > 0) sig_i /= f;
       const long long s = s0 + i;  // this step's index (0-based)
       double T = T0;
       for (int t = 0; t <= i; ++t) T *= decay;
@@ -279,6 +282,7 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
         mm.dE = (float)dE; mm.T = (float)T; mm.acc = acc ? 1.f : 0.f;
         mm.comp = comp ? (float)comp[(size_t)c * B + i] : 0.f;
         mm.lr = lr ? (float)lr[(size_t)c * B + i] : 0.f;
+        mm.sig = (float)sig_i;
         meta[((size_t)(launch % meta_cap) * nch + c) * B + i] = mm;
       }
       if (st.last >= 0) continue;  // past the taken step: logged only
@@ -372,6 +376,25 @@ __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ co
   }
 }
 
+// The network proposes relative to the candidate's isotropic step size sigma_i: for
+// head outputs (mu^_k, s^_k) of the K shells, mu_k = sigma_i mu^_k and
+// s_k = log sigma_i + s^_k - mean_k s^_k, so the network sets how the step is shared
+// between shells and directions while the chain's adapted sigma sets its size.
+__device__ inline void shell_scale_mean(const double (*hs)[3], int K, double m[3]) {
+  m[0] = m[1] = m[2] = 0.0;
+  for (int k = 0; k < K; ++k)
+    for (int d = 0; d < 3; ++d) m[d] += hs[k][d];
+  for (int d = 0; d < 3; ++d) m[d] /= K;
+}
+
+__device__ inline void shell_params(const double hmu[3], const double hs[3], const double m[3], double sg, double ls,
+                                    double mu[3], double s[3]) {
+  for (int d = 0; d < 3; ++d) {
+    mu[d] = sg * hmu[d];
+    s[d] = ls + hs[d] - m[d];
+  }
+}
+
 // Per-shell proposal.  grid: nch * B (candidate (chain, i)); block 128.
 // O (nullable): raw network outputs at the current state, rows (chain, i, shell).
 // Writes the candidate's coefficients, its steps v [cand][K][3], the component drawn,
@@ -387,6 +410,7 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   __shared__ double2 xs[4][2 * tp3::kMaxRotL + 1], ys[4][2 * tp3::kMaxRotL + 1];
   __shared__ double eul[kMaxShells][3];
   __shared__ double red[2][128];
+  __shared__ double hmu[kMaxShells][3], hs[kMaxShells][3];
   const int cid = blockIdx.x / B, i = blockIdx.x % B;
   const int ncoef = LMAX * LMAX;
   const double2* src = state + (size_t)cid * K * ncoef;
@@ -397,13 +421,20 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   uint32_t pc[4] = {(uint32_t)step, (uint32_t)cid, (uint32_t)kPurposeComponent, 0u};
   philox4x32_10(pc, (uint32_t)seed, (uint32_t)(seed >> 32));
   const bool use_net = O != nullptr && u01(pc[0]) < p_net;
+  const double ls = log(sg);
+  double smean[3] = {0, 0, 0};
+  if (O) {
+    for (int k = threadIdx.x; k < K; k += blockDim.x)
+      mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hmu[k], hs[k]);
+    __syncthreads();
+    shell_scale_mean(hs, K, smean);
+  }
   double lnet = 0.0, liso = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double z[4];
     normals4(seed, step, cid, kPurposeShell, k, z);
     double mu[3] = {0, 0, 0}, s[3], v[3];
-    if (O) mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, mu, s);
-    const double ls = log(sg);
+    if (O) shell_params(hmu[k], hs[k], smean, sg, ls, mu, s);
     for (int d = 0; d < 3; ++d) v[d] = use_net ? mu[d] + exp(s[d]) * z[d] : sg * z[d];
     const double si[3] = {ls, ls, ls}, zero[3] = {0, 0, 0};
     liso += rot_logdens(v, zero, si);
@@ -451,12 +482,23 @@ __device__ inline double logaddexp(double a, double b) {
 // grid: nch * B; block 64.  O2: raw network outputs at the proposed states.
 // lr[cand] = log q(x | x') - log q(x' | x) for the mixture p q_net + (1 - p) q_iso.
 __global__ void k_mh_ratio(const float* __restrict__ O2, const double* __restrict__ v, const double* __restrict__ lq,
-                           int K, double p_net, double* __restrict__ lr) {
+                           int K, double p_net, const ChainState* __restrict__ cs, const double* __restrict__ sigma,
+                           int nl, int B, double f, double* __restrict__ lr) {
   __shared__ double red[64];
+  __shared__ double hmu[kMaxShells][3], hs[kMaxShells][3];
+  const int cid = blockIdx.x / B, i = blockIdx.x % B;
+  double sg = sigma[(size_t)cid * nl];
+  for (int t = 0; t < i; ++t) sg /= f;
+  const double ls = log(sg);
+  for (int k = threadIdx.x; k < K; k += blockDim.x)
+    mlp_head(O2 + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hmu[k], hs[k]);
+  __syncthreads();
+  double smean[3];
+  shell_scale_mean(hs, K, smean);
   double acc = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double mu[3], s[3];
-    mlp_head(O2 + ((size_t)blockIdx.x * K + k) * kMlpOutPad, mu, s);
+    shell_params(hmu[k], hs[k], smean, sg, ls, mu, s);
     const double* vk = v + ((size_t)blockIdx.x * K + k) * 3;
     const double rv[3] = {-vk[0], -vk[1], -vk[2]};
     acc += rot_logdens(rv, mu, s);
@@ -494,13 +536,14 @@ __global__ void k_log_gather(const long long* __restrict__ idx, int K, int nch, 
   const MoveMeta mm = meta[pos];
   const __nv_bfloat16 tb = __float2bfloat16_rn(mlp_temp_feature((double)mm.T));
   for (int t = threadIdx.x; t < xs; t += blockDim.x) X[(size_t)row * xs + t] = t == tcol ? tb : f[t];
-  if (threadIdx.x < 3) V[(size_t)row * 3 + threadIdx.x] = vlog[((size_t)pos * K + k) * 3 + threadIdx.x];
+  if (threadIdx.x < 3) V[(size_t)row * 3 + threadIdx.x] = vlog[((size_t)pos * K + k) * 3 + threadIdx.x] / mm.sig;
   if (k == 0 && threadIdx.x == 0) {
-    M[(size_t)j * 5 + 0] = mm.dE;
-    M[(size_t)j * 5 + 1] = mm.T;
-    M[(size_t)j * 5 + 2] = mm.acc;
-    M[(size_t)j * 5 + 3] = mm.comp;
-    M[(size_t)j * 5 + 4] = mm.lr;
+    M[(size_t)j * 6 + 0] = mm.dE;
+    M[(size_t)j * 6 + 1] = mm.T;
+    M[(size_t)j * 6 + 2] = mm.acc;
+    M[(size_t)j * 6 + 3] = mm.comp;
+    M[(size_t)j * 6 + 4] = mm.lr;
+    M[(size_t)j * 6 + 5] = mm.sig;
   }
 }
 
@@ -594,7 +637,8 @@ int chains_enqueue(tp3_chains* h) {
                                                    h->decay, h->d_hist, X, h->xs, nullptr, lctr, h->mlog_cap);
       if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
-      k_mh_ratio<<<n, 64, 0, c->stream>>>(O, h->d_v, h->d_lq, h->K, h->p_net, h->d_lr);
+      k_mh_ratio<<<n, 64, 0, c->stream>>>(O, h->d_v, h->d_lq, h->K, h->p_net, h->d_cs, h->d_sigma, h->nl, h->B, h->f,
+                                          h->d_lr);
     }
   }
   e = cudaGetLastError();

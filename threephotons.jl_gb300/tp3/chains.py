@@ -123,8 +123,8 @@ class Chains:
         return n.value
 
     def move_log_gather(self, n: int, d_idx: int, d_x: int, d_v: int, d_meta: int) -> None:
-        """Device pointers: idx int64[n]; x bf16[n*K][stride]; v float[n*K][3]; meta float[n][5]
-        (dE, T, accepted, drawn-from-network, log MH ratio)."""
+        """Device pointers: idx int64[n]; x bf16[n*K][stride]; v float[n*K][3] (steps / sigma_i);
+        meta float[n][6] (dE, T, accepted, drawn-from-network, log MH ratio, sigma_i)."""
         check(self._lib.tp3_chains_move_log_gather(self._h, n, ctypes.c_void_p(d_idx), ctypes.c_void_p(d_x),
                                                    ctypes.c_void_p(d_v), ctypes.c_void_p(d_meta)), self.basis.ctx)
 

@@ -92,7 +92,7 @@ class ProposalMLP:
 # ---------------------------------------------------------------------------
 
 def move_weights(meta):
-    """Training weight of a logged candidate (torch tensor [n, 5] -> [n]): accepted moves,
+    """Training weight of a logged candidate (torch tensor [n, 6] -> [n]): accepted moves,
     counted more the more they lowered the energy (1 + min(-dE/T, 5) for dE < 0)."""
     import torch
     dE, T, acc = meta[:, 0], meta[:, 1], meta[:, 2]
@@ -122,7 +122,7 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
     X = torch.zeros((rows, net.stride), dtype=torch.bfloat16, device=dev)
     V = torch.zeros((rows, 3), dtype=torch.float32, device=dev)
     W = torch.zeros(rows, dtype=torch.float32, device=dev)
-    M = torch.zeros((nb, 5), dtype=torch.float32, device=dev)
+    M = torch.zeros((nb, 6), dtype=torch.float32, device=dev)
 
     def fill(idx_cpu):
         n = idx_cpu.numel()
@@ -178,3 +178,99 @@ def time_to_energy(chains, target: float, max_launches: int, chunk: int = 10):
             break
     torch.cuda.synchronize()
     return time.perf_counter() - t0, done, med, trace
+
+
+def haar_axis_angles(rng: np.random.Generator, shape) -> np.ndarray:
+    """Axis-angle vectors (shape + (3,)) of Haar-uniform rotations (uniform unit quaternions)."""
+    q = rng.normal(size=tuple(shape) + (4,))
+    q /= np.linalg.norm(q, axis=-1, keepdims=True)
+    q *= np.where(q[..., :1] < 0, -1.0, 1.0)
+    w = np.clip(q[..., 0], -1.0, 1.0)
+    ang = 2.0 * np.arccos(w)
+    s = np.sqrt(np.maximum(1.0 - w * w, 1e-300))
+    return q[..., 1:] / s[..., None] * ang[..., None]
+
+
+def rotated_starts(basis, base: np.ndarray, nchains: int, seed: int) -> np.ndarray:
+    """nchains copies of base[:K] with every shell turned by its own Haar-random rotation
+    (on the device, tp3_rotate_shells_device)."""
+    import torch
+    K, ncoef = basis.K, basis.LMAX ** 2
+    rng = np.random.default_rng(seed)
+    v = haar_axis_angles(rng, (nchains, K))
+    dev = torch.device("cuda")
+    c = np.repeat(np.ascontiguousarray(base[:K], dtype=np.complex128)[None], nchains, axis=0)
+    d_c = torch.from_numpy(c.view(np.float64).copy()).to(dev)
+    d_v = torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+    basis.rotate_shells_device(nchains, d_c.data_ptr(), d_v.data_ptr(), d_c.data_ptr())
+    basis.sync()
+    return d_c.cpu().numpy().view(np.complex128).reshape(nchains, K, ncoef)
+
+
+def learned_vs_plain(basis, base: np.ndarray, nchains: int = 64, ncand: int = 16, collect_launches: int = 977,
+                     train_steps: int = 1500, batch_candidates: int = 1024, eval_launches: int = 300,
+                     sigma0: float = 0.2, stepsizefactor: float = 1.02, temperature_decay: float = 0.9995,
+                     temperature_factor: float = 0.1, p_net: float = 0.8, hidden: int = 512, lr: float = 1e-3,
+                     seed: int = 2024, chunk: int = 10) -> dict:
+    """The learned-proposal experiment on the basis's histogram (set beforehand):
+    1. the plain annealer (isotropic per-shell steps) logs its moves from Haar-rotated
+       starts (collect_launches x nchains x ncand candidates);
+    2. the network is trained on the device on the weighted NLL of those moves;
+    3. from fresh starts (another seed), the plain annealer runs eval_launches launches;
+       its final median energy is the target;
+    4. the learned annealer (mixture p_net network / isotropic, MH-corrected) runs from
+       the same starts with the same schedule until its median energy reaches the target.
+    Times are wall clock around graph replays (chunks of `chunk` launches)."""
+    import time
+    from .chains import Chains
+    K, L = basis.K, basis.L
+    out = {"nchains": nchains, "candidates_per_launch": ncand, "sigma0": sigma0, "stepsizefactor": stepsizefactor,
+           "temperature_decay": temperature_decay, "p_net": p_net, "hidden": hidden}
+    # temperature: temperature_factor x std of the start energies
+    starts_c = rotated_starts(basis, base, nchains, seed)
+    E0 = basis.energy_batch(starts_c)
+    T0 = temperature_factor * float(np.std(E0))
+    out["T0"] = T0
+    # 1. collect
+    t = time.perf_counter()
+    col = Chains(basis, starts_c, T0, 0.1, stepsizefactor, temperature_decay, seed + 1, ncand=ncand)
+    col.set_move(1, sigma0)
+    col.enable_move_log(collect_launches)
+    col.run(collect_launches)
+    n_moves = col.move_log_count()
+    out["collect"] = {"launches": collect_launches, "moves": n_moves, "seconds": time.perf_counter() - t,
+                      "median_E_end": float(np.median(col.state()["E"]))}
+    # 2. train
+    t = time.perf_counter()
+    rows = max(((nchains * ncand * K + 127) // 128) * 128, ((batch_candidates * K + 127) // 128) * 128)
+    net = ProposalMLP(basis, n_in_for(L), hidden=hidden, max_rows=rows, seed=seed + 2)
+    losses, before, after = train_on_log(net, col, train_steps, batch_candidates, lr=lr, seed=seed + 3,
+                                         log_every=max(1, train_steps // 10))
+    col.close()
+    out["train"] = {"steps": train_steps, "batch_candidates": batch_candidates, "lr": lr,
+                    "heldout_nll_before": before, "heldout_nll_after": after, "seconds": time.perf_counter() - t,
+                    "loss_trace": losses}
+    # 3. plain
+    ev_starts = rotated_starts(basis, base, nchains, seed + 10)
+    plain = Chains(basis, ev_starts, T0, 0.1, stepsizefactor, temperature_decay, seed + 11, ncand=ncand)
+    plain.set_move(1, sigma0)
+    plain.run(1)
+    sec_p, n_p, med_p, trace_p = time_to_energy(plain, -float("inf"), eval_launches - 1, chunk)
+    stp = plain.state()
+    plain.close()
+    target = med_p
+    # 4. learned
+    lrn = Chains(basis, ev_starts, T0, 0.1, stepsizefactor, temperature_decay, seed + 11, ncand=ncand)
+    lrn.set_move(2, sigma0, p_net, net)
+    lrn.run(1)
+    sec_l, n_l, med_l, trace_l = time_to_energy(lrn, target, eval_launches - 1, chunk)
+    stl = lrn.state()
+    lrn.close()
+    net.close()
+    out["plain"] = {"seconds": sec_p, "launches": n_p + 1, "final_median_E": med_p,
+                    "accept_rate": float(stp["accepted"].sum() / max(stp["steps"].sum(), 1)), "trace": trace_p}
+    out["learned"] = {"seconds_to_target": sec_l, "launches": n_l + 1, "median_E": med_l,
+                      "reached": bool(med_l <= target),
+                      "accept_rate": float(stl["accepted"].sum() / max(stl["steps"].sum(), 1)), "trace": trace_l}
+    out["time_ratio"] = sec_l / sec_p if med_l <= target else None
+    return out
