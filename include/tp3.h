@@ -95,6 +95,16 @@ void tp3_ctx_destroy(tp3_ctx* ctx);
 int tp3_set_stream(tp3_ctx* ctx, void* cuda_stream);
 int tp3_set_mode(tp3_ctx* ctx, int mode);
 int tp3_get_mode(const tp3_ctx* ctx, int* mode);
+
+/* Autotuner (no reference counterpart): times, on n synthetic real-function
+ * proposals scored against the context's histogram, every evaluation variant this
+ * shape supports -- the plain FP32 path and each tensor-core split mode (BF16 x3,
+ * TF32 x3) with each coupling form that fits (fused pair coupling, two-kernel split
+ * coupling) -- selects the fastest for this context and records it for the shape
+ * (L, LMAX, N, K, lambda, dq) in the process, where TP3_MODE_AUTO finds it.
+ * report (nullable): up to *nreport rows of (mode, split coupling 0/1, ms per
+ * proposal); *nreport returns the number of variants.  Synchronises. */
+int tp3_autotune(tp3_ctx* ctx, int n, double* report, int* nreport);
 /* Pre-size scratch for batches of up to n proposals (otherwise sized on first use). */
 int tp3_reserve(tp3_ctx* ctx, int n);
 
@@ -123,6 +133,22 @@ int tp3_energy_batch(tp3_ctx* ctx, int n, const double* coeffs, double* E);
  * memory, d_E = n doubles in device memory.  Asynchronous on the context stream. */
 int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E);
 
+/* ---- ragged batches (no reference counterpart) --------------------------------
+ * Proposals of different (L, K) scored in one launch on the context's shape (its L
+ * and K are the largest): orders l > L and shells k > K of a proposal are treated as
+ * absent -- exactly the reference's c3 of basis (L, K), whose shell triples are the
+ * first K(K+1)(K+2)/6 of the context's -- and each proposal is scored against its own
+ * histogram of a set.  Tensor-core modes with the one-kernel coupling only. */
+/* Histogram set: nhist histograms (each as for tp3_set_histogram, with K3s[h] >= Ks[h]
+ * shells stored and Ks[h] <= the context's K scored). */
+int tp3_set_histograms(tp3_ctx* ctx, int nhist, const double* const* c3refs, const int* K3s, const int* Ks);
+/* Energies of n proposals (d_coeffs as for tp3_energy_batch_device) with per-proposal
+ * (L, K, histogram index) triples d_lkh (n x 3 int32, device).  Out-of-range triples
+ * are clamped and reported by the next synchronising call as TP3_ERR_ARG. */
+int tp3_energy_batch_ragged_device(tp3_ctx* ctx, int n, const void* d_coeffs, const int* d_lkh, void* d_E);
+/* Upload per-proposal (L, K, histogram) limits without scoring (used by chains). */
+int tp3_ragged_limits_device(tp3_ctx* ctx, int n, const int* d_lkh);
+
 /* Wait for the context stream and report any device-side error (TP3_ERR_TIMEOUT
  * when a bounded wait inside a kernel ran out). */
 int tp3_sync(tp3_ctx* ctx);
@@ -149,6 +175,15 @@ typedef struct tp3_chains tp3_chains;
 int tp3_chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
                       double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
                       int log_capacity, tp3_chains** out);
+/* Chains of different (L, K) scored together (no reference counterpart): chain c
+ * uses chain_lkh[3c..3c+2] = (L, K, histogram index of the context's set,
+ * tp3_set_histograms), with L <= the context's L (the move rotates orders 2..L) and
+ * K <= the histogram's K; all chains' candidates go through one ragged launch per
+ * step.  Other arguments as tp3_chains_create; coeff0 holds the context's K shells
+ * per chain (shells beyond a chain's K are carried along unscored). */
+int tp3_chains_create_ragged(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
+                             double initial_stepsize, double stepsizefactor, double temperature_decay,
+                             uint64_t seed, int log_capacity, const int* chain_lkh, tp3_chains** out);
 void tp3_chains_destroy(tp3_chains* chains);
 /* Enqueue `launches` graph replays (ncand speculative steps per chain each). */
 int tp3_chains_run(tp3_chains* chains, int launches);

@@ -125,7 +125,9 @@ __device__ inline int sidx(int l, int m, int LMAX) {  // 0-based seanindex
 // warp rotates one even l (2..L) of every shell.
 __global__ void __launch_bounds__(256) k_propose(const double2* __restrict__ state, double2* __restrict__ cand,
                                                  const ChainState* __restrict__ cs, const double* __restrict__ sigma,
-                                                 int nl, int B, int K, int LMAX, int L, double f, uint64_t seed) {
+                                                 int nl, int B, int K, int LMAX, int L, double f, uint64_t seed,
+                                                 const tp3::RagInfo* __restrict__ rag) {
+  if (rag) L = rag[blockIdx.x].L;  // a ragged chain rotates its own orders only
   __shared__ double sp[8][2 * kMaxL + 1], sq[8][2 * kMaxL + 1];
   const int cid = blockIdx.x / B, i = blockIdx.x % B;
   const int ncoef = LMAX * LMAX;
@@ -406,8 +408,10 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
                                                        double p_net, double* __restrict__ vout, int* __restrict__ comp,
                                                        double* __restrict__ lq, const double* __restrict__ delta,
                                                        const int* __restrict__ doff, float* __restrict__ vlog,
-                                                       const long long* __restrict__ launch_ctr, int log_cap, int nch) {
+                                                       const long long* __restrict__ launch_ctr, int log_cap, int nch,
+                                                       const tp3::RagInfo* __restrict__ rag) {
   __shared__ double2 xs[4][2 * tp3::kMaxRotL + 1], ys[4][2 * tp3::kMaxRotL + 1];
+  if (rag) L = rag[blockIdx.x].L;
   __shared__ double eul[kMaxShells][3];
   __shared__ double red[2][128];
   __shared__ double hmu[kMaxShells][3], hs[kMaxShells][3];
@@ -574,6 +578,8 @@ struct tp3_chains {
   double* d_sigma = nullptr;
   LogRow* d_log = nullptr;
   float* d_hist = nullptr;      // [nch][kMlpHist] dE/T history, newest last
+  tp3::RagInfo* d_rag = nullptr;  // [nch*B] per-candidate limits of ragged chains (null: the context's shape)
+  int* d_lkh = nullptr;           // [nch*B][3] (L, K, histogram) per candidate
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_gen = -1;   // context scratch generation the graph was captured against
@@ -604,6 +610,7 @@ void chains_free(tp3_chains* h) {
   cudaFree(h->d_state); cudaFree(h->d_cand); cudaFree(h->d_Ecand); cudaFree(h->d_cs); cudaFree(h->d_sigma);
   cudaFree(h->d_log); cudaFree(h->d_hist); cudaFree(h->d_v); cudaFree(h->d_lq); cudaFree(h->d_lr); cudaFree(h->d_comp);
   cudaFree(h->d_launch); cudaFree(h->d_lfeat); cudaFree(h->d_lv); cudaFree(h->d_lmeta);
+  cudaFree(h->d_rag); cudaFree(h->d_lkh);
 }
 
 // one launch: propose B candidates per chain, score them, accept/reject, commit
@@ -617,7 +624,7 @@ int chains_enqueue(tp3_chains* h) {
   long long* lctr = h->d_launch;
   if (!shell) {
     k_propose<<<n, 256, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX, h->L,
-                                        h->f, h->seed);
+                                        h->f, h->seed, h->d_rag);
   } else {
     const float* O = nullptr;
     __nv_bfloat16* X = net ? tp3::mlp_input(h->net) : nullptr;
@@ -631,7 +638,8 @@ int chains_enqueue(tp3_chains* h) {
     }
     k_propose_shell<<<n, 128, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX,
                                               h->L, h->f, h->seed, O, h->p_net, h->d_v, h->d_comp, h->d_lq, c->d_delta,
-                                              c->d_doff, mlog ? h->d_lv : nullptr, lctr, h->mlog_cap, h->nch);
+                                              c->d_doff, mlog ? h->d_lv : nullptr, lctr, h->mlog_cap, h->nch,
+                                              h->d_rag);
     if (net) {
       k_features<<<n * h->K, 128, 0, c->stream>>>(h->d_cand, 0, h->nch, h->B, h->B, h->K, h->LMAX, h->L, h->d_cs,
                                                    h->decay, h->d_hist, X, h->xs, nullptr, lctr, h->mlog_cap);
@@ -643,7 +651,7 @@ int chains_enqueue(tp3_chains* h) {
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "propose");
-  if (int r = tp3::ctx_run_energy(c, n, h->d_cand, h->d_Ecand)) return r;
+  if (int r = tp3::ctx_run_energy(c, n, h->d_cand, h->d_Ecand, h->d_rag)) return r;
   k_select<<<(h->nch + 127) / 128, 128, 0, c->stream>>>(
       h->d_cs, h->d_sigma, h->d_Ecand, h->nch, h->nl, h->B, h->f, h->decay, h->seed, h->d_log, h->logcap,
       shell ? 0 : h->nl - 1, net ? h->d_lr : nullptr, h->d_hist, shell ? h->d_comp : nullptr,
@@ -688,16 +696,36 @@ int capture(tp3_chains* h) {
 
 extern "C" {
 
+static int chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
+                         double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
+                         int log_capacity, const int* lkh, tp3_chains** out);
+
 int tp3_chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
                       double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
                       int log_capacity, tp3_chains** out) {
+  return chains_create(ctx, nchains, ncand, coeff0, T0, initial_stepsize, stepsizefactor, temperature_decay, seed,
+                       log_capacity, nullptr, out);
+}
+
+int tp3_chains_create_ragged(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
+                             double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
+                             int log_capacity, const int* chain_lkh, tp3_chains** out) {
+  if (!chain_lkh) return tp3::ctx_fail(ctx, TP3_ERR_ARG, "chain_lkh is NULL");
+  return chains_create(ctx, nchains, ncand, coeff0, T0, initial_stepsize, stepsizefactor, temperature_decay, seed,
+                       log_capacity, chain_lkh, out);
+}
+
+static int chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0, const double* T0,
+                         double initial_stepsize, double stepsizefactor, double temperature_decay, uint64_t seed,
+                         int log_capacity, const int* lkh, tp3_chains** out) {
   if (int r = tp3::ctx_check(ctx)) return r;
   if (!out || !coeff0 || !T0 || nchains < 1 || ncand < 1 || log_capacity < 0)
     return tp3::ctx_fail(ctx, TP3_ERR_ARG, "bad chain arguments");
   if (!(stepsizefactor > 0.0) || !(temperature_decay > 0.0))
     return tp3::ctx_fail(ctx, TP3_ERR_ARG, "step-size factor and temperature decay must be positive");
   if (ctx->b.L > kMaxL) return tp3::ctx_fail(ctx, TP3_ERR_UNSUPPORTED, "chains need L <= 62");
-  if (!ctx->has_hist) return tp3::ctx_fail(ctx, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
+  if (!lkh && !ctx->has_hist) return tp3::ctx_fail(ctx, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
+  if (lkh && ctx->nhist == 0) return tp3::ctx_fail(ctx, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
   *out = nullptr;
   tp3_chains* h = new tp3_chains();
   h->ctx = ctx;
@@ -725,8 +753,27 @@ int tp3_chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coeff0
     chains_free(h); delete h;
     return tp3::ctx_cuda_fail(ctx, e, "chain upload");
   }
+  const tp3::RagInfo* rag0 = nullptr;
+  if (lkh) {
+    // per-candidate limits [nch * B], then the chains' own [nch] for the initial energies
+    const size_t nc = (size_t)nchains * ncand;
+    std::vector<int> hl(3 * (nc + nchains));
+    for (size_t i = 0; i < nc + nchains; ++i) {
+      const size_t c = i < nc ? i / ncand : i - nc;
+      for (int j = 0; j < 3; ++j) hl[3 * i + j] = lkh[3 * c + j];
+    }
+    if ((e = cudaMalloc(&h->d_lkh, hl.size() * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_rag, (nc + nchains) * sizeof(tp3::RagInfo))) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_lkh, hl.data(), hl.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess) {
+      chains_free(h); delete h;
+      cudaGetLastError();
+      return tp3::ctx_fail(ctx, TP3_ERR_ALLOC, std::string("ragged limits: ") + cudaGetErrorString(e));
+    }
+    if (int r = tp3::ctx_make_rag(ctx, (int)(nc + nchains), h->d_lkh, h->d_rag)) { chains_free(h); delete h; return r; }
+    rag0 = h->d_rag + nc;
+  }
   double* dE0 = h->d_Ecand;  // scratch for the initial energies
-  if (int r = tp3::ctx_run_energy(ctx, nchains, h->d_state, dE0)) { chains_free(h); delete h; return r; }
+  if (int r = tp3::ctx_run_energy(ctx, nchains, h->d_state, dE0, rag0)) { chains_free(h); delete h; return r; }
   std::vector<double> E0(nchains);
   if ((e = cudaMemcpyAsync(E0.data(), dE0, nchains * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
       (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
@@ -919,6 +966,7 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
     if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "set sigma0");
   }
   if (kind == TP3_MOVE_LEARNED) {
+    if (h->d_rag) return tp3::ctx_fail(c, TP3_ERR_UNSUPPORTED, "learned moves need chains of one shape");
     if (!net) return tp3::ctx_fail(c, TP3_ERR_ARG, "learned moves need a network");
     if (!(p_net > 0.0 && p_net <= 1.0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "p_net must be in (0, 1]");
     if (tp3::mlp_n_in_of(net) != tp3::mlp_n_in(h->L))

@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <random>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -27,6 +29,19 @@ using tp3::TcTables;
 
 namespace {
 thread_local std::string g_create_error;
+
+// Autotuned evaluation variant (mode, coupling form) per shape, shared by every
+// context of the process; TP3_MODE_AUTO uses it when present.
+struct TuneEntry {
+  int mode = -1;
+  int split = 0;
+};
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, double, double>, TuneEntry> g_tuned;
+
+std::tuple<int, int, int, int, double, double> tune_key(const tp3::Basis& b) {
+  return std::make_tuple(b.L, b.LMAX, b.N, b.K, b.lambda, b.dq);
+}
 
 }  // namespace
 
@@ -306,6 +321,7 @@ std::string setup_tc(tp3_ctx* c) {
   if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
       (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
       (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, chunks_sym, &tc.chunks_sym)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
+      (e = upload(c, b.c_l, &tc.cl)) != cudaSuccess ||
       (e = upload(c, cmir, &tc.cmir)) != cudaSuccess || (e = upload(c, doff, &tc.doff)) != cudaSuccess ||
       (e = upload(c, units_sym, &tc.units_sym)) != cudaSuccess ||
       (e = upload(c, units_gen, &tc.units_gen)) != cudaSuccess ||
@@ -412,14 +428,18 @@ int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) {
 }
 
 // Gather + coupling stage for n proposals whose FP64 coefficients are in d_coeff.
-int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool compact = false) {
+int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool compact = false,
+                 const tp3::RagInfo* rag = nullptr) {
   const auto& t = c->t;
   cudaError_t e;
   const tp3::CoeffLayout lay = compact ? tp3::CoeffLayout{t.cident, t.nc} : tp3::CoeffLayout{t.csean, t.LMAX * t.LMAX};
   if (is_tc(c->mode)) {
-    if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream, rag)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
-    if (c->tc.split)
+    if (rag)  // ragged batches use the one-kernel coupling (it skips absent blocks and shells)
+      e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, c->mode == TP3_MODE_TC_TF32X3,
+                                  want_T32 ? c->d_T : nullptr, c->stream, rag);
+    else if (c->tc.split)
       e = tp3::launch_couple_split(t, c->tc, n, c->d_cc, c->d_sym, c->d_D, c->d_Thi, c->d_Tlo,
                                    c->mode == TP3_MODE_TC_TF32X3, want_T32 ? c->d_T : nullptr, c->stream);
     else
@@ -440,20 +460,28 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
 const float* plain_A(tp3_ctx* c) { return c->t.nqp > 0 ? c->d_H : c->d_T; }
 
 // Score n proposals whose FP64 coefficients are already in d_coeff (device).
-int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool compact = false) {
+int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool compact = false,
+               const tp3::RagInfo* rag = nullptr) {
   const auto& t = c->t;
   cudaError_t e;
-  if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
-  if (int r = run_coupling(c, n, d_coeff, false, compact)) return r;
+  if (rag) {
+    if (c->nhist == 0) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
+    if (!is_tc(c->mode) || !c->tc.fused_ok)
+      return fail(c, TP3_ERR_UNSUPPORTED, "ragged batches need a tensor-core mode with the one-kernel coupling");
+  } else if (!c->has_hist) {
+    return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
+  }
+  if (int r = run_coupling(c, n, d_coeff, false, compact, rag)) return r;
   cudaEvent_t a, b;
   int pr = prof_begin(c, &a, &b);
   if (is_tc(c->mode)) {
     const bool tf = c->mode == TP3_MODE_TC_TF32X3;
-    if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, c->d_qt, c->d_Qfold, c->d_Eslab, nullptr,
-                                    c->d_err, tf, c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, rag ? c->d_qt_set : c->d_qt,
+                                    rag ? c->d_Qf_set : c->d_Qfold, c->d_Eslab, nullptr, c->d_err, tf, c->stream,
+                                    rag)) != cudaSuccess)
       return cuda_fail(c, e, "angular_tc");
     if (pr) cudaEventRecord(b, c->stream);
-    if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream)) != cudaSuccess)
+    if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream, rag)) != cudaSuccess)
       return cuda_fail(c, e, "finalize_slabs");
   } else {
     const int ncg = tp3::plain_ncg(t);
@@ -473,7 +501,9 @@ int check_device_error(tp3_ctx* c) {
   if (*c->h_err != 0) {
     const int code = *c->h_err;
     cudaMemset(c->d_err, 0, sizeof(int));
-    return fail(c, code, "a bounded device wait ran out; results of this call are invalid");
+    return fail(c, code, code == TP3_ERR_TIMEOUT ? "a bounded device wait ran out; results of this call are invalid"
+                                                 : "a device-side argument check failed (ragged limits out of range); "
+                                                   "results of this call are invalid");
   }
   return TP3_OK;
 }
@@ -485,16 +515,73 @@ int check_ctx(tp3_ctx* c) {
   return TP3_OK;
 }
 
+// Folded, slab-normalised histogram of Kh shells (slabs with k1 < Kh; the rest zero)
+// in the tensor-core epilogue layout qt [klp/128][Gu][128] and the folded slab sums Qf.
+const char* fold_histogram(const Basis& b, const DevTables& t, const double* c3ref, int K3, int Kh, float* qt,
+                           double* Qf) {
+  const int G = b.G;
+  const int klen = Kh * (Kh + 1) * (Kh + 2) / 6;
+  std::vector<double> fold(b.Gu);
+  std::fill(qt, qt + (size_t)t.klp * b.Gu, 0.f);
+  for (int ki = 0; ki < b.klength; ++ki) {
+    Qf[ki] = 0.0;
+    if (ki >= klen) continue;
+    const size_t off = (size_t)G * ((size_t)b.k3s[ki] + (size_t)K3 * ((size_t)b.k2s[ki] + (size_t)K3 * b.k1s[ki]));
+    const double* s = c3ref + off;
+    double l1 = 0.0;
+    for (int g = 0; g < G; ++g) {
+      if (!std::isfinite(s[g])) return "histogram holds NaN or Inf";
+      l1 += std::fabs(s[g]);
+    }
+    if (!(l1 > 0.0)) return "histogram slab with zero L1 norm";
+    std::fill(fold.begin(), fold.end(), 0.0);
+    for (int g = 0; g < G; ++g) fold[b.g_to_u[g]] += s[g] / l1;
+    const int tile = ki / 128, r = ki % 128;
+    double qf = 0.0;
+    for (int u = 0; u < b.Gu; ++u) {
+      const float vf = (float)fold[u];
+      qt[((size_t)tile * b.Gu + u) * 128 + r] = vf;
+      qf += (double)vf;
+    }
+    Qf[ki] = qf;
+  }
+  return nullptr;
+}
+
+// (L, K, hist) triples -> RagInfo, clamped into range; a bad triple sets *err.
+__global__ void k_rag_info(const int* __restrict__ lkh, int n, int Lmax, int Kmax, int nhist,
+                           const int* __restrict__ histK, tp3::RagInfo* __restrict__ out, int* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int L = lkh[3 * i], K = lkh[3 * i + 1], h = lkh[3 * i + 2];
+  bool bad = false;
+  if (h < 0 || h >= nhist) { bad = true; h = 0; }
+  if (L < 0 || L > Lmax) { bad = true; L = L < 0 ? 0 : Lmax; }
+  if (K < 1 || K > histK[h]) { bad = true; K = K < 1 ? 1 : histK[h]; }
+  if (K > Kmax) K = Kmax;
+  if (bad) atomicExch(err, TP3_ERR_ARG);
+  tp3::RagInfo r;
+  r.L = L; r.K = K; r.klen = K * (K + 1) * (K + 2) / 6; r.hist = h;
+  out[i] = r;
+}
+
 }  // namespace
 
 int tp3::ctx_fail(tp3_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
 int tp3::ctx_cuda_fail(tp3_ctx* c, cudaError_t e, const char* where) { return cuda_fail(c, e, where); }
 int tp3::ctx_check(tp3_ctx* c) { return check_ctx(c); }
 int tp3::ctx_ensure_cap(tp3_ctx* c, int n) { return ensure_cap(c, n); }
-int tp3::ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E) {
-  return run_energy(c, n, d_coeff, d_E);
+int tp3::ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, const tp3::RagInfo* rag) {
+  return run_energy(c, n, d_coeff, d_E, false, rag);
 }
 int tp3::ctx_check_device_error(tp3_ctx* c) { return check_device_error(c); }
+int tp3::ctx_make_rag(tp3_ctx* c, int n, const int* d_lkh, tp3::RagInfo* out) {
+  if (c->nhist == 0) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
+  k_rag_info<<<(n + 127) / 128, 128, 0, c->stream>>>(d_lkh, n, c->b.L, c->b.K, c->nhist, c->d_hist_K, out, c->d_err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "ragged limits");
+  return TP3_OK;
+}
 
 extern "C" {
 
@@ -688,6 +775,7 @@ void tp3_ctx_destroy(tp3_ctx* c) {
   free_scratch(c);
   for (void* p : c->allocs) cudaFree(p);
   cudaFree(c->d_qfull); cudaFree(c->d_Qfull); cudaFree(c->d_qt); cudaFree(c->d_Qfold); cudaFree(c->d_c3);
+  cudaFree(c->d_qt_set); cudaFree(c->d_Qf_set); cudaFree(c->d_rag);
   cudaFree(c->d_err);
   cudaFreeHost(c->h_err);
   for (auto ev : c->ev) cudaEventDestroy(ev);
@@ -703,10 +791,127 @@ int tp3_set_stream(tp3_ctx* c, void* s) {
 
 int tp3_set_mode(tp3_ctx* c, int mode) {
   if (int r = check_ctx(c)) return r;
-  if (mode == TP3_MODE_AUTO) mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
+  if (mode == TP3_MODE_AUTO) {
+    TuneEntry te;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tuned.find(tune_key(c->b));
+      if (it != g_tuned.end()) te = it->second;
+    }
+    if (te.mode >= 0 && (te.mode == TP3_MODE_PLAIN_FP32 || c->tc_ok)) {
+      c->mode = te.mode;
+      if (c->tc_ok) c->tc.split = te.split ? c->tc.split_ok : !c->tc.fused_ok;
+      return TP3_OK;
+    }
+    mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
+  }
   if (is_tc(mode) && !c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core mode unavailable: " + c->tc_why);
   if (mode != TP3_MODE_PLAIN_FP32 && !is_tc(mode)) return fail(c, TP3_ERR_ARG, "unknown mode");
   c->mode = mode;
+  return TP3_OK;
+}
+
+int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
+  if (int r = check_ctx(c)) return r;
+  if (n < 1) return fail(c, TP3_ERR_ARG, "n must be >= 1");
+  if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "autotune scores proposals: set a histogram first");
+  const Basis& b = c->b;
+  // variants: the plain path, and each tensor-core mode with each coupling form it can run
+  std::vector<std::pair<int, int>> vars = {{TP3_MODE_PLAIN_FP32, 0}};
+  if (c->tc_ok)
+    for (int m : {TP3_MODE_TC_BF16X3, TP3_MODE_TC_TF32X3}) {
+      if (c->tc.fused_ok) vars.push_back({m, 0});
+      if (c->tc.split_ok) vars.push_back({m, 1});
+    }
+  // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
+  const size_t nco = (size_t)b.K * b.LMAX * b.LMAX;
+  std::vector<double> h(2 * nco * n, 0.0);
+  std::mt19937_64 rng(12345);
+  std::normal_distribution<double> nd(0.0, 1.0);
+  for (int p = 0; p < n; ++p)
+    for (int k = 0; k < b.K; ++k)
+      for (int l = 0; l < b.LMAX; ++l)
+        for (int m = 0; m <= l; ++m) {
+          double* a = &h[2 * ((size_t)p * nco + (size_t)k * b.LMAX * b.LMAX + tp3::seanindex0(l, m, b.LMAX))];
+          const double sc = 1.0 / (1.0 + l + 0.2 * k);
+          a[0] = nd(rng) * sc;
+          a[1] = m == 0 ? 0.0 : nd(rng) * sc;
+          if (m > 0) {
+            double* bb = &h[2 * ((size_t)p * nco + (size_t)k * b.LMAX * b.LMAX + tp3::seanindex0(l, -m, b.LMAX))];
+            const double sg = (m & 1) ? -1.0 : 1.0;
+            bb[0] = sg * a[0];
+            bb[1] = -sg * a[1];
+          }
+        }
+  double2* d_c = nullptr;
+  double* d_e = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e;
+  if ((e = cudaMalloc(&d_c, nco * n * sizeof(double2))) != cudaSuccess ||
+      (e = cudaMalloc(&d_e, n * sizeof(double))) != cudaSuccess || (e = cudaEventCreate(&e0)) != cudaSuccess ||
+      (e = cudaEventCreate(&e1)) != cudaSuccess ||
+      (e = cudaMemcpy(d_c, h.data(), nco * n * sizeof(double2), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    cudaFree(d_c); cudaFree(d_e);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return cuda_fail(c, e, "autotune setup");
+  }
+  const int mode0 = c->mode;
+  const bool split0 = c->tc_ok ? c->tc.split : false;
+  const bool prof0 = c->prof;
+  c->prof = false;
+  int best = -1, rc = TP3_OK;
+  double best_ms = 0.0;
+  std::vector<double> ms(vars.size(), -1.0);
+  for (size_t v = 0; v < vars.size() && rc == TP3_OK; ++v) {
+    c->mode = vars[v].first;
+    if (c->tc_ok) c->tc.split = vars[v].second != 0;
+    if ((rc = ensure_cap(c, n)) != TP3_OK) break;
+    if ((rc = run_energy(c, n, d_c, d_e)) != TP3_OK) break;  // warm-up
+    double mn = 1e300;
+    for (int rep = 0; rep < 3 && rc == TP3_OK; ++rep) {
+      cudaEventRecord(e0, c->stream);
+      rc = run_energy(c, n, d_c, d_e);
+      cudaEventRecord(e1, c->stream);
+      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) { rc = cuda_fail(c, e, "autotune timing"); break; }
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      mn = std::min(mn, (double)t);
+    }
+    if (rc == TP3_OK) rc = check_device_error(c);
+    if (rc != TP3_OK) break;
+    ms[v] = mn / n;
+    if (best < 0 || ms[v] < best_ms) { best = (int)v; best_ms = ms[v]; }
+  }
+  cudaFree(d_c); cudaFree(d_e);
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  c->prof = prof0;
+  if (rc != TP3_OK || best < 0) {
+    c->mode = mode0;
+    if (c->tc_ok) c->tc.split = split0;
+    return rc != TP3_OK ? rc : fail(c, TP3_ERR_UNSUPPORTED, "no variant ran");
+  }
+  c->mode = vars[best].first;
+  if (c->tc_ok) c->tc.split = vars[best].second != 0 ? true : !c->tc.fused_ok;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    TuneEntry te;
+    te.mode = vars[best].first;
+    te.split = vars[best].second;
+    g_tuned[tune_key(b)] = te;
+  }
+  if (nreport) {
+    const int cap = *nreport;
+    int k = 0;
+    for (size_t v = 0; v < vars.size() && k < cap; ++v, ++k) {
+      if (report) {
+        report[3 * k] = vars[v].first;
+        report[3 * k + 1] = vars[v].second;
+        report[3 * k + 2] = ms[v];
+      }
+    }
+    *nreport = (int)vars.size();
+  }
   return TP3_OK;
 }
 
@@ -777,6 +982,71 @@ int tp3_set_histogram(tp3_ctx* c, const double* c3ref, int K3) {
     return cuda_fail(c, e, "histogram upload");
   c->has_hist = true;
   return TP3_OK;
+}
+
+int tp3_set_histograms(tp3_ctx* c, int nhist, const double* const* c3refs, const int* K3s, const int* Ks) {
+  if (int r = check_ctx(c)) return r;
+  if (nhist < 1 || !c3refs || !K3s || !Ks) return fail(c, TP3_ERR_ARG, "bad histogram set");
+  const Basis& b = c->b;
+  const DevTables& t = c->t;
+  const size_t per = (size_t)t.klp * b.Gu;
+  std::vector<float> qt(per * nhist);
+  std::vector<double> Qf((size_t)b.klength * nhist);
+  std::vector<int> hk(nhist);
+  for (int h = 0; h < nhist; ++h) {
+    if (!c3refs[h]) return fail(c, TP3_ERR_ARG, "histogram pointer is NULL");
+    if (Ks[h] < 1 || Ks[h] > b.K || K3s[h] < Ks[h])
+      return fail(c, TP3_ERR_ARG, "each histogram needs 1 <= K <= the basis K and K3 >= K");
+    if (const char* m = fold_histogram(b, t, c3refs[h], K3s[h], Ks[h], qt.data() + per * h, Qf.data() + (size_t)b.klength * h))
+      return fail(c, TP3_ERR_BAD_HISTOGRAM, m);
+    hk[h] = Ks[h];
+  }
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "histogram set sync");
+  cudaFree(c->d_qt_set); cudaFree(c->d_Qf_set);
+  c->d_qt_set = nullptr; c->d_Qf_set = nullptr; c->nhist = 0;
+  int* d_hk = nullptr;
+  if ((e = cudaMalloc(&c->d_qt_set, qt.size() * sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_Qf_set, Qf.size() * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&d_hk, hk.size() * sizeof(int))) != cudaSuccess)
+    return cuda_fail(c, e, "cudaMalloc histogram set");
+  c->allocs.push_back(d_hk);
+  if ((e = cudaMemcpy(c->d_qt_set, qt.data(), qt.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(c->d_Qf_set, Qf.data(), Qf.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(d_hk, hk.data(), hk.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(c, e, "histogram set upload");
+  c->hist_K = hk;
+  c->d_hist_K = d_hk;
+  c->nhist = nhist;
+  return TP3_OK;
+}
+
+int tp3_ragged_limits_device(tp3_ctx* c, int n, const int* d_lkh) {
+  if (int r = check_ctx(c)) return r;
+  if (n < 1 || !d_lkh) return fail(c, TP3_ERR_ARG, "bad ragged limits");
+  if (c->nhist == 0) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
+  cudaError_t e;
+  if (n > c->rag_cap) {
+    cudaFree(c->d_rag);
+    c->d_rag = nullptr;
+    c->rag_cap = 0;
+    if ((e = cudaMalloc(&c->d_rag, (size_t)n * sizeof(tp3::RagInfo))) != cudaSuccess)
+      return cuda_fail(c, e, "cudaMalloc ragged limits");
+    c->rag_cap = n;
+    c->scratch_gen++;
+  }
+  k_rag_info<<<(n + 127) / 128, 128, 0, c->stream>>>(d_lkh, n, c->b.L, c->b.K, c->nhist, c->d_hist_K, c->d_rag,
+                                                      c->d_err);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "ragged limits");
+  return TP3_OK;
+}
+
+int tp3_energy_batch_ragged_device(tp3_ctx* c, int n, const void* d_coeffs, const int* d_lkh, void* d_E) {
+  if (int r = check_ctx(c)) return r;
+  if (n < 1 || !d_coeffs || !d_E) return fail(c, TP3_ERR_ARG, "bad batch arguments");
+  if (int r = ensure_cap(c, n)) return r;
+  if (int r = tp3_ragged_limits_device(c, n, d_lkh)) return r;
+  return run_energy(c, n, (const double2*)d_coeffs, (double*)d_E, false, c->d_rag);
 }
 
 int tp3_c3(tp3_ctx* c, const double* coeff, float* out) {

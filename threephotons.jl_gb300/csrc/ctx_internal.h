@@ -62,6 +62,15 @@ struct tp3_ctx {
   double* h_E = nullptr;       // pinned [cap]
   int* h_err = nullptr;        // pinned
 
+  // histogram set of ragged batches: [nhist][klp/128][Gu][128] and [nhist][klength]
+  int nhist = 0;
+  float* d_qt_set = nullptr;
+  double* d_Qf_set = nullptr;
+  std::vector<int> hist_K;          // shells of each histogram of the set
+  int* d_hist_K = nullptr;
+  tp3::RagInfo* d_rag = nullptr;    // [cap] per-proposal limits of the current ragged batch
+  int rag_cap = 0;
+
   // Wigner-D tables: Delta^l = d^l(pi/2) row-major for l = 0..rot_lmax, at d_doff[l]
   int rot_lmax = -1;
   double* d_delta = nullptr;
@@ -80,9 +89,12 @@ int ctx_fail(tp3_ctx* c, int code, const std::string& msg);
 int ctx_cuda_fail(tp3_ctx* c, cudaError_t e, const char* where);
 int ctx_check(tp3_ctx* c);
 int ctx_ensure_cap(tp3_ctx* c, int n);
-// Score n proposals whose FP64 seanindex-ordered coefficients are in device memory.
-int ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E);
+// Score n proposals whose FP64 seanindex-ordered coefficients are in device memory
+// (rag: per-proposal limits of a ragged batch, device; null for the whole shape).
+int ctx_run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, const RagInfo* rag = nullptr);
 int ctx_check_device_error(tp3_ctx* c);
+// Per-proposal RagInfo from (L, K, histogram) triples (device), validated on the device.
+int ctx_make_rag(tp3_ctx* c, int n, const int* d_lkh, RagInfo* out);
 // Upload the Wigner-D tables for orders 0..lmax once (shellrot.cu).
 int ctx_ensure_rot_tables(tp3_ctx* c, int lmax);
 // Proposal network hooks (mlp.cu): its input buffer (rows of mlp_n_in_pad bf16),

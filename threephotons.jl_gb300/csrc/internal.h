@@ -85,6 +85,7 @@ struct TcTables {
   int dmax = 0;                  // largest l1 (or l2) of any block
   int unit_wmax = 0;             // largest 3j row range of any unit (floats)
   const int* cm = nullptr;       // [nc] m of each compact coefficient
+  const int* cl = nullptr;       // [nc] l of each compact coefficient
   const int* cmir = nullptr;     // [nc] compact index of (l, -m)
   int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
   int NP = 0, nhalf = 0;   // unique grid points padded to 256 * nhalf
@@ -98,6 +99,14 @@ struct TcTables {
   const float* Flo32 = nullptr;        // [NP][KP] fp32 remainder
 };
 
+// Per-proposal limits of a ragged batch (chains of different L and K scored in one
+// launch on the context's largest shape): orders above L and shells from K on are
+// treated as absent, only the first klen = K(K+1)(K+2)/6 shell triples are scored,
+// against histogram number hist of the context's histogram set.
+struct RagInfo {
+  int L, K, klen, hist;
+};
+
 struct TcMaps {
   CUtensorMap a_hi, a_lo, b_hi, b_lo;
 };
@@ -108,12 +117,16 @@ size_t tc_smem_bytes();
 constexpr int kCoupleMaxDynSmem = 227 * 1024 - 2048;
 cudaError_t tc_configure();
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
-                              float2* cc, int* sym, cudaStream_t s);
+                              float2* cc, int* sym, cudaStream_t s, const RagInfo* rag = nullptr);
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s);
+                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s,
+                               const RagInfo* rag = nullptr);
+// qt / Qs: one histogram, or (rag) the histogram set with strides klp * Gu and klength.
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
-                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s);
-cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s);
+                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s,
+                              const RagInfo* rag = nullptr);
+cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s,
+                                  const RagInfo* rag = nullptr);
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
 size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
 cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);

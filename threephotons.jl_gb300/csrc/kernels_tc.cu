@@ -68,7 +68,8 @@ __device__ __forceinline__ int ki_index(int k1, int k2, int k3) {
 __global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, const int* __restrict__ csean,
                                                     const int* __restrict__ cm, const int* __restrict__ cmir,
                                                     const double2* __restrict__ coeff, float2* __restrict__ cc,
-                                                    int* __restrict__ sym) {
+                                                    int* __restrict__ sym, const int* __restrict__ cl,
+                                                    const RagInfo* __restrict__ rag) {
   const int prop = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const double2* cp = coeff + (size_t)prop * K * ncoef;
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, co
       const double2 a = ck[csean[c]];
       v = make_float2((float)a.x, (s && m == 0) ? 0.f : (float)a.y);
     }
+    if (rag && (cl[c] > rag[prop].L || k >= rag[prop].K)) v = make_float2(0.f, 0.f);  // absent orders / shells
     out[i] = v;
   }
   if (threadIdx.x == 0) sym[prop] = s;
@@ -132,9 +134,24 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
     const int2* __restrict__ chunks_gen, int nchunks_gen, int pmax_gen, int SDp,
     const int2* __restrict__ chunks_sym, int nchunks_sym, int pmax_sym, int SDhp, int wsmem, int klp, int KP,
     const int* __restrict__ symflags, void* __restrict__ Thi, void* __restrict__ Tlo, bool tf32out,
-    float* __restrict__ T32, int ldT32) {
+    float* __restrict__ T32, int ldT32, const RagInfo* __restrict__ rag) {
   extern __shared__ __align__(16) float smf[];
   const int prop = blockIdx.y;
+  int Kp = K;
+  if (rag) {
+    const RagInfo ri = rag[prop];
+    Kp = ri.K;
+    const PairBlock pb0 = pbs[blockIdx.x];
+    if (pb0.l1 > ri.L || pb0.l2 > ri.L) {
+      // absent orders: the block's l-triples are zero for this proposal's scored rows
+      for (int i = threadIdx.x; i < ri.klen * pb0.nl3; i += blockDim.x) {
+        const int ki = i / pb0.nl3, sj = i - ki * pb0.nl3;
+        store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + pb0.lt_base + sj, 0.f, tf32out);
+        if (T32) T32[((size_t)prop * klp + ki) * ldT32 + pb0.lt_base + sj] = 0.f;
+      }
+      return;
+    }
+  }
   // real-function coefficients: only m3 >= 0 of D is formed, D[-m3] = (-1)^m3 conj(D[m3])
   // and T = Re(D[0] c[0]) + 2 sum_{m3 > 0} Re(D[m3] c[m3]); D rows then hold m3 = 0..l3
   // only (row length SDhp instead of SDp), so a chunk holds about twice the shell pairs.
@@ -166,9 +183,12 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
   // D is double-buffered: phase 2 of chunk ch and phase 1 of chunk ch+1 need no
   // barrier between them, so one __syncthreads per chunk suffices and uneven items
   // of the two phases overlap across warps.
+  int done = 0;  // chunks processed (parity of the D buffer)
   for (int ch = 0; ch < nchunks; ++ch) {
     const int k1hi = chunks[ch].x, k1lo = chunks[ch].y;
-    float2* Dbuf = sD + (size_t)(ch & 1) * pmax * rowD;
+    if (k1lo >= Kp) continue;  // shells beyond this proposal's K: rows not scored
+    float2* Dbuf = sD + (size_t)(done & 1) * pmax * rowD;
+    ++done;
     int npairs = 0;
     for (int k1 = k1hi; k1 >= k1lo; --k1) npairs += k1 + 1;
     // ---- phase 1: longest diagonals (small |m3|) first ----
@@ -341,8 +361,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
     const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
     int Gu, int nhalf, int klength, const float* __restrict__ qt, const double* __restrict__ Qs,
     const double* __restrict__ tf, int mult, double* __restrict__ Eslab, float* __restrict__ c3out,
-    const int* __restrict__ u_to_g, int N, int* __restrict__ err) {
+    const int* __restrict__ u_to_g, int N, int* __restrict__ err, const RagInfo* __restrict__ rag) {
   extern __shared__ uint8_t smem_raw[];
+  if (rag) {
+    // ragged batch: tiles past the proposal's scored shell triples do no work, and
+    // the Bayes terms read the proposal's own histogram
+    const RagInfo ri = rag[blockIdx.y];
+    if ((int)blockIdx.x * kBM >= ri.klen) return;
+    qt += (size_t)ri.hist * klp * Gu;
+    Qs += (size_t)ri.hist * klength;
+  }
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stages = base;
   TcSmemHeader* hd = (TcSmemHeader*)(base + kStages * kStageBytes);
@@ -519,14 +547,16 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
   e = (a - (s - bb)) + (b - bb);
 }
 
-// grid: n; block 256.  Deterministic compensated sum of per-slab energies.
+// grid: n; block 256.  Deterministic compensated sum of per-slab energies (the first
+// rag[prop].klen slabs of a ragged batch).
 __global__ void __launch_bounds__(256) k_finalize_slabs(const double* __restrict__ Eslab, int klength,
-                                                        double* __restrict__ E) {
+                                                        double* __restrict__ E, const RagInfo* __restrict__ rag) {
   __shared__ double ss[256], sc[256];
   const int prop = blockIdx.x;
   const double* e = Eslab + (size_t)prop * klength;
+  const int nk = rag ? rag[prop].klen : klength;
   double s = 0.0, c = 0.0;
-  for (int ki = threadIdx.x; ki < klength; ki += blockDim.x) {
+  for (int ki = threadIdx.x; ki < nk; ki += blockDim.x) {
     double t, err;
     two_sum(s, e[ki], t, err);
     s = t;
@@ -576,19 +606,20 @@ cudaError_t tc_configure() {
 }
 
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
-                              float2* cc, int* sym, cudaStream_t s) {
-  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, lay.stride, lay.map, tc.cm, tc.cmir, coeff, cc, sym);
+                              float2* cc, int* sym, cudaStream_t s, const RagInfo* rag) {
+  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, lay.stride, lay.map, tc.cm, tc.cmir, coeff, cc, sym, tc.cl, rag);
   return cudaGetLastError();
 }
 
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
-                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s) {
+                               void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s, const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
   const size_t smem = tc.couple_smem;
 #define TP3_CP_LAUNCH(S, W)                                                                                \
   k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(                                                  \
       cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,         \
-      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, tf32, T32, t.n_ltp)
+      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, tf32, T32, t.n_ltp, \
+      rag)
   if (tc.w_smem) {
     if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true);
     else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true);
@@ -607,13 +638,14 @@ cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, co
 }
 
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
-                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s) {
+                              const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s,
+                              const RagInfo* rag) {
   dim3 grid(t.klp / kBM, n);
   const size_t smem = tc_smem_bytes();
 #define TP3_ANG(ST, TF)                                                                                        \
   k_angular_tc<ST, TF><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, \
                                                      tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out,      \
-                                                     t.u_to_g, t.N, err)
+                                                     t.u_to_g, t.N, err, rag)
   if (c3out) {
     if (tf32) TP3_ANG(true, true); else TP3_ANG(true, false);
   } else {
@@ -623,8 +655,9 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s) {
-  k_finalize_slabs<<<n, 256, 0, s>>>(Eslab, klength, E);
+cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s,
+                                  const RagInfo* rag) {
+  k_finalize_slabs<<<n, 256, 0, s>>>(Eslab, klength, E, rag);
   return cudaGetLastError();
 }
 

@@ -49,6 +49,7 @@ SIGNATURES = {
     "tp3_set_mode": (c_int, [c_void_p, c_int]),
     "tp3_get_mode": (c_int, [c_void_p, P(c_int)]),
     "tp3_reserve": (c_int, [c_void_p, c_int]),
+    "tp3_autotune": (c_int, [c_void_p, c_int, c_void_p, P(c_int)]),
     "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),
     "tp3_c3": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tp3_c3_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
@@ -57,8 +58,13 @@ SIGNATURES = {
     "tp3_energy": (c_int, [c_void_p, c_void_p, P(c_double)]),
     "tp3_energy_batch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "tp3_energy_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "tp3_set_histograms": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "tp3_energy_batch_ragged_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "tp3_ragged_limits_device": (c_int, [c_void_p, c_int, c_void_p]),
     "tp3_chains_create": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_double,
                                   ctypes.c_uint64, c_int, P(c_void_p)]),
+    "tp3_chains_create_ragged": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_double,
+                                         ctypes.c_uint64, c_int, c_void_p, P(c_void_p)]),
     "tp3_chains_destroy": (None, [c_void_p]),
     "tp3_chains_run": (c_int, [c_void_p, c_int]),
     "tp3_chains_state": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -148,6 +148,14 @@ class BasisTypeGB300:
     def reserve(self, n: int) -> None:
         check(self._lib.tp3_reserve(self._ctx, n), self._ctx)
 
+    def autotune(self, n: int = 64) -> list:
+        """Time every evaluation variant on n synthetic proposals, keep the fastest (also
+        for later TP3_MODE_AUTO contexts of this shape); returns [(mode, split, ms/proposal)]."""
+        cap = ctypes.c_int(16)
+        rep = np.zeros(3 * 16)
+        check(self._lib.tp3_autotune(self._ctx, n, rep.ctypes.data, ctypes.byref(cap)), self._ctx)
+        return [(int(rep[3 * i]), int(rep[3 * i + 1]), float(rep[3 * i + 2])) for i in range(min(cap.value, 16))]
+
     def _adopt(self, obj) -> None:
         """Register an object holding library handles on this context (chains, networks);
         close() releases it first, so no handle outlives its context."""
@@ -222,6 +230,21 @@ class BasisTypeGB300:
     def energy_batch_device(self, n: int, d_coeffs_ptr: int, d_E_ptr: int) -> None:
         check(self._lib.tp3_energy_batch_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr),
                                                 ctypes.c_void_p(d_E_ptr)), self._ctx)
+
+    def set_histograms(self, hists, Ks) -> None:
+        """Histogram set of ragged batches: hists[h] as for set_histogram (N x 2N x K3 x K3 x K3,
+        K3 >= Ks[h]), scored on its first Ks[h] shells."""
+        arrs = [np.asfortranarray(h, dtype=np.float64) for h in hists]
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        K3 = np.array([a.shape[2] for a in arrs], dtype=np.int32)
+        Kh = np.ascontiguousarray(Ks, dtype=np.int32)
+        check(self._lib.tp3_set_histograms(self._ctx, len(arrs), ptrs, K3.ctypes.data, Kh.ctypes.data), self._ctx)
+        self._hist_set = arrs  # keep alive until uploaded (the call copies)
+
+    def energy_batch_ragged_device(self, n: int, d_coeffs_ptr: int, d_lkh_ptr: int, d_E_ptr: int) -> None:
+        check(self._lib.tp3_energy_batch_ragged_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr),
+                                                       ctypes.c_void_p(d_lkh_ptr), ctypes.c_void_p(d_E_ptr)),
+              self._ctx)
 
     def c3_batch_device(self, n: int, d_coeffs_ptr: int, d_c3_ptr: int) -> None:
         check(self._lib.tp3_c3_batch_device(self._ctx, n, ctypes.c_void_p(d_coeffs_ptr), ctypes.c_void_p(d_c3_ptr)),

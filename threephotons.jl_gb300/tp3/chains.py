@@ -58,7 +58,8 @@ class Chains:
 
     def __init__(self, basis: BasisTypeGB300, coeff0: np.ndarray, T0, initial_stepsize: float,
                  stepsizefactor: float, temperature_decay: float, seed: int, ncand: int = 16,
-                 log_capacity: int = 0):
+                 log_capacity: int = 0, shapes=None):
+        """shapes (ragged chains): per chain (L, K, histogram index) of basis.set_histograms."""
         self.basis = basis
         self._lib = load()
         c = np.ascontiguousarray(np.asarray(coeff0)[:, : basis.K], dtype=np.complex128)
@@ -69,10 +70,17 @@ class Chains:
         self.log_capacity = log_capacity
         T = np.ascontiguousarray(np.broadcast_to(np.asarray(T0, dtype=np.float64), (self.n,)))
         self._h = ctypes.c_void_p()
-        check(self._lib.tp3_chains_create(basis.ctx, self.n, ncand, c.ctypes.data, T.ctypes.data,
-                                          float(initial_stepsize), float(stepsizefactor),
-                                          float(temperature_decay), ctypes.c_uint64(seed), log_capacity,
-                                          ctypes.byref(self._h)), basis.ctx)
+        if shapes is None:
+            check(self._lib.tp3_chains_create(basis.ctx, self.n, ncand, c.ctypes.data, T.ctypes.data,
+                                              float(initial_stepsize), float(stepsizefactor),
+                                              float(temperature_decay), ctypes.c_uint64(seed), log_capacity,
+                                              ctypes.byref(self._h)), basis.ctx)
+        else:
+            lkh = np.ascontiguousarray(shapes, dtype=np.int32).reshape(self.n, 3)
+            check(self._lib.tp3_chains_create_ragged(basis.ctx, self.n, ncand, c.ctypes.data, T.ctypes.data,
+                                                     float(initial_stepsize), float(stepsizefactor),
+                                                     float(temperature_decay), ctypes.c_uint64(seed), log_capacity,
+                                                     lkh.ctypes.data, ctypes.byref(self._h)), basis.ctx)
         basis._adopt(self)
 
     def run(self, launches: int) -> None:
