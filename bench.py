@@ -1,7 +1,12 @@
 """Throughput benchmark: c3 + Bayes proposal evaluations per second at L=18, K=26, N=32.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--mode plain|tc|auto]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--mode auto|tuned|plain|tc|tf32]
     python bench.py --impl reference [--steps K] [--warmup W]
+    python bench.py --workload ragged      # 64 chains x 16 candidates, K in 16..26, L in 12..18, own histograms
+    python bench.py --workload learned     # learned vs plain annealer: time to the plain final energy
+
+--mode tuned (and auto) runs the evaluation-variant autotuner first and benchmarks its
+choice; plain / tc / tf32 force the plain FP32, BF16 hi/lo x3 or TF32 hi/lo x3 path.
 
 Workload (one "step" = one batch of B proposals scored end to end):
   * a seeded 327-atom synthetic molecule (C/N/O/S 60/20/18/2 %, uniform in a 13 A
@@ -44,6 +49,8 @@ N_ATOMS, MOL_SEED, HIST_SEED, PROP_SEED = 327, 20240601, 7, 99
 TRIPLETS = 1e9
 METRIC = "c3+Bayes proposal evals/s at L18 K26 N32"
 UNIT = "proposals/s"
+MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
+DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
 
 
 def dist_env():
@@ -209,19 +216,143 @@ def run_reference(args):
     return 0
 
 
+def _molecule_job(args):
+    n_atoms, seed, kcount = args
+    from tp3.structure import synthetic_molecule, intensity_coefficients
+    return intensity_coefficients(synthetic_molecule(n_atoms, seed=seed), LMAX, KMAX, RMAX, kcount=kcount)
+
+
+def run_ragged(args):
+    """64 chains x 16 speculative candidates per launch; chain c has its own K (16..26), L
+    (12..18), molecule (200-400 atoms) and 1e9-triplet histogram; all candidates of a
+    launch go through one ragged tensor-core launch on the L18 K26 N32 shape, replayed
+    from a CUDA graph."""
+    import multiprocessing as mp
+    import torch
+    import tp3
+    from tp3.chains import Chains
+    from tp3.structure import poisson_histogram, loadHistograms
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    nch, ncand = 64, 16
+    rng = np.random.default_rng(20250301 + rank)
+    Ks = rng.integers(16, K + 1, nch)
+    Ls = rng.choice([12, 14, 16, 18], nch)
+    atoms = rng.integers(200, 401, nch)
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        coeffs = pool.map(_molecule_job, [(int(a), 5000 + 97 * c + rank, K) for c, a in enumerate(atoms)])
+    coeffs = np.stack([c[:K] for c in coeffs])
+    basis = tp3.calculate_basis(L, LMAX, N, K)
+    from tp3.structure import seanindex0
+    hists = []
+    for c in range(nch):
+        x = coeffs[c].copy()
+        for l in range(Ls[c] + 1, LMAX):
+            x[:, [seanindex0(l, m, LMAX) for m in range(-l, l + 1)]] = 0
+        c3 = basis.c3_raw(x).astype(np.float64)
+        kl = int(Ks[c] * (Ks[c] + 1) * (Ks[c] + 2) // 6)
+        hists.append(loadHistograms(poisson_histogram(c3[:, :kl], int(Ks[c]), N, TRIPLETS, seed=HIST_SEED + c),
+                                    int(Ks[c])))
+    basis.set_histograms(hists, Ks)
+    # the autotuner times full-shape proposals against the first full-K chain's histogram
+    full = int(np.argmax(Ks))
+    c3f = basis.c3_raw(coeffs[full]).astype(np.float64)
+    basis.set_histogram(loadHistograms(poisson_histogram(c3f, K, N, TRIPLETS, seed=HIST_SEED), K))
+    tuning = basis.autotune(64)
+    if basis.mode == tp3.TP3_MODE_PLAIN_FP32:
+        basis.set_mode(tp3.TP3_MODE_TC_BF16X3)  # ragged launches are tensor-core only
+    shapes = [(int(Ls[c]), int(Ks[c]), c) for c in range(nch)]
+    ch = Chains(basis, coeffs, 0.1, math.pi / 4, 1.02, 0.99998, 4242 + rank, ncand=ncand, shapes=shapes)
+    for _ in range(args.warmup):
+        ch.run(1)
+    s0 = ch.state()
+    stream = torch.cuda.Stream()  # a real stream: the library treats handle 0 as "its own stream"
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.steps)
+    torch.cuda.synchronize()
+    basis.set_stream(stream.cuda_stream)
+    ev0.record(stream)
+    ch.run(reps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    s1 = ch.state()
+    basis.set_stream(None)
+    ch.close()
+    ms = max_over_ranks(ms)
+    value = whole_job_rate(ws, nch * ncand, reps, ms)
+    line = {"metric": "ragged c3+Bayes proposal evals/s, 64 chains x 16 candidates, K 16..26, L 12..18, N32",
+            "value": value, "unit": UNIT, "n_gpus": ws, "steps": reps, "warmup": args.warmup,
+            "ms_per_step": ms / reps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES.get(basis.mode, "fp32"), "data": "synthetic",
+            "config": {"workload": "64 chains (own molecule of 200-400 atoms, own 1e9-triplet histogram, K in "
+                                   "16..26, L in 12..18, N32, LMAX25) x 16 speculative candidates per CUDA-graph "
+                                   "replay; one ragged tensor-core launch per step on the L18 K26 shape",
+                       "Ks": Ks.tolist(), "Ls": Ls.tolist(), "mode": MODE_NAMES.get(basis.mode),
+                       "autotune": [{"mode": MODE_NAMES.get(m), "split_coupling": bool(sp), "ms_per_proposal": t}
+                                    for m, sp, t in tuning]},
+            "chain_steps_per_s": float((s1["steps"] - s0["steps"]).sum()) / (ms / 1e3),
+            # per replay: propose, gather, couple, angular + Bayes, finalize, select, commit
+            "gpu_launches": 7 * reps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    basis.close()
+    return 0
+
+
+def run_learned(args):
+    """The learned-proposal experiment at L18 K26 N32 (64 chains x 16 candidates): the
+    isotropic per-shell annealer logs >= 1e6 moves, the network is trained on the device,
+    and the learned annealer's wall-clock to the plain annealer's final median energy is
+    measured from fresh starts (each shell of the molecule turned by a Haar rotation)."""
+    import torch
+    import tp3
+    from tp3.learned import learned_vs_plain
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    base = molecule_coefficients()
+    basis = tp3.calculate_basis(L, LMAX, N, K)
+    basis.set_histogram(build_histogram(basis, base))
+    basis.autotune(64)
+    res = learned_vs_plain(basis, base, seed=2024 + rank)
+    basis.close()
+    plain_s = res["plain"]["seconds"]
+    lrn_s = res["learned"]["seconds_to_target"] if res["learned"]["reached"] else None
+    line = {"metric": "time to the plain annealer's final median energy (learned proposal), L18 K26 N32",
+            "value": lrn_s, "unit": "s", "n_gpus": ws, "steps": res["plain"]["launches"], "warmup": 1,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, fp64 moves",
+            "data": "synthetic",
+            "config": {"workload": "64 chains x 16 candidates, per-shell SO(3) moves, 327-atom molecule, "
+                                   "1e9-triplet histogram; plain = isotropic steps, learned = 0.8 network / 0.2 "
+                                   "isotropic mixture with Metropolis-Hastings correction",
+                       "collect_moves": res["collect"]["moves"]},
+            "plain_seconds": plain_s, "time_ratio": res["time_ratio"],
+            "plain_final_median_E": res["plain"]["final_median_E"], "learned_median_E": res["learned"]["median_E"],
+            "accept_rate": {"plain": res["plain"]["accept_rate"], "learned": res["learned"]["accept_rate"]},
+            "train": {k: res["train"][k] for k in ("steps", "heldout_nll_before", "heldout_nll_after", "seconds")}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--mode", default="auto", choices=["auto", "plain", "tc"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "tuned", "plain", "tc", "tf32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chains", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ragged":
+        return run_ragged(args)
+    if args.workload == "learned":
+        return run_learned(args)
     args.warmup = max(args.warmup, 3)
 
     import torch
@@ -231,13 +362,19 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    mode = {"auto": tp3.TP3_MODE_AUTO, "plain": tp3.TP3_MODE_PLAIN_FP32, "tc": tp3.TP3_MODE_TC_BF16X3}[args.mode]
+    mode = {"auto": None, "tuned": None, "plain": tp3.TP3_MODE_PLAIN_FP32, "tc": tp3.TP3_MODE_TC_BF16X3,
+            "tf32": tp3.TP3_MODE_TC_TF32X3}[args.mode]
 
     base = molecule_coefficients()
     basis = tp3.calculate_basis(L, LMAX, N, K)
     hist = build_histogram(basis, base)
     basis.set_histogram(hist)
-    basis.set_mode(mode)
+    tuning = None
+    if mode is None:
+        tuning = [{"mode": MODE_NAMES.get(m, str(m)), "split_coupling": bool(sp), "ms_per_proposal": ms}
+                  for m, sp, ms in basis.autotune(args.batch)]
+    else:
+        basis.set_mode(mode)
     mode_used = basis.mode
     B = args.batch
     basis.reserve(B)
@@ -355,12 +492,12 @@ def main():
     kernels_per_step = 4
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {0: "fp32", 1: "bf16x3 (fp32 accumulate)"}.get(mode_used, "fp32"),
+            "vs_baseline": None, "dtype": DTYPES.get(mode_used, "fp32"),
             "data": "synthetic",
             "config": {"workload": f"L18 K26 N32 LMAX25, {B} proposals per step (get_MC_step moves of a 327-atom "
                                    "synthetic molecule's intensity), 1e9-triplet Poisson histogram",
                        "L": L, "K": K, "N": N, "LMAX": LMAX, "proposals_per_step": B,
-                       "mode": {0: "plain_fp32", 1: "tc_bf16x3"}.get(mode_used, str(mode_used)),
+                       "mode": MODE_NAMES.get(mode_used, str(mode_used)), "autotune": tuning,
                        "l2": "flushed (512 MB write) between steps, outside the per-step events"},
             "e2e": e2e, "roofline": roofline, "clocks": clocks, "chains": chains_info,
             "gpu_launches": kernels_per_step * args.steps}

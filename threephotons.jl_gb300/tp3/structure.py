@@ -139,8 +139,9 @@ def seanindex0(l: int, m: int, LMAX: int) -> int:
 
 
 def intensity_coefficients(atoms: list, LMAX: int, KMAX: int, rmax: float, n_theta: int = 0,
-                           n_phi: int = 0) -> np.ndarray:
-    """Intensity SH coefficients, complex128 [KMAX, LMAX^2] in seanindex order."""
+                           n_phi: int = 0, kcount: int = 0) -> np.ndarray:
+    """Intensity SH coefficients, complex128 [KMAX, LMAX^2] in seanindex order (only the
+    first kcount shells computed when kcount > 0, the rest zero)."""
     n_theta = n_theta or 2 * LMAX
     n_phi = n_phi or 4 * LMAX
     xg, wg = np.polynomial.legendre.leggauss(n_theta)
@@ -164,7 +165,7 @@ def intensity_coefficients(atoms: list, LMAX: int, KMAX: int, rmax: float, n_the
     dq = math.pi / rmax
     proj = dirs @ pos.T                                                           # [P, atoms]
     out = np.zeros((KMAX, LMAX * LMAX), dtype=np.complex128)
-    for k in range(1, KMAX + 1):
+    for k in range(1, (kcount or KMAX) + 1):
         q = k * dq
         f = RB[:, 1] * np.exp(-0.5 * RB[:, 0] ** 2 * q * q)
         amp = np.exp(1j * q * proj) @ f
