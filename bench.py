@@ -50,6 +50,7 @@ TRIPLETS = 1e9
 METRIC = "c3+Bayes proposal evals/s at L18 K26 N32"
 UNIT = "proposals/s"
 MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
+COUPLING_NAMES = {0: "fused_512", 1: "split", 2: "fused_256x2", 3: "warp_local"}
 DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
 
 
@@ -289,8 +290,8 @@ def run_ragged(args):
                                    "16..26, L in 12..18, N32, LMAX25) x 16 speculative candidates per CUDA-graph "
                                    "replay; one ragged tensor-core launch per step on the L18 K26 shape",
                        "Ks": Ks.tolist(), "Ls": Ls.tolist(), "mode": MODE_NAMES.get(basis.mode),
-                       "autotune": [{"mode": MODE_NAMES.get(m), "split_coupling": bool(sp), "ms_per_proposal": t}
-                                    for m, sp, t in tuning]},
+                       "autotune": [{"mode": MODE_NAMES.get(m), "coupling": COUPLING_NAMES.get(sp) if m else None,
+                                     "ms_per_proposal": t} for m, sp, t in tuning]},
             "chain_steps_per_s": float((s1["steps"] - s0["steps"]).sum()) / (ms / 1e3),
             # per replay: propose, gather, couple, angular + Bayes, finalize, select, commit
             "gpu_launches": 7 * reps}
@@ -344,6 +345,8 @@ def main():
     ap.add_argument("--mode", default="auto", choices=["auto", "tuned", "plain", "tc", "tf32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned"])
+    ap.add_argument("--coupling", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+                    help="force a tensor-core coupling form (with --mode tc/tf32)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chains", action="store_true")
     args = ap.parse_args()
@@ -371,10 +374,12 @@ def main():
     basis.set_histogram(hist)
     tuning = None
     if mode is None:
-        tuning = [{"mode": MODE_NAMES.get(m, str(m)), "split_coupling": bool(sp), "ms_per_proposal": ms}
-                  for m, sp, ms in basis.autotune(args.batch)]
+        tuning = [{"mode": MODE_NAMES.get(m, str(m)), "coupling": COUPLING_NAMES.get(sp) if m else None,
+                   "ms_per_proposal": ms} for m, sp, ms in basis.autotune(args.batch)]
     else:
         basis.set_mode(mode)
+        if args.coupling >= 0:
+            basis.set_coupling(args.coupling)
     mode_used = basis.mode
     B = args.batch
     basis.reserve(B)

@@ -153,3 +153,31 @@ def test_errors_are_statuses(config1):
     b.close()
     with pytest.raises(tp3.TP3Error):
         tp3.calculate_basis(8, 8, 16, 8)  # LMAX must exceed L
+
+
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
+@pytest.mark.parametrize("kind", ["general", "real_function"])
+def test_coupling_forms_agree(basis1, config1, config1_hist, form, kind):
+    """Every coupling form the autotuner may pick (one-kernel 512 threads, split, one-kernel
+    256 threads x 2 CTAs per SM, warp-local) gives the oracle's triple products and the
+    same energy."""
+    basis1.set_mode(tp3.TP3_MODE_TC_BF16X3)
+    basis1.set_coupling(form)
+    p = config1["params"]
+    LMAX = p["LMAX"]
+    rng = np.random.default_rng(form + 7)
+    c = rng.normal(size=(p["K"], LMAX * LMAX)) + 1j * rng.normal(size=(p["K"], LMAX * LMAX))
+    if kind == "real_function":
+        from tp3.structure import seanindex0
+        for l in range(LMAX):
+            c[:, seanindex0(l, 0, LMAX)] = c[:, seanindex0(l, 0, LMAX)].real
+            for m in range(1, l + 1):
+                c[:, seanindex0(l, -m, LMAX)] = (-1) ** m * np.conj(c[:, seanindex0(l, m, LMAX)])
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    T64 = triple_products(b, c)
+    T = basis1.triple_products(c).astype(np.float64)
+    assert np.max(np.abs(T - T64)) / np.abs(T64).max() < 2e-5
+    basis1.set_histogram(config1_hist)
+    E = basis1.energy_batch(config1["coeff"][None, : p["K"]])[0]
+    assert E == pytest.approx(float(config1["E_fp64"]), rel=1e-6)
+    basis1.set_coupling(0)

@@ -213,6 +213,28 @@ std::string setup_tc(tp3_ctx* c) {
   tc.nchunks = (int)chunks.size();
   tc.nchunks_sym = (int)chunks_sym.size();
   if (tc.nchunks_sym > 64 || tc.nchunks > 64) tc.fused_ok = false;
+  // the small tiling (256 threads, two CTAs per SM)
+  const size_t limit_s = tp3::kCoupleSmallSmem;
+  int pmax_s = std::max(b.K, 128);
+  tc.w_smem_s = true;
+  while (need(pmax_s, true) > limit_s && pmax_s > b.K) --pmax_s;
+  if (need(pmax_s, true) > limit_s) { tc.w_smem_s = false; pmax_s = std::max(b.K, 128); }
+  while (need(pmax_s, false) > limit_s && pmax_s > b.K) --pmax_s;
+  tc.small_ok = need(pmax_s, tc.w_smem_s) <= limit_s;
+  tc.pmax_s = pmax_s;
+  tc.couple_smem_s = need(pmax_s, tc.w_smem_s);
+  tc.pmax_sym_s = (int)((2 * (size_t)pmax_s * tc.SDp) / (2 * (size_t)tc.SDhp));
+  std::vector<int2> chunks_s = make_chunks(pmax_s), chunks_sym_s = make_chunks(tc.pmax_sym_s);
+  tc.nchunks_s = (int)chunks_s.size();
+  tc.nchunks_sym_s = (int)chunks_sym_s.size();
+  if (tc.nchunks_s > 64 || tc.nchunks_sym_s > 64) tc.small_ok = false;
+  // the warp-local coupling: 16 warps x 4 shell pairs of D (general rows, SDp)
+  {
+    const size_t dw = (size_t)16 * 4 * tc.SDp * sizeof(float2);
+    tc.w_smem_w = base + (size_t)wmax * 4 + dw <= limit;
+    tc.couple_smem_w = base + (tc.w_smem_w ? (size_t)wmax * 4 : 0) + dw;
+    tc.warp_ok = tc.couple_smem_w <= limit && b.K <= 64;
+  }
   // split coupling: D offsets, L2-sized sub-batches, balanced (pair block, m3 range) units
   const int npairs = b.K * (b.K + 1) / 2;
   std::vector<long long> doff(pbs.size());
@@ -320,7 +342,9 @@ std::string setup_tc(tp3_ctx* c) {
   cudaError_t e;
   if ((e = upload(c, b.coff, &tc.coff)) != cudaSuccess || (e = upload(c, pbs, &tc.pbs)) != cudaSuccess ||
       (e = upload(c, eofs, &tc.eofs)) != cudaSuccess || (e = upload(c, wtab, &tc.wtab)) != cudaSuccess ||
-      (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, chunks_sym, &tc.chunks_sym)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
+      (e = upload(c, chunks, &tc.chunks)) != cudaSuccess || (e = upload(c, chunks_sym, &tc.chunks_sym)) != cudaSuccess ||
+      (e = upload(c, chunks_s, &tc.chunks_s)) != cudaSuccess ||
+      (e = upload(c, chunks_sym_s, &tc.chunks_sym_s)) != cudaSuccess || (e = upload(c, b.c_m, &tc.cm)) != cudaSuccess ||
       (e = upload(c, b.c_l, &tc.cl)) != cudaSuccess ||
       (e = upload(c, cmir, &tc.cmir)) != cudaSuccess || (e = upload(c, doff, &tc.doff)) != cudaSuccess ||
       (e = upload(c, units_sym, &tc.units_sym)) != cudaSuccess ||
@@ -513,6 +537,16 @@ int check_ctx(tp3_ctx* c) {
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
   return TP3_OK;
+}
+
+// Coupling form of the tensor-core path: 0 one-kernel, 1 split, 2 one-kernel small
+// tiling; a form this shape cannot run falls back to one that it can.
+void apply_coupling(tp3_ctx* c, int form) {
+  TcTables& tc = c->tc;
+  tc.use_small = form == 2 && tc.small_ok;
+  tc.use_warp = form == 3 && tc.warp_ok;
+  tc.split = (form == 1 && tc.split_ok) || (!tc.fused_ok && !tc.use_warp);
+  if (tc.split) tc.use_small = tc.use_warp = false;
 }
 
 // Folded, slab-normalised histogram of Kh shells (slabs with k1 < Kh; the rest zero)
@@ -800,7 +834,7 @@ int tp3_set_mode(tp3_ctx* c, int mode) {
     }
     if (te.mode >= 0 && (te.mode == TP3_MODE_PLAIN_FP32 || c->tc_ok)) {
       c->mode = te.mode;
-      if (c->tc_ok) c->tc.split = te.split ? c->tc.split_ok : !c->tc.fused_ok;
+      if (c->tc_ok) apply_coupling(c, te.split);
       return TP3_OK;
     }
     mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
@@ -817,10 +851,14 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   if (!c->has_hist) return fail(c, TP3_ERR_NO_HISTOGRAM, "autotune scores proposals: set a histogram first");
   const Basis& b = c->b;
   // variants: the plain path, and each tensor-core mode with each coupling form it can run
+  // coupling forms: 0 one-kernel (512 threads, one CTA per SM), 1 two-kernel split,
+  // 2 one-kernel small tiling (256 threads, two CTAs per SM)
   std::vector<std::pair<int, int>> vars = {{TP3_MODE_PLAIN_FP32, 0}};
   if (c->tc_ok)
     for (int m : {TP3_MODE_TC_BF16X3, TP3_MODE_TC_TF32X3}) {
       if (c->tc.fused_ok) vars.push_back({m, 0});
+      if (c->tc.small_ok) vars.push_back({m, 2});
+      if (c->tc.warp_ok) vars.push_back({m, 3});
       if (c->tc.split_ok) vars.push_back({m, 1});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
@@ -858,6 +896,8 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   }
   const int mode0 = c->mode;
   const bool split0 = c->tc_ok ? c->tc.split : false;
+  const bool small0 = c->tc_ok ? c->tc.use_small : false;
+  const bool warp0 = c->tc_ok ? c->tc.use_warp : false;
   const bool prof0 = c->prof;
   c->prof = false;
   int best = -1, rc = TP3_OK;
@@ -865,7 +905,7 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   std::vector<double> ms(vars.size(), -1.0);
   for (size_t v = 0; v < vars.size() && rc == TP3_OK; ++v) {
     c->mode = vars[v].first;
-    if (c->tc_ok) c->tc.split = vars[v].second != 0;
+    if (c->tc_ok) apply_coupling(c, vars[v].second);
     if ((rc = ensure_cap(c, n)) != TP3_OK) break;
     if ((rc = run_energy(c, n, d_c, d_e)) != TP3_OK) break;  // warm-up
     double mn = 1e300;
@@ -888,11 +928,11 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   c->prof = prof0;
   if (rc != TP3_OK || best < 0) {
     c->mode = mode0;
-    if (c->tc_ok) c->tc.split = split0;
+    if (c->tc_ok) { c->tc.split = split0; c->tc.use_small = small0; c->tc.use_warp = warp0; }
     return rc != TP3_OK ? rc : fail(c, TP3_ERR_UNSUPPORTED, "no variant ran");
   }
   c->mode = vars[best].first;
-  if (c->tc_ok) c->tc.split = vars[best].second != 0 ? true : !c->tc.fused_ok;
+  if (c->tc_ok) apply_coupling(c, vars[best].first == TP3_MODE_PLAIN_FP32 ? 0 : vars[best].second);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     TuneEntry te;
@@ -912,6 +952,16 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
     }
     *nreport = (int)vars.size();
   }
+  return TP3_OK;
+}
+
+int tp3_set_coupling(tp3_ctx* c, int form) {
+  if (int r = check_ctx(c)) return r;
+  if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
+  const bool ok = (form == 0 && c->tc.fused_ok) || (form == 1 && c->tc.split_ok) || (form == 2 && c->tc.small_ok) ||
+                  (form == 3 && c->tc.warp_ok);
+  if (!ok) return fail(c, form < 0 || form > 3 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
+  apply_coupling(c, form);
   return TP3_OK;
 }
 

@@ -72,6 +72,21 @@ struct TcTables {
   const int2* chunks = nullptr;  // (k1 high, k1 low) runs of shells, pairs per run <= pmax
   const int2* chunks_sym = nullptr;  // same for the real-function path (rows of SDhp)
   int nchunks_sym = 0, pmax_sym = 0, SDhp = 0;
+  // second tiling of the one-kernel coupling: 256 threads and at most kCoupleSmallSmem
+  // bytes of shared memory per CTA, so two CTAs share an SM (one computes while the
+  // other waits at its chunk barrier)
+  bool small_ok = false;
+  bool use_small = false;
+  bool w_smem_s = false;
+  size_t couple_smem_s = 0;
+  const int2* chunks_s = nullptr;
+  const int2* chunks_sym_s = nullptr;
+  int nchunks_s = 0, nchunks_sym_s = 0, pmax_s = 0, pmax_sym_s = 0;
+  // warp-local one-kernel coupling (k_couple_warp): per-warp D buffers of 4 shell pairs
+  bool warp_ok = false;
+  bool use_warp = false;
+  bool w_smem_w = false;
+  size_t couple_smem_w = 0;
   // split coupling (kernels_couple.cu)
   bool split = false;            // use the two-kernel coupling
   bool split_ok = false;         // the two-kernel coupling fits this shape
@@ -115,6 +130,7 @@ size_t tc_smem_bytes();
 // Dynamic shared memory the coupling kernel may request (the opt-in maximum of
 // 227 KB minus its static counters and slack).
 constexpr int kCoupleMaxDynSmem = 227 * 1024 - 2048;
+constexpr int kCoupleSmallSmem = 110 * 1024;
 cudaError_t tc_configure();
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
                               float2* cc, int* sym, cudaStream_t s, const RagInfo* rag = nullptr);

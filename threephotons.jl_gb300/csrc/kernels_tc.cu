@@ -127,8 +127,8 @@ __global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, co
 // grid: (n_pb, n); block kCoupleThreads.
 constexpr int kCoupleThreads = 512;
 
-template <int MAXS, bool W_SMEM>
-__global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
+template <int MAXS, bool W_SMEM, int THREADS>
+__global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_pair(
     const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
     const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab,
     const int2* __restrict__ chunks_gen, int nchunks_gen, int pmax_gen, int SDp,
@@ -318,6 +318,189 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_pair(
         }
       }
     }
+  }
+}
+
+
+// Warp-local form of the pair coupling (no CTA barrier after the loads).  One CTA =
+// one (l1, l2) pair block of one proposal; its warps take work units from a shared
+// counter.  A unit is one shell k1 and a quad of k2 (k2 = 4q .. 4q+3, <= k1): the warp
+// forms D for those (up to) four shell pairs and every m3 / l3 in its own shared-memory
+// buffer (phase 1: lanes own (m3, pair) items, so lanes with one m3 read the same 3j row),
+// then contracts D with every k3-quad <= q (phase 2: lanes own (l3, k3-quad) items and
+// read the unit's D rows as broadcasts).  Both phases synchronise only the warp.
+// grid: (n_pb, n); block kCoupleThreads.
+template <int MAXS, bool W_SMEM>
+__global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_warp(
+    const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
+    const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab, int SDp,
+    int SDhp, int wsmem, int klp, int KP, const int* __restrict__ symflags, void* __restrict__ Thi,
+    void* __restrict__ Tlo, bool tf32out, float* __restrict__ T32, int ldT32, const RagInfo* __restrict__ rag) {
+  extern __shared__ __align__(16) float smf[];
+  __shared__ int s_next, s_total;
+  __shared__ int s_ustart[64];  // first unit index of each k1 (units ordered by k1 descending)
+  const int prop = blockIdx.y;
+  int Kp = K;
+  const PairBlock pb = pbs[blockIdx.x];
+  if (rag) {
+    const RagInfo ri = rag[prop];
+    Kp = ri.K;
+    if (pb.l1 > ri.L || pb.l2 > ri.L) {
+      for (int i = threadIdx.x; i < ri.klen * pb.nl3; i += blockDim.x) {
+        const int ki = i / pb.nl3, sj = i - ki * pb.nl3;
+        store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + pb.lt_base + sj, 0.f, tf32out);
+        if (T32) T32[((size_t)prop * klp + ki) * ldT32 + pb.lt_base + sj] = 0.f;
+      }
+      return;
+    }
+  }
+  const bool sym = symflags[prop] != 0;
+  const int rowD = sym ? SDhp : SDp;
+  float2* sc = reinterpret_cast<float2*>(smf);                  // [K][ncp]
+  float* sw = smf + (2 * (size_t)K * ncp + 3) / 4 * 4;           // [wsmem]
+  float2* sD = reinterpret_cast<float2*>(sw + (W_SMEM ? wsmem : 0));  // [warps][4][rowD]
+  const float2* src = cc + (size_t)prop * K * nc;
+  for (int i = threadIdx.x; i < Kp * nc; i += blockDim.x) {
+    const int k = i / nc, c = i - k * nc;
+    sc[k * ncp + c] = src[i];
+  }
+  const float* wblk = wtab + pb.wofs;
+  if (W_SMEM) {
+    const float4* w4 = reinterpret_cast<const float4*>(wblk);
+    float4* s4 = reinterpret_cast<float4*>(sw);
+    for (int i = threadIdx.x; i < pb.wcount / 4; i += blockDim.x) s4[i] = w4[i];
+  }
+  if (threadIdx.x == 0) {
+    int u = 0;
+    for (int k1 = Kp - 1; k1 >= 0; --k1) {
+      s_ustart[k1] = u;
+      u += (k1 + 4) >> 2;
+    }
+    s_total = u;
+    s_next = 0;
+  }
+  __syncthreads();
+  const float* wsrc = W_SMEM ? sw : wblk;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float2* Dw = sD + (size_t)warp * 4 * rowD;
+  const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, nl3p = pb.nl3p, l3min = pb.l3min, M = pb.M;
+  const int off1 = coff[l1 >> 1] + l1, off2 = coff[l2 >> 1] + l2;
+  const int nm3 = sym ? M + 1 : 2 * M + 1;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&s_next, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= s_total) break;
+    // decode unit u (k1 descending, then q ascending)
+    int k1 = Kp - 1;
+    while (k1 > 0 && s_ustart[k1 - 1] <= u) --k1;
+    const int q = u - s_ustart[k1];
+    const int np = min(4, k1 - 4 * q + 1);
+    // ---- phase 1: D[i][l3][m3] for the unit's pairs (k1, 4q + i) ----
+    const int nI = nm3 * np;
+    for (int it = lane; it < nI; it += 32) {
+      const int eo = it / np, i = it - eo * np;
+      const int m3 = sym ? eo : ((eo & 1) ? -((eo + 1) >> 1) : (eo >> 1));
+      const int e = m3 + M;
+      const int k2 = 4 * q + i;
+      const int m1lo = max(-l1, -l2 - m3), m1hi = min(l1, l2 - m3);
+      const float* wp = wsrc + eofs[pb.eofs + e];
+      const float2* c1 = sc + k1 * ncp + off1;
+      const float2* c2 = sc + k2 * ncp + off2 - m3;
+      float ar[MAXS], ai[MAXS];
+#pragma unroll
+      for (int s = 0; s < MAXS; ++s) { ar[s] = 0.f; ai[s] = 0.f; }
+      for (int m1 = m1lo; m1 <= m1hi; ++m1) {
+        const float2 a = c1[m1];
+        const float2 b = c2[-m1];
+        const float xr = a.x * b.x - a.y * b.y;
+        const float xi = a.x * b.y + a.y * b.x;
+        const float2* wr = reinterpret_cast<const float2*>(wp + (m1 - m1lo) * nl3p);
+#pragma unroll
+        for (int s2 = 0; s2 < (MAXS + 1) / 2; ++s2) {
+          if (2 * s2 < nl3) {
+            const float2 wv = wr[s2];
+            ar[2 * s2] = fmaf(wv.x, xr, ar[2 * s2]);
+            ai[2 * s2] = fmaf(wv.x, xi, ai[2 * s2]);
+            if (2 * s2 + 1 < MAXS) {
+              ar[2 * s2 + 1] = fmaf(wv.y, xr, ar[2 * s2 + 1]);
+              ai[2 * s2 + 1] = fmaf(wv.y, xi, ai[2 * s2 + 1]);
+            }
+          }
+        }
+      }
+      float2* d = Dw + (size_t)i * rowD;
+      int dofs = 0;
+#pragma unroll
+      for (int s = 0; s < MAXS; ++s) {
+        if (s < nl3) {
+          const int l3 = l3min + 2 * s;
+          if (sym) {
+            if (m3 <= l3) d[dofs + m3] = make_float2(ar[s], ai[s]);
+            dofs += l3 + 1;
+          } else {
+            if (m3 >= -l3 && m3 <= l3) d[dofs + m3 + l3] = make_float2(ar[s], ai[s]);
+            dofs += 2 * l3 + 1;
+          }
+        }
+      }
+    }
+    __syncwarp();
+    // ---- phase 2: T for (k1, k2 in the quad, k3-quad rb <= q, l3) ----
+    const int nI2 = nl3 * (q + 1);
+    for (int it = lane; it < nI2; it += 32) {
+      const int s = nl3 - 1 - it / (q + 1);  // largest l3 first
+      const int rb = it % (q + 1);
+      const int l3 = l3min + 2 * s;
+      const int dofs = sym ? s * (l3min + s) : s * (2 * l3min + 2 * s - 1) + l3min + 2 * s;
+      const int off3 = coff[l3 >> 1] + l3;
+      const float2* drow[4];
+      const float2* crow[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        drow[i] = Dw + (size_t)min(i, np - 1) * rowD + dofs;
+        crow[i] = sc + min(4 * rb + i, k1) * ncp + off3;
+      }
+      float acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+      for (int m3 = sym ? 1 : -l3; m3 <= l3; ++m3) {
+        float2 x[4], y[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { x[i] = drow[i][m3]; y[i] = crow[i][m3]; }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, acc[i][j]));
+      }
+      if (sym) {
+        float2 x[4], y[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { x[i] = drow[i][0]; y[i] = crow[i][0]; }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, 2.f * acc[i][j]));
+      }
+      const int lt = pb.lt_base + s;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k2 = 4 * q + i;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k3 = 4 * rb + j;
+          if (k2 <= k1 && k3 <= k2) {
+            const int ki = ki_index(k1, k2, k3);
+            const float v = acc[i][j];
+            store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + lt, v, tf32out);
+            if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
+          }
+        }
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -593,15 +776,25 @@ cudaError_t tc_configure() {
       (e = cudaFuncSetAttribute(k_angular_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
           cudaSuccess)
     return e;
-  const int cs = kCoupleMaxDynSmem;
-#define TP3_CP_ATTR(S, W)                                                                              \
-  if ((e = cudaFuncSetAttribute(k_couple_pair<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
-      cudaSuccess)                                                                                     \
+  const int cs = kCoupleMaxDynSmem, css = kCoupleSmallSmem;
+#define TP3_CP_ATTR(S, W)                                                                                    \
+  if ((e = cudaFuncSetAttribute(k_couple_pair<S, W, kCoupleThreads>,                                         \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||          \
+      (e = cudaFuncSetAttribute(k_couple_pair<S, W, kCoupleThreads / 2>,                                     \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, css)) != cudaSuccess)           \
     return e;
   TP3_CP_ATTR(4, true) TP3_CP_ATTR(8, true) TP3_CP_ATTR(10, true) TP3_CP_ATTR(12, true) TP3_CP_ATTR(16, true)
   TP3_CP_ATTR(4, false) TP3_CP_ATTR(8, false) TP3_CP_ATTR(10, false) TP3_CP_ATTR(12, false)
   TP3_CP_ATTR(16, false)
 #undef TP3_CP_ATTR
+#define TP3_CW_ATTR(S, W)                                                                               \
+  if ((e = cudaFuncSetAttribute(k_couple_warp<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
+      cudaSuccess)                                                                                      \
+    return e;
+  TP3_CW_ATTR(4, true) TP3_CW_ATTR(8, true) TP3_CW_ATTR(10, true) TP3_CW_ATTR(12, true) TP3_CW_ATTR(16, true)
+  TP3_CW_ATTR(4, false) TP3_CW_ATTR(8, false) TP3_CW_ATTR(10, false) TP3_CW_ATTR(12, false)
+  TP3_CW_ATTR(16, false)
+#undef TP3_CW_ATTR
   return cudaSuccess;
 }
 
@@ -614,25 +807,59 @@ cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, con
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s, const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
-  const size_t smem = tc.couple_smem;
-#define TP3_CP_LAUNCH(S, W)                                                                                \
-  k_couple_pair<S, W><<<grid, kCoupleThreads, smem, s>>>(                                                  \
-      cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.chunks, tc.nchunks, tc.pmax, tc.SDp,         \
-      tc.chunks_sym, tc.nchunks_sym, tc.pmax_sym, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, tf32, T32, t.n_ltp, \
-      rag)
-  if (tc.w_smem) {
-    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true);
-    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true);
-    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, true);
-    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, true);
-    else TP3_CP_LAUNCH(16, true);
-  } else {
-    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, false);
-    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, false);
-    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, false);
-    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, false);
-    else TP3_CP_LAUNCH(16, false);
+  if (tc.use_warp && tc.warp_ok) {
+#define TP3_CW_LAUNCH(S, W)                                                                                 \
+  k_couple_warp<S, W><<<grid, kCoupleThreads, tc.couple_smem_w, s>>>(cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs,  \
+                                                                     tc.eofs, tc.wtab, tc.SDp, tc.SDhp, tc.wsmem, \
+                                                                     t.klp, tc.KP, sym, Thi, Tlo, tf32, T32,      \
+                                                                     t.n_ltp, rag)
+    if (tc.w_smem_w) {
+      if (tc.maxs <= 4) TP3_CW_LAUNCH(4, true);
+      else if (tc.maxs <= 8) TP3_CW_LAUNCH(8, true);
+      else if (tc.maxs <= 10) TP3_CW_LAUNCH(10, true);
+      else if (tc.maxs <= 12) TP3_CW_LAUNCH(12, true);
+      else TP3_CW_LAUNCH(16, true);
+    } else {
+      if (tc.maxs <= 4) TP3_CW_LAUNCH(4, false);
+      else if (tc.maxs <= 8) TP3_CW_LAUNCH(8, false);
+      else if (tc.maxs <= 10) TP3_CW_LAUNCH(10, false);
+      else if (tc.maxs <= 12) TP3_CW_LAUNCH(12, false);
+      else TP3_CW_LAUNCH(16, false);
+    }
+#undef TP3_CW_LAUNCH
+    return cudaGetLastError();
   }
+  const bool sm = tc.use_small && tc.small_ok;
+  const size_t smem = sm ? tc.couple_smem_s : tc.couple_smem;
+  const bool wsm = sm ? tc.w_smem_s : tc.w_smem;
+  const int2* ch = sm ? tc.chunks_s : tc.chunks;
+  const int2* chs = sm ? tc.chunks_sym_s : tc.chunks_sym;
+  const int nch = sm ? tc.nchunks_s : tc.nchunks, nchs = sm ? tc.nchunks_sym_s : tc.nchunks_sym;
+  const int pm = sm ? tc.pmax_s : tc.pmax, pms = sm ? tc.pmax_sym_s : tc.pmax_sym;
+#define TP3_CP_LAUNCH(S, W, TH)                                                                            \
+  k_couple_pair<S, W, TH><<<grid, TH, smem, s>>>(                                                          \
+      cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, ch, nch, pm, tc.SDp, chs, nchs, pms, tc.SDhp, \
+      tc.wsmem, t.klp, tc.KP, sym, Thi, Tlo, tf32, T32, t.n_ltp, rag)
+#define TP3_CP_PICK(TH)                                        \
+  if (wsm) {                                                   \
+    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, true, TH);              \
+    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, true, TH);         \
+    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, true, TH);       \
+    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, true, TH);       \
+    else TP3_CP_LAUNCH(16, true, TH);                          \
+  } else {                                                     \
+    if (tc.maxs <= 4) TP3_CP_LAUNCH(4, false, TH);             \
+    else if (tc.maxs <= 8) TP3_CP_LAUNCH(8, false, TH);        \
+    else if (tc.maxs <= 10) TP3_CP_LAUNCH(10, false, TH);      \
+    else if (tc.maxs <= 12) TP3_CP_LAUNCH(12, false, TH);      \
+    else TP3_CP_LAUNCH(16, false, TH);                         \
+  }
+  if (sm) {
+    TP3_CP_PICK(kCoupleThreads / 2)
+  } else {
+    TP3_CP_PICK(kCoupleThreads)
+  }
+#undef TP3_CP_PICK
 #undef TP3_CP_LAUNCH
   return cudaGetLastError();
 }

@@ -50,6 +50,7 @@ SIGNATURES = {
     "tp3_get_mode": (c_int, [c_void_p, P(c_int)]),
     "tp3_reserve": (c_int, [c_void_p, c_int]),
     "tp3_autotune": (c_int, [c_void_p, c_int, c_void_p, P(c_int)]),
+    "tp3_set_coupling": (c_int, [c_void_p, c_int]),
     "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),
     "tp3_c3": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tp3_c3_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
