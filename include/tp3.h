@@ -261,6 +261,36 @@ int tp3_chains_graph(const tp3_chains* chains, int* captured);
  * the arguments return at once (detail in tp3_last_error(NULL)). */
 int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, int K, int N, double* d_E, void* stream);
 
+/* ---- triplet histograms of photon pictures (src/datagen.jl:228-277) ---------- */
+/* histogramCorrelationsInPicture_alltoall for n pictures at once: picture p holds the
+ * photons d_photons[d_offsets[p] .. d_offsets[p+1]) (device, (x, y) detector doubles,
+ * the reference's photon vectors with z = 0; d_offsets int64, device).  Adds EXACT
+ * entry counts to the device histograms (unsigned 64-bit, the reference's Julia
+ * layouts, column-major): c1[K2], c2[N, K2, K2] (ai, k2, k1), c3[N, 2N, K3, K3, K3]
+ * (ai, bi, k3, k2, k1).  The reference's weighted histograms are count / k1,
+ * count / (doubletFactor k1 k2), count / (tripletFactor k1 k2 k3).  At most 1536
+ * photons per picture survive the k filter; a larger picture is skipped and reported
+ * as TP3_ERR_ARG by the next synchronising call.  Asynchronous on the context stream. */
+int tp3_histogram_pictures(tp3_ctx* ctx, int n_pictures, const void* d_photons, const int64_t* d_offsets, double dq,
+                           int N, int K2, int K3, unsigned long long* d_c1, unsigned long long* d_c2,
+                           unsigned long long* d_c3);
+/* pointsPerOrientation (src/datagen.jl:88-144) for pictures first_picture ..
+ * first_picture + n_pictures - 1 of an intensity given by SH coefficients d_coeff
+ * (KMAX x LMAX^2 complex128, seanindex order, shell k at |q| = k dq, linear in |q|
+ * between shells): a Haar-random orientation per picture, incident_photons Gaussian
+ * detector photons of width envelope_sigma, those with |p| <= qcut mapped to the Ewald
+ * sphere (wavelength lambda) and kept with probability
+ * I(R e(p)) exp(|e(p)|^2 / (2 sigma^2)) / max_intensity.  Accepted (x, y) go to
+ * d_photons[p][0 .. d_counts[p]) (n_pictures x max_out double pairs, device).
+ * Philox4x32-10 streams keyed by seed (independent of how pictures are batched). */
+int tp3_sample_pictures(tp3_ctx* ctx, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX, int LMAX,
+                        double dq, double qcut, double envelope_sigma, int incident_photons, double lambda,
+                        double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts);
+/* Largest intensity on the shells x (n_theta x n_phi) grid (the maximum the
+ * rejection sampling is normalised by).  Synchronises. */
+int tp3_intensity_max(tp3_ctx* ctx, const void* d_coeff, int KMAX, int LMAX, double dq, int n_theta, int n_phi,
+                      double* out);
+
 /* ---- Wigner-D rotations (src/spherical_harmonics.jl:572-603) --------------- */
 /* rotationMatrix(theta, phi, gamma, l) of src/spherical_harmonics.jl:590-592:
  * D[m, s] = exp(-i s gamma - i m phi) d^l_{ms}(theta), m, s = -l..l, written
