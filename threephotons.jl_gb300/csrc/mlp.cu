@@ -50,6 +50,7 @@ struct GemmArgs {
   int ldt;
   float* out_f32;               // [M][ldf]
   int ldf;
+  int ksplit;                   // > 1: grid.z splits K; out_f32 accumulated with atomics (pre-zeroed)
   int* err;
 };
 
@@ -77,7 +78,11 @@ __global__ void __launch_bounds__(kGThreads, 1) k_gemm_tn(const __grid_constant_
   GemmSmemHeader* hd = (GemmSmemHeader*)(base + kGStages * kStage);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kGBM, n0 = blockIdx.y * BN;
-  const int nk = (g.K + kGBK - 1) / kGBK;
+  const int nk_all = (g.K + kGBK - 1) / kGBK;
+  // split K: this CTA reduces k-blocks [kb0, kb0 + nk)
+  const int ks = g.ksplit > 1 ? g.ksplit : 1;
+  const int kb0 = (int)(((long long)nk_all * blockIdx.z) / ks);
+  const int nk = (int)(((long long)nk_all * (blockIdx.z + 1)) / ks) - kb0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kGStages; ++s) {
       mbar_init(&hd->full[s], 1);
@@ -111,8 +116,8 @@ __global__ void __launch_bounds__(kGThreads, 1) k_gemm_tn(const __grid_constant_
         last[s] = kc;
         uint8_t* st = base + s * kStage;
         mbar_expect_tx(&hd->full[s], kStage);
-        tma_load_2d(st, &tmA, &hd->full[s], kc * kGBK, m0);
-        tma_load_2d(st + kGABytes, &tmB, &hd->full[s], kc * kGBK, n0);
+        tma_load_2d(st, &tmA, &hd->full[s], (kb0 + kc) * kGBK, m0);
+        tma_load_2d(st + kGABytes, &tmB, &hd->full[s], (kb0 + kc) * kGBK, n0);
       }
       if (*abort_flag) {
         for (int s = 0; s < kGStages; ++s) {
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(kGThreads, 1) k_gemm_tn(const __grid_constant_
     const int q = warp & 3;  // TMEM lane quarter this warp may read
     const int r = q * 32 + lane;
     const int m = m0 + r;
-    if (mbar_wait(&hd->tmem_full, 0u, abort_flag, g.err)) {
+    if (nk > 0 && mbar_wait(&hd->tmem_full, 0u, abort_flag, g.err)) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int c = 0; c < (BN + 31) / 32; ++c) {
         float v[32];
@@ -160,7 +165,10 @@ __global__ void __launch_bounds__(kGThreads, 1) k_gemm_tn(const __grid_constant_
             if (g.bias) x += g.bias[n];
             if (g.relu) x = fmaxf(x, 0.f);
             if (g.gate && !(__bfloat162float(g.gate[(size_t)m * g.ldg + n]) > 0.f)) x = 0.f;
-            if (g.out_f32) g.out_f32[(size_t)m * g.ldf + n] = x;
+            if (g.out_f32) {
+              if (ks > 1) atomicAdd(&g.out_f32[(size_t)m * g.ldf + n], x);
+              else g.out_f32[(size_t)m * g.ldf + n] = x;
+            }
             const __nv_bfloat16 xb = __float2bfloat16_rn(x);
             if (g.out_bf) g.out_bf[(size_t)m * g.ldo + n] = xb;
             if (g.outT_bf) g.outT_bf[(size_t)n * g.ldt + m] = xb;
@@ -340,6 +348,8 @@ cudaError_t gemm(tp3_mlp* net, const CUtensorMap& A, const CUtensorMap& B, GemmA
   const int bn = pick_bn(g.N);
   g.err = net->d_err;
   dim3 grid((g.M + kGBM - 1) / kGBM, (g.N + bn - 1) / bn);
+  if (g.ksplit < 1) g.ksplit = 1;
+  grid.z = g.ksplit;
   cudaStream_t s = net->ctx->stream;
   if (bn == 16) k_gemm_tn<16><<<grid, kGThreads, gemm_smem_bytes<16>(), s>>>(A, B, g);
   else if (bn == 128) k_gemm_tn<128><<<grid, kGThreads, gemm_smem_bytes<128>(), s>>>(A, B, g);
@@ -406,9 +416,19 @@ cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w) {
   float* gW[4];
   float* gb[4];
   for (int l = 0; l < 4; ++l) { gW[l] = n->d_grad + n->off_W[l]; gb[l] = n->d_grad + n->off_b[l]; }
+  // weight gradients reduce over the R rows: split K so that about two CTAs per SM work
+  if ((e = cudaMemsetAsync(n->d_grad, 0, n->n_par * sizeof(float), s)) != cudaSuccess) return e;
+  auto split = [&](int M, int N) {
+    const int tiles = ((M + kGBM - 1) / kGBM) * ((N + pick_bn(N) - 1) / pick_bn(N));
+    const int nk = (R + kGBK - 1) / kGBK;
+    int k = 304 / tiles;
+    k = k < 1 ? 1 : k;
+    k = k > nk / 4 ? (nk / 4 > 0 ? nk / 4 : 1) : k;
+    return k;
+  };
   // B1: dW4 = dO^T H3  [6 x H]
   GemmArgs g = args(kMlpOut, H, R);
-  g.out_f32 = gW[3]; g.ldf = H;
+  g.out_f32 = gW[3]; g.ldf = H; g.ksplit = split(kMlpOut, H);
   if ((e = gemm(n, n->bA[0], n->bB[0], g)) != cudaSuccess) return e;
   k_rowsum_bf16<<<kMlpOut, 256, 0, s>>>(n->dOt, MR, R, gb[3]);
   // B2: dZ3 = (dO W4) . [H3 > 0] -> P, Tt
@@ -417,7 +437,7 @@ cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w) {
   if ((e = gemm(n, n->bA[1], n->bB[1], g)) != cudaSuccess) return e;
   // B3: dW3 = dZ3^T H2
   g = args(H, H, R);
-  g.out_f32 = gW[2]; g.ldf = H;
+  g.out_f32 = gW[2]; g.ldf = H; g.ksplit = split(H, H);
   if ((e = gemm(n, n->bA[2], n->bB[2], g)) != cudaSuccess) return e;
   k_rowsum_bf16<<<H, 256, 0, s>>>(n->Tt, MR, R, gb[2]);
   // B4: dZ2 = (dZ3 W3) . [H2 > 0] -> Q, Tt
@@ -426,7 +446,7 @@ cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w) {
   if ((e = gemm(n, n->bA[3], n->bB[3], g)) != cudaSuccess) return e;
   // B5: dW2 = dZ2^T H1
   g = args(H, H, R);
-  g.out_f32 = gW[1]; g.ldf = H;
+  g.out_f32 = gW[1]; g.ldf = H; g.ksplit = split(H, H);
   if ((e = gemm(n, n->bA[4], n->bB[4], g)) != cudaSuccess) return e;
   k_rowsum_bf16<<<H, 256, 0, s>>>(n->Tt, MR, R, gb[1]);
   // B6: dZ1^T = ((dZ2 W2) . [H1 > 0])^T -> Tt
@@ -435,7 +455,7 @@ cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w) {
   if ((e = gemm(n, n->bA[5], n->bB[5], g)) != cudaSuccess) return e;
   // B7: dW1 = dZ1^T X  [H x n_in]
   g = args(H, n->n_in, R);
-  g.out_f32 = gW[0]; g.ldf = n->n_in;
+  g.out_f32 = gW[0]; g.ldf = n->n_in; g.ksplit = split(H, n->n_in);
   if ((e = gemm(n, n->bA[6], n->bB[6], g)) != cudaSuccess) return e;
   k_rowsum_bf16<<<H, 256, 0, s>>>(n->Tt, MR, R, gb[0]);
   return cudaGetLastError();
