@@ -493,6 +493,23 @@ def main():
                        "note": "wall clock around graph replays incl. one final synchronise; proposals include "
                                "device-side move generation and the Metropolis update"}
         ch.close()
+        # the same chains on the plain FP32 path: seeded chains follow the same trajectory in
+        # both modes, so the time to a given energy scales with chain steps per second
+        if mode_used != tp3.TP3_MODE_PLAIN_FP32:
+            basis.set_mode(tp3.TP3_MODE_PLAIN_FP32)
+            chp = Chains(basis, np.repeat(base[None, :K], nch, axis=0), T0, math.pi / 4, 1.02, 0.99998, 12345,
+                         ncand=ncand)
+            chp.run(1)
+            q0 = chp.state()
+            t0 = time.perf_counter()
+            chp.run(2)
+            q1 = chp.state()
+            dtp = time.perf_counter() - t0
+            chp.close()
+            basis.set_mode(mode_used)
+            plain_steps = float((q1["steps"] - q0["steps"]).sum()) / dtp
+            chains_info["plain_fp32_chain_steps_per_s"] = plain_steps
+            chains_info["time_to_energy_speedup_vs_plain_fp32"] = chains_info["chain_steps_per_s"] / plain_steps
 
     kernels_per_step = 4
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

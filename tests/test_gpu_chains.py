@@ -120,3 +120,26 @@ def test_snapshot_restore_is_bit_exact(setup):
     with pytest.raises(tp3.TP3Error):
         ch.restore(blob[:-8])
     ch.close()
+
+
+@pytest.mark.parametrize("mode", [tp3.TP3_MODE_PLAIN_FP32, tp3.TP3_MODE_TC_BF16X3])
+def test_config1_protocol_1000_steps(setup, config1_hist, mode):
+    """The small determination case as run by the reference: one chain from the true
+    structure with every shell turned by a uniform random rotation, 1000
+    rotate_all_at_once steps with the Bayes measure; the GPU chain (FP32 evaluation)
+    follows the FP64 oracle chain's accept/reject sequence up to the first decision that
+    lies within the energy tolerance of a boundary."""
+    from tp3.learned import rotated_starts
+    basis, e64, coeff, T0, p = setup
+    basis.set_mode(mode)
+    start = rotated_starts(basis, coeff, 1, 2024)[0]
+    ch = Chains(basis, start[None], T0, math.pi / 4, 1.02, 0.99, SEED + 7, ncand=4, log_capacity=1100)
+    while ch.state()["steps"][0] < 1000:
+        ch.run(8)
+    rows = ch.log(0)[:1000]
+    _, _, _, _, ref = oc.run_chain(e64, start, p["L"], p["LMAX"], T0, math.pi / 4, 1.02, 0.99, SEED + 7, 0, 1000)
+    compared = _compare(rows, ref, ref[0][3], 0)
+    print(f"\n[config 1] mode {mode}: {compared} of 1000 steps follow the FP64 chain "
+          f"(accepted {int((ref[:compared, 1] != 0).sum())}); E {ref[0][3]:.4f} -> {ref[compared - 1][3]:.4f}")
+    assert compared >= 50   # disagreements before that would have failed inside _compare
+    ch.close()
