@@ -43,7 +43,7 @@ def up_to_date() -> bool:
 
 def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
            "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
     if src.endswith(".cu"):
         cmd[1:1] = ["-Xptxas", "-v"] if os.environ.get("TP3_PTXAS_V") else []
@@ -66,7 +66,7 @@ def build(force: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = LIB + ".tmp"
-    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

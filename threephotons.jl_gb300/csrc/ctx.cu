@@ -1167,9 +1167,10 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
   const Basis& b = c->b;
   const size_t ncoef = (size_t)t.LMAX * t.LMAX;
   // Only the even-l <= L block of each shell reaches the kernels: pack it on the host
-  // (3.3x fewer bytes at L=18, LMAX=25) in chunks, so packing chunk i+1 overlaps the
-  // copy and the kernels of chunk i.
-  const int nchunk = n >= 32 ? 4 : 1;
+  // (3.3x fewer bytes at L=18, LMAX=25) with all host threads, then one copy and one
+  // launch sequence for the whole batch; very large batches go in chunks so that packing
+  // chunk i+1 overlaps the copy and kernels of chunk i.
+  const int nchunk = n >= 1024 ? 4 : 1;
   const int per = (n + nchunk - 1) / nchunk;
   const double2* src = (const double2*)coeffs;
   double2* pin = (double2*)c->h_coeff;
@@ -1177,6 +1178,8 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
   cudaError_t e;
   for (int p0 = 0; p0 < n; p0 += per) {
     const int m = std::min(per, n - p0);
+    // host threads pack the proposals of a chunk (the previous chunk's kernels run meanwhile)
+#pragma omp parallel for schedule(static) if (m >= 8)
     for (int p = p0; p < p0 + m; ++p)
       for (int k = 0; k < t.K; ++k) {
         const double2* s = src + ((size_t)p * t.K + k) * ncoef;
