@@ -263,17 +263,19 @@ int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, int K, int 
 
 /* ---- triplet histograms of photon pictures (src/datagen.jl:228-277) ---------- */
 /* histogramCorrelationsInPicture_alltoall for n pictures at once: picture p holds the
- * photons d_photons[d_offsets[p] .. d_offsets[p+1]) (device, (x, y) detector doubles,
- * the reference's photon vectors with z = 0; d_offsets int64, device).  Adds EXACT
+ * photons d_photons[d_offsets[p] .. d_offsets[p+1]) (device, n_photons (x, y) detector
+ * doubles, the reference's photon vectors with z = 0; d_offsets int64, device; a
+ * picture whose range leaves [0, n_photons] is skipped and reported as TP3_ERR_ARG by
+ * the next synchronising call).  Adds EXACT
  * entry counts to the device histograms (unsigned 64-bit, the reference's Julia
  * layouts, column-major): c1[K2], c2[N, K2, K2] (ai, k2, k1), c3[N, 2N, K3, K3, K3]
  * (ai, bi, k3, k2, k1).  The reference's weighted histograms are count / k1,
  * count / (doubletFactor k1 k2), count / (tripletFactor k1 k2 k3).  At most 1536
  * photons per picture survive the k filter; a larger picture is skipped and reported
  * as TP3_ERR_ARG by the next synchronising call.  Asynchronous on the context stream. */
-int tp3_histogram_pictures(tp3_ctx* ctx, int n_pictures, const void* d_photons, const int64_t* d_offsets, double dq,
-                           int N, int K2, int K3, unsigned long long* d_c1, unsigned long long* d_c2,
-                           unsigned long long* d_c3);
+int tp3_histogram_pictures(tp3_ctx* ctx, int n_pictures, const void* d_photons, int64_t n_photons,
+                           const int64_t* d_offsets, double dq, int N, int K2, int K3, unsigned long long* d_c1,
+                           unsigned long long* d_c2, unsigned long long* d_c3);
 /* pointsPerOrientation (src/datagen.jl:88-144) for pictures first_picture ..
  * first_picture + n_pictures - 1 of an intensity given by SH coefficients d_coeff
  * (KMAX x LMAX^2 complex128, seanindex order, shell k at |q| = k dq, linear in |q|

@@ -114,3 +114,30 @@ def test_device_training_fits_a_state_dependent_step():
     assert l1 < l0 - 3.0, (l0, l1)
     assert math.isfinite(l1)
     basis.close()
+
+
+@pytest.mark.gpu
+def test_network_at_chain_batch_size():
+    """Forward and training step at the learned annealer's batch (64 chains x 16 candidates
+    x 26 shells = 26 624 rows, 370 features, 3 x 512): finite outputs, loss falls."""
+    import torch
+    n_in, H, R = 370, 512, 26624
+    rng = np.random.default_rng(9)
+    basis, net = _net(n_in, H, R)
+    X = np.zeros((R, net.stride), dtype=np.float32)
+    X[:, :n_in] = rng.normal(size=(R, n_in)).astype(np.float32) * 0.5
+    dev = torch.device("cuda")
+    dX = torch.tensor(X, dtype=torch.bfloat16, device=dev)
+    dv = torch.tensor(rng.normal(size=(R, 3)).astype(np.float32) * 0.1, device=dev)
+    dw = torch.full((R,), 1.0 / R, dtype=torch.float32, device=dev)
+    out = torch.empty((R, 6), dtype=torch.float32, device=dev)
+    for _ in range(3):
+        net.forward_device(R, dX.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.isfinite(out).all()
+    l0 = net.train_step(R, dX.data_ptr(), dv.data_ptr(), dw.data_ptr(), 1e-3, want_loss=True)
+    for _ in range(20):
+        net.train_step(R, dX.data_ptr(), dv.data_ptr(), dw.data_ptr(), 1e-3)
+    l1, _ = net.loss_grad(R, dX.data_ptr(), dv.data_ptr(), dw.data_ptr(), want_grad=False)
+    assert math.isfinite(l1) and l1 < l0
+    basis.close()

@@ -771,7 +771,10 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   }
 
   cudaError_t e;
-  if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess) {
+  // a blocking stream: ordered with the legacy default stream, so device buffers that a
+  // caller fills there (e.g. PyTorch's default stream) are complete before the context's
+  // kernels read them, and results are complete before later default-stream work
+  if ((e = cudaStreamCreate(&c->own)) != cudaSuccess) {
     std::string msg = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
     delete c;
     return fail(nullptr, TP3_ERR_CUDA, msg);

@@ -53,7 +53,8 @@ __device__ inline double angle_between(double x1, double y1, double x2, double y
 
 // grid: pictures; block kBinThreads.  photons [total][2] (x, y), offsets [n + 1].
 __global__ void __launch_bounds__(kBinThreads) k_bin_pictures(const double2* __restrict__ photons,
-                                                              const long long* __restrict__ offsets, double dq, int N,
+                                                              const long long* __restrict__ offsets,
+                                                              long long n_photons, double dq, int N,
                                                               int K2, int K3, unsigned long long* __restrict__ c1,
                                                               unsigned long long* __restrict__ c2,
                                                               unsigned long long* __restrict__ c3, int* __restrict__ err) {
@@ -61,6 +62,10 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_pictures(const double2* __r
   __shared__ int sk[kMaxPhotons];
   __shared__ int s_count;
   const long long o0 = offsets[blockIdx.x], o1 = offsets[blockIdx.x + 1];
+  if (o0 < 0 || o1 < o0 || o1 > n_photons) {  // offsets outside the photon array: report, skip
+    if (threadIdx.x == 0) atomicExch(err, TP3_ERR_ARG);
+    return;
+  }
   if (threadIdx.x == 0) s_count = 0;
   __syncthreads();
   // keep photons with 1 <= k <= K2
@@ -267,15 +272,16 @@ __global__ void k_intensity_grid_max(const double2* __restrict__ coeff, int KMAX
 
 extern "C" {
 
-int tp3_histogram_pictures(tp3_ctx* c, int n_pictures, const void* d_photons, const int64_t* d_offsets, double dq,
-                           int N, int K2, int K3, unsigned long long* d_c1, unsigned long long* d_c2,
-                           unsigned long long* d_c3) {
+int tp3_histogram_pictures(tp3_ctx* c, int n_pictures, const void* d_photons, int64_t n_photons,
+                           const int64_t* d_offsets, double dq, int N, int K2, int K3, unsigned long long* d_c1,
+                           unsigned long long* d_c2, unsigned long long* d_c3) {
   if (int r = tp3::ctx_check(c)) return r;
-  if (n_pictures < 1 || !d_photons || !d_offsets || !d_c1 || !d_c2 || !d_c3 || !(dq > 0.0) || N < 1 || K2 < 1 ||
-      K3 < 1 || K3 > K2)
+  if (n_pictures < 1 || !d_photons || n_photons < 0 || !d_offsets || !d_c1 || !d_c2 || !d_c3 || !(dq > 0.0) ||
+      N < 1 || K2 < 1 || K3 < 1 || K3 > K2)
     return tp3::ctx_fail(c, TP3_ERR_ARG, "bad histogram arguments");
-  k_bin_pictures<<<n_pictures, kBinThreads, 0, c->stream>>>((const double2*)d_photons, (const long long*)d_offsets, dq,
-                                                           N, K2, K3, d_c1, d_c2, d_c3, c->d_err);
+  k_bin_pictures<<<n_pictures, kBinThreads, 0, c->stream>>>((const double2*)d_photons, (const long long*)d_offsets,
+                                                           (long long)n_photons, dq, N, K2, K3, d_c1, d_c2, d_c3,
+                                                           c->d_err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "histogram pictures");
   return TP3_OK;

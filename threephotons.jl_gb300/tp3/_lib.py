@@ -79,7 +79,7 @@ SIGNATURES = {
     "tp3_chains_move_log_count": (c_int, [c_void_p, P(c_int64)]),
     "tp3_chains_move_log_gather": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tp3_bayes_energy_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
-    "tp3_histogram_pictures": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_double, c_int, c_int, c_int,
+    "tp3_histogram_pictures": (c_int, [c_void_p, c_int, c_void_p, c_int64, c_void_p, c_double, c_int, c_int, c_int,
                                        c_void_p, c_void_p, c_void_p]),
     "tp3_sample_pictures": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_int, c_int, c_double, c_double, c_double,
                                     c_int, c_double, c_double, ctypes.c_uint64, c_int, c_void_p, c_void_p]),

@@ -52,7 +52,8 @@ def histogram_pictures(basis, pictures, dq: float, N: int, K2: int, K3: int, ret
     c1 = torch.zeros(K2, dtype=torch.int64, device=dev)
     c2 = torch.zeros(N * K2 * K2, dtype=torch.int64, device=dev)
     c3 = torch.zeros(N * 2 * N * K3 ** 3, dtype=torch.int64, device=dev)
-    check(basis._lib.tp3_histogram_pictures(basis.ctx, len(pics), ctypes.c_void_p(d_p.data_ptr()),
+    torch.cuda.synchronize()  # the zeroed histograms (filled on PyTorch's stream) before the library reads them
+    check(basis._lib.tp3_histogram_pictures(basis.ctx, len(pics), ctypes.c_void_p(d_p.data_ptr()), int(d_p.shape[0]),
                                             ctypes.c_void_p(d_o.data_ptr()), float(dq), N, K2, K3,
                                             ctypes.c_void_p(c1.data_ptr()), ctypes.c_void_p(c2.data_ptr()),
                                             ctypes.c_void_p(c3.data_ptr())), basis.ctx)
@@ -105,6 +106,7 @@ def generateHistogram(basis, coeff: np.ndarray, dq: float, qcut: float, K2: int,
     ph = torch.empty((nb, max_out, 2), dtype=torch.float64, device=dev)
     cnt = torch.empty(nb, dtype=torch.int32, device=dev)
     done = 0
+    torch.cuda.synchronize()  # zeroed histograms before the library adds to them
     while done < pictures:
         n = min(nb, pictures - done)
         check(basis._lib.tp3_sample_pictures(basis.ctx, n, done, ctypes.c_void_p(d_c.data_ptr()), KMAX, LMAX,
@@ -112,6 +114,7 @@ def generateHistogram(basis, coeff: np.ndarray, dq: float, qcut: float, K2: int,
                                              float(lambda_), float(Imax), ctypes.c_uint64(seed), max_out,
                                              ctypes.c_void_p(ph.data_ptr()), ctypes.c_void_p(cnt.data_ptr())),
               basis.ctx)
+        basis.sync()  # the sampled photons and counts before PyTorch compacts them
         counts = cnt[:n].to(torch.int64)
         mask = torch.arange(max_out, device=dev)[None, :] < counts[:, None]
         flat = ph[:n][mask].contiguous()
@@ -119,7 +122,8 @@ def generateHistogram(basis, coeff: np.ndarray, dq: float, qcut: float, K2: int,
         offs[1:] = torch.cumsum(counts, 0)
         if flat.numel() == 0:
             flat = torch.zeros((1, 2), dtype=torch.float64, device=dev)
-        check(basis._lib.tp3_histogram_pictures(basis.ctx, n, ctypes.c_void_p(flat.data_ptr()),
+        torch.cuda.synchronize()  # the compacted photons and offsets before the library reads them
+        check(basis._lib.tp3_histogram_pictures(basis.ctx, n, ctypes.c_void_p(flat.data_ptr()), int(flat.shape[0]),
                                                 ctypes.c_void_p(offs.data_ptr()), float(dqh), N, K2, K3,
                                                 ctypes.c_void_p(c1.data_ptr()), ctypes.c_void_p(c2.data_ptr()),
                                                 ctypes.c_void_p(c3.data_ptr())), basis.ctx)

@@ -127,13 +127,16 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
     def fill(idx_cpu):
         n = idx_cpu.numel()
         idx = idx_cpu.to(dev, dtype=torch.int64)
+        torch.cuda.synchronize()   # indices (PyTorch's stream) before the gather reads them
         chains.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
+        chains.basis.sync()        # gathered rows before PyTorch computes the weights
         w = move_weights(M[:n])
         W.zero_()
         W[: n * K] = (w / torch.clamp(w.sum(), min=1e-12)).repeat_interleave(K)
         if n * K < rows:
             X[n * K:].zero_()
             V[n * K:].zero_()
+        torch.cuda.synchronize()   # weights and padding before the library trains on them
 
     def heldout_loss():
         tot, wsum = 0.0, 0
