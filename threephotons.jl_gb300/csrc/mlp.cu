@@ -156,10 +156,60 @@ __global__ void __launch_bounds__(kGThreads, 1) k_gemm_tn(const __grid_constant_
       for (int c = 0; c < (BN + 31) / 32; ++c) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), v);
-        if (m < g.M) {
+        const int nb = n0 + c * 32;
+        // a whole 32-column run inside the tile and the matrix: 16-byte vector loads/stores
+        const bool full = c * 32 + 32 <= BN && nb + 32 <= g.N && (!g.out_bf || g.ldo % 8 == 0) &&
+                          (!g.gate || g.ldg % 8 == 0);
+        if (m < g.M && full) {
+          float x[32];
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int n = n0 + c * 32 + j;
+            x[j] = v[j];
+            if (g.bias) x[j] += g.bias[nb + j];
+            if (g.relu) x[j] = fmaxf(x[j], 0.f);
+          }
+          if (g.gate) {
+            const uint4* gp = reinterpret_cast<const uint4*>(g.gate + (size_t)m * g.ldg + nb);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+              const uint4 u = gp[q4];
+              const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&w4[t]);
+                if (!(__low2float(h) > 0.f)) x[q4 * 8 + 2 * t] = 0.f;
+                if (!(__high2float(h) > 0.f)) x[q4 * 8 + 2 * t + 1] = 0.f;
+              }
+            }
+          }
+          if (g.out_f32) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (ks > 1) atomicAdd(&g.out_f32[(size_t)m * g.ldf + nb + j], x[j]);
+              else g.out_f32[(size_t)m * g.ldf + nb + j] = x[j];
+            }
+          }
+          if (g.out_bf) {
+            uint4* op = reinterpret_cast<uint4*>(g.out_bf + (size_t)m * g.ldo + nb);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+              uint32_t w4[4];
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(x[q4 * 8 + 2 * t], x[q4 * 8 + 2 * t + 1]);
+                w4[t] = *reinterpret_cast<const uint32_t*>(&h);
+              }
+              op[q4] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            }
+          }
+          if (g.outT_bf) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) g.outT_bf[(size_t)(nb + j) * g.ldt + m] = __float2bfloat16_rn(x[j]);
+          }
+        } else if (m < g.M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = nb + j;
             if (c * 32 + j >= BN || n >= g.N) continue;
             float x = v[j];
             if (g.bias) x += g.bias[n];
@@ -386,8 +436,9 @@ cudaError_t pack_all(tp3_mlp* n) {
   return cudaGetLastError();
 }
 
-// forward on rows [0, R) of the net's input buffer
-cudaError_t forward(tp3_mlp* n, int R) {
+// forward on rows [0, R) of the net's input buffer; the transposed activations the
+// backward pass reads are written only when training (with_t)
+cudaError_t forward(tp3_mlp* n, int R, bool with_t) {
   cudaError_t e;
   const int H = n->H;
   for (int l = 0; l < 3; ++l) {
@@ -395,7 +446,7 @@ cudaError_t forward(tp3_mlp* n, int R) {
     g.bias = n->d_par + n->off_b[l];
     g.relu = 1;
     g.out_bf = n->Hh[l]; g.ldo = H;
-    g.outT_bf = n->Ht[l]; g.ldt = n->max_rows;
+    if (with_t) { g.outT_bf = n->Ht[l]; g.ldt = n->max_rows; }
     if ((e = gemm(n, n->fA[l], n->fB[l], g)) != cudaSuccess) return e;
   }
   GemmArgs g = args(R, kMlpOut, H);
@@ -477,7 +528,7 @@ cudaError_t mlp_configure() {
 
 // Raw network outputs (before the head mapping) of rows [0, R) of the input buffer.
 int mlp_forward_raw(tp3_mlp* n, int R, const float** out) {
-  cudaError_t e = forward(n, R);
+  cudaError_t e = forward(n, R, false);
   if (e != cudaSuccess) return ctx_cuda_fail(n->ctx, e, "mlp forward");
   *out = n->O;
   return TP3_OK;
@@ -642,7 +693,7 @@ int tp3_mlp_forward_device(tp3_mlp* n, int rows, const void* d_x, void* d_out) {
   if (!n || !d_out) return TP3_ERR_ARG;
   if (int r = mlp_load_input(n, rows, d_x)) return r;
   tp3_ctx* c = n->ctx;
-  cudaError_t e = tp3::forward(n, rows);
+  cudaError_t e = tp3::forward(n, rows, false);
   if (e == cudaSuccess) {
     tp3::k_head_map<<<(rows + 127) / 128, 128, 0, c->stream>>>(n->O, rows, (float*)d_out);
     e = cudaGetLastError();
@@ -657,7 +708,7 @@ static int mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v
   if (!d_v || !d_w) return tp3::ctx_fail(c, TP3_ERR_ARG, "NULL targets or weights");
   if (int r = mlp_load_input(n, rows, d_x)) return r;
   cudaError_t e = cudaMemsetAsync(n->d_err, 0, sizeof(int), c->stream);
-  if (e == cudaSuccess) e = tp3::forward(n, rows);
+  if (e == cudaSuccess) e = tp3::forward(n, rows, true);
   if (e == cudaSuccess) e = tp3::backward(n, rows, d_v, d_w);
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "mlp backward");
   if (loss) {
