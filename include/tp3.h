@@ -344,6 +344,13 @@ int tp3_mlp_loss_grad(tp3_mlp* net, int rows, const void* d_x, const float* d_v,
 int tp3_mlp_train_step(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w, float lr,
                        double* loss);
 
+/* ---- failure detection self test (no reference counterpart) ------------------- */
+/* Launch a kernel whose bounded mbarrier wait can never complete, with a limit of
+ * `cycles` SM clocks (1e3 .. 4e9): the wait runs out, the kernel records
+ * TP3_ERR_TIMEOUT and returns, and the next synchronising call on the context
+ * (tp3_sync, tp3_energy*, ...) reports TP3_ERR_TIMEOUT; the context stays usable. */
+int tp3_selftest_timeout(tp3_ctx* ctx, long long cycles);
+
 /* ---- per-launch timing of the dominant kernel ----------------------------- */
 /* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on
  * the launching stream; tp3_profile_read returns the launch count and the summed

@@ -181,3 +181,18 @@ def test_coupling_forms_agree(basis1, config1, config1_hist, form, kind):
     E = basis1.energy_batch(config1["coeff"][None, : p["K"]])[0]
     assert E == pytest.approx(float(config1["E_fp64"]), rel=1e-6)
     basis1.set_coupling(0)
+
+
+def test_bounded_wait_reports_timeout_and_context_stays_usable(basis1, config1, config1_hist):
+    """Failure detection without a fault: a device wait on a flag nothing sets runs out
+    after ~5 ms, the status reaches the host as TP3_ERR_TIMEOUT at the next synchronising
+    call, and the context then scores correctly again."""
+    lib = tp3.load()
+    basis1.set_histogram(config1_hist)
+    assert lib.tp3_selftest_timeout(basis1.ctx, 10_000_000) == 0
+    with pytest.raises(tp3.TP3Error) as ei:
+        basis1.sync()
+    assert ei.value.status == _lib.TP3_ERR_TIMEOUT
+    p = config1["params"]
+    E = basis1.energy_batch(config1["coeff"][None, : p["K"]])[0]
+    assert E == pytest.approx(float(config1["E_fp64"]), rel=1e-6)
