@@ -202,8 +202,9 @@ int tp3_chains_coeff(tp3_chains* chains, double* coeff);
  * E_new, E, dE, T, acceptance probability, sigma_L. */
 int tp3_chains_log(tp3_chains* chains, int chain, double* rows, int64_t* nrows);
 /* Checkpoint: with buf NULL, *bytes receives the size; otherwise the chain state
- * (coefficients, E, T, counters, step sizes) is written to buf.  Restore is
- * bit-exact; the RNG needs no state beyond the step counters. */
+ * (coefficients, E, T, counters, step sizes, the network's history inputs) is
+ * written to buf.  Restore is bit-exact; the RNG needs no state beyond the step
+ * counters. */
 int tp3_chains_snapshot(tp3_chains* chains, void* buf, size_t capacity, size_t* bytes);
 int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
 /* Move of a chain set.  TP3_MOVE_REFERENCE (default): get_MC_step
@@ -211,10 +212,20 @@ int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
  * exp([v]x), v ~ N(0, sigma^2 I3), with the Wigner-D rotation of rotateStructure
  * (src/spherical_harmonics.jl:595-603) on every even l; sigma starts at sigma0 and
  * is multiplied / divided by the step-size factor on accept / reject like the
- * reference's step sizes.  TP3_MOVE_LEARNED: a candidate comes from the network
- * (tp3_mlp) with probability p_net and from the isotropic step otherwise; the
- * Metropolis-Hastings ratio of the mixture density corrects the acceptance.  The
- * network must have n_in = (L+1)^2 + 9 and max_rows >= chains x candidates x K.
+ * reference's step sizes.  Every launch of per-shell moves also estimates, per chain
+ * and shell, the energy gradient from its B candidates (all drawn at the launch's
+ * start state):  e_k = (1/B) sum_i ((dE_i - mean_j dE_j) / T) w_ik,  w_ik the
+ * candidate's whitened step noise (z for an isotropic step; see below), T the first
+ * candidate's temperature; the last 8 launches' e_k are features of the network.
+ * TP3_MOVE_LEARNED: a candidate comes from the network (tp3_mlp) with probability
+ * p_net and from the isotropic step otherwise.  A network candidate with outputs
+ * (u_k, s_k) draws a = +-1 (equally likely) and
+ *     v_k = sigma_i (a sqrt(16) u_k / sqrt(sum_k |u_k|^2 + 0.01) + exp(s_k - mean_k s_k) z_k),
+ * z_k ~ N(0, I3) (whitened noise exp(-(s_k - mean s)) z_k): a two-sided drift along
+ * the network's gradient estimate.  The Metropolis-Hastings ratio of the mixture
+ * density (the network part a two-component mixture over a, evaluated at x' for the
+ * reverse step with the network re-run there) corrects the acceptance.  The network
+ * must have n_in = (L+1)^2 + 33 and max_rows >= chains x candidates x K.
  * No reference counterpart for the two per-shell kinds. */
 #define TP3_MOVE_REFERENCE 0
 #define TP3_MOVE_SHELL_SO3 1
@@ -223,15 +234,15 @@ int tp3_chains_set_move(tp3_chains* chains, int kind, double sigma0, double p_ne
 
 /* Move log for training the network: a ring of `launches` launches of per-shell
  * moves; per candidate the state's feature rows, the steps v, and
- * (dE, T, accepted, drawn-from-network, log q(x|x') - log q(x'|x), sigma_i) where
- * accepted is the Metropolis decision with the candidate's own uniform (the chain's
- * actual decision up to its taken step) and sigma_i the candidate's isotropic step
- * size.  The network proposes relative to sigma_i: for its outputs (mu^_k, s^_k),
- * shell k's step is N(sigma_i mu^_k, exp(2 (log sigma_i + s^_k - mean_k s^_k))).  tp3_chains_move_log_count returns the candidates held (synchronising);
+ * (dE, T, accepted, drawn-from-network, log q(x|x') - log q(x'|x), sigma_i,
+ *  (dE - mean over the launch's candidates of dE) / T) where accepted is the
+ * Metropolis decision with the candidate's own uniform (the chain's actual decision
+ * up to its taken step) and sigma_i the candidate's isotropic step size.
+ * tp3_chains_move_log_count returns the candidates held (synchronising);
  * tp3_chains_move_log_gather writes, for n candidate positions d_idx (int64, device,
- * each < count), n x K feature rows (BF16, stride (L+1)^2 + 9 rounded up to 32, the
+ * each < count), n x K feature rows (BF16, stride (L+1)^2 + 33 rounded up to 32, the
  * temperature column set to the candidate's), n x K x 3 steps divided by sigma_i
- * (float) and n x 6 meta floats in that order into device buffers. */
+ * (float) and n x 7 meta floats in that order into device buffers. */
 int tp3_chains_enable_move_log(tp3_chains* chains, int launches);
 int tp3_chains_move_log_count(tp3_chains* chains, int64_t* candidates);
 int tp3_chains_move_log_gather(tp3_chains* chains, int n, const int64_t* d_idx, void* d_x, float* d_v, float* d_meta);
@@ -319,8 +330,9 @@ int tp3_rotate_shells_device(tp3_ctx* ctx, int n, const void* d_coeffs, const vo
  * Architecture: n_in -> hidden -> hidden -> hidden -> 6, ReLU, BF16 weights and
  * activations, FP32 accumulation on the tensor cores, FP32 master weights and
  * Adam.  Rows are shells; input rows are BF16 with a stride of n_in rounded up to
- * 32 (the padding columns must be zero).  Outputs per row: mu[3] (the mean axis-angle
- * step, |mu_d| < 0.5) and s[3] (log of its standard deviation, in (-7, 1)).
+ * 32 (the padding columns must be zero).  Outputs per row: u[3] (the shell's drift
+ * direction: an estimate of sigma g / T, g the energy gradient of the shell's rotation)
+ * and s[3] (log of the step's standard deviation in units of sigma, in (-7, 1)).
  * Parameters are one FP32 vector: W1 (hidden x n_in, row-major), b1, W2, b2, W3, b3,
  * W4 (6 x hidden), b4. */
 int tp3_mlp_create(tp3_ctx* ctx, int n_in, int hidden, int max_rows, uint64_t seed, tp3_mlp** out);
@@ -331,18 +343,23 @@ int tp3_mlp_set_params(tp3_mlp* net, const float* host, int64_t count);
 /* The network's own input buffer (max_rows x row_stride BF16, device): writing the
  * features there saves the copy that the calls below make from any other pointer. */
 int tp3_mlp_input_buffer(tp3_mlp* net, void** d_x, int* row_stride);
-/* (mu, s) of rows [0, rows) into d_out = rows x 6 floats (device).  Asynchronous. */
+/* (u, s) of rows [0, rows) into d_out = rows x 6 floats (device).  Asynchronous. */
 int tp3_mlp_forward_device(tp3_mlp* net, int rows, const void* d_x, void* d_out);
-/* Loss sum_r w_r NLL(v_r; mu_r, s_r) of axis-angle steps d_v (rows x 3 floats) with
- * weights d_w (rows floats), and its gradient (FP32, the parameter layout) copied to
- * grad_host when not NULL.  rows must be a multiple of 128 (pad with w = 0 and zero
- * features).  Synchronises. */
-int tp3_mlp_loss_grad(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w, double* loss,
-                      float* grad_host);
+/* Training loss of logged candidates, `shells` consecutive rows each, steps d_v
+ * (rows x 3 floats, v / sigma):
+ *   sum_j lambda_j (t_j - sum_k u_k . v_k)^2 / 2            (d_target = (t_j, lambda_j)
+ *                                                           per candidate, rows/shells
+ *                                                           float pairs; NULL: no term)
+ * + sum_r w_r sum_d [s_d + v_d^2 exp(-2 s_d) / 2 + log(2 pi) / 2]   (weights d_w, rows)
+ * and its gradient (FP32, the parameter layout) copied to grad_host when not NULL.
+ * rows must be a multiple of 128 (pad with w = 0, lambda = 0 and zero features).
+ * Synchronises. */
+int tp3_mlp_loss_grad(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w,
+                      const float* d_target, int shells, double* loss, float* grad_host);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss; the loss is returned
  * (synchronising) when loss is not NULL, else the call stays asynchronous. */
-int tp3_mlp_train_step(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w, float lr,
-                       double* loss);
+int tp3_mlp_train_step(tp3_mlp* net, int rows, const void* d_x, const float* d_v, const float* d_w,
+                       const float* d_target, int shells, float lr, double* loss);
 
 /* ---- failure detection self test (no reference counterpart) ------------------- */
 /* Launch a kernel whose bounded mbarrier wait can never complete, with a limit of

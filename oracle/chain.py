@@ -168,23 +168,53 @@ def rot_logdens(v, mu, s) -> float:
     return m + math.log(sum(math.exp(t - m) for t in terms))
 
 
-def shell_params(mu_hat, s_hat, sigma: float):
+def drift_factor(u_hat) -> float:
+    """sqrt(gamma) / sqrt(sum over the candidate's shells of |u|^2 + eps^2)."""
+    from .mlp import DRIFT_GAMMA, DRIFT_EPS
+    u = np.asarray(u_hat, dtype=np.float64)
+    return math.sqrt(DRIFT_GAMMA) / math.sqrt(float(np.sum(u * u)) + DRIFT_EPS ** 2)
+
+
+def shell_params(u_hat, s_hat, sigma: float):
     """Per-shell step parameters from the network head relative to the isotropic step
-    size: mu = sigma mu^, s = log sigma + s^ - mean over shells of s^."""
-    mu_hat, s_hat = np.asarray(mu_hat, dtype=np.float64), np.asarray(s_hat, dtype=np.float64)
-    return sigma * mu_hat, math.log(sigma) + s_hat - s_hat.mean(axis=0, keepdims=True)
+    size: drift m = sigma f u^ (f = drift_factor), s = log sigma + s^ - mean over shells
+    of s^."""
+    u_hat, s_hat = np.asarray(u_hat, dtype=np.float64), np.asarray(s_hat, dtype=np.float64)
+    return sigma * drift_factor(u_hat) * u_hat, math.log(sigma) + s_hat - s_hat.mean(axis=0, keepdims=True)
 
 
-def mixture_log_ratio(v, mu, s, mu2, s2, sigma: float, p_net: float) -> float:
-    """log q(x|x') - log q(x'|x) of the mixture p q_net + (1 - p) q_iso over all shells."""
+def net_logdens(v, m, s) -> float:
+    """log q_net(v) = log((prod_k q(v_k; +m_k, s_k) + prod_k q(v_k; -m_k, s_k)) / 2)."""
+    K = v.shape[0]
+    lp = sum(rot_logdens(v[k], m[k], s[k]) for k in range(K))
+    lm = sum(rot_logdens(v[k], -m[k], s[k]) for k in range(K))
+    return float(np.logaddexp(lp, lm) - math.log(2.0))
+
+
+def mixture_log_ratio(v, m, s, m2, s2, sigma: float, p_net: float) -> float:
+    """log q(x|x') - log q(x'|x) of the mixture p q_net + (1 - p) q_iso over all shells;
+    (m, s) the network's step parameters at x, (m2, s2) at x'."""
     K = v.shape[0]
     ls = np.full(3, math.log(sigma))
-    fnet = sum(rot_logdens(v[k], mu[k], s[k]) for k in range(K))
-    rnet = sum(rot_logdens(-v[k], mu2[k], s2[k]) for k in range(K))
+    fnet = net_logdens(v, m, s)
+    rnet = net_logdens(-v, m2, s2)
     fiso = sum(rot_logdens(v[k], np.zeros(3), ls) for k in range(K))
     lp = math.log(p_net)
     lq = math.log1p(-p_net) if p_net < 1 else -math.inf
     return float(np.logaddexp(lp + rnet, lq + fiso) - np.logaddexp(lp + fnet, lq + fiso))
+
+
+def gradient_estimate(dE, T1: float, w) -> np.ndarray:
+    """The launch's per-shell gradient estimate from its B candidates (all drawn at the
+    same state): e = (1/n) sum_i ((dE_i - mean dE) / T1) w_i over the n candidates with a
+    finite dE; w [B][K][3] the whitened step noise (z for an isotropic step)."""
+    dE = np.asarray(dE, dtype=np.float64)
+    w = np.asarray(w, dtype=np.float64)
+    ok = np.isfinite(dE)
+    if not ok.any():
+        return np.zeros(w.shape[1:])
+    d = dE[ok] - dE[ok].mean()
+    return np.tensordot(d, w[ok], axes=(0, 0)) / (ok.sum() * T1)
 
 
 def run_shell_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, sigma0: float,

@@ -8,8 +8,10 @@ FP64, so the device (FP32 accumulation on the tensor cores) agrees with it to
 accumulation rounding.
 
 Parameter vector (FP32): W1 (H x n_in), b1, W2 (H x H), b2, W3, b3, W4 (6 x H), b4.
-Head: mu = 0.5 tanh(o[0:3]), s = -3 + 4 tanh(o[3:6]).
-Loss: sum_r w_r sum_d [s_d + (v_d - mu_d)^2 exp(-2 s_d) / 2 + log(2 pi) / 2].
+Head: u = o[0:3] (drift direction), s = -3 + 4 tanh(o[3:6]) (log-scale).
+Loss over candidates j of K consecutive rows with targets (t_j, lambda_j):
+    sum_j lambda_j (t_j - sum_k u_k . v_k)^2 / 2
+  + sum_r w_r sum_d [s_d + v_d^2 exp(-2 s_d) / 2 + log(2 pi) / 2].
 """
 from __future__ import annotations
 
@@ -17,7 +19,9 @@ import math
 
 import numpy as np
 
-MU_SCALE, S_MID, S_HALF = 0.5, -3.0, 4.0
+S_MID, S_HALF = -3.0, 4.0
+DRIFT_GAMMA, DRIFT_EPS = 16.0, 0.1
+N_GHIST = 8
 
 
 def bf16(x) -> np.ndarray:
@@ -58,22 +62,29 @@ def forward(p, X, n_in: int, H: int):
 
 
 def head(O):
-    return MU_SCALE * np.tanh(O[:, :3]), S_MID + S_HALF * np.tanh(O[:, 3:6])
+    return np.asarray(O[:, :3], dtype=np.float64), S_MID + S_HALF * np.tanh(O[:, 3:6])
 
 
-def loss_grad(p, X, v, w, n_in: int, H: int):
-    """(loss, gradient vector in the parameter layout)."""
+def loss_grad(p, X, v, w, n_in: int, H: int, tw=None, K: int = 1):
+    """(loss, gradient vector in the parameter layout); tw: (t_j, lambda_j) per candidate
+    of K rows (None: no regression term)."""
     layers = split_params(p, n_in, H)
     O, A = forward(p, X, n_in, H)
-    tm, ts = np.tanh(O[:, :3]), np.tanh(O[:, 3:6])
-    mu, s = MU_SCALE * tm, S_MID + S_HALF * ts
-    e = v - mu
+    u, ts = O[:, :3], np.tanh(O[:, 3:6])
+    s = S_MID + S_HALF * ts
     is2 = np.exp(-2.0 * s)
-    loss = float(np.sum(w[:, None] * (s + 0.5 * e * e * is2 + 0.5 * math.log(2 * math.pi))))
-    dmu = -e * is2
-    ds = 1.0 - e * e * is2
-    dO = bf16(np.concatenate([w[:, None] * dmu * MU_SCALE * (1 - tm * tm),
-                              w[:, None] * ds * S_HALF * (1 - ts * ts)], axis=1))
+    loss = float(np.sum(w[:, None] * (s + 0.5 * v * v * is2 + 0.5 * math.log(2 * math.pi))))
+    du = np.zeros_like(u)
+    if tw is not None:
+        R = O.shape[0]
+        nc = R // K
+        pred = np.sum((u[:nc * K] * v[:nc * K]).reshape(nc, K * 3), axis=1)
+        res = tw[:nc, 0] - pred
+        loss += float(np.sum(0.5 * tw[:nc, 1] * res * res))
+        rr = f32(tw[:nc, 1] * res)  # the device keeps the weighted residual in FP32
+        du[:nc * K] = -np.repeat(rr, K)[:, None] * v[:nc * K]
+    ds = 1.0 - v * v * is2
+    dO = bf16(np.concatenate([du, w[:, None] * ds * S_HALF * (1 - ts * ts)], axis=1))
     grads = []
     W4, _ = layers[3]
     gW = dO.T @ A[3]
@@ -102,10 +113,11 @@ def init_params(n_in: int, H: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride: int) -> np.ndarray:
+def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride: int, ghist=None) -> np.ndarray:
     """Feature rows (K x stride, BF16 values) of a state's shells: (L+1)^2 real SH
     coefficients x = Umat(l) c_l scaled to norm 8, the 8 history values dE/T clipped to
-    +-10 and divided by 10, log10(T)/4, zeros."""
+    +-10 and divided by 10, log10(T)/4, the shell's gradient estimates of the last 8
+    launches (ghist [8][K][3], newest first; FP32, clipped to +-8 and halved), zeros."""
     from .sh import Umat, seanindex
     K = coeff.shape[0]
     nf = (L + 1) ** 2
@@ -121,4 +133,7 @@ def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride:
         out[k, :nf] = x * (8.0 / nrm) if nrm > 0 else 0.0
         out[k, nf:nf + 8] = h
         out[k, nf + 8] = math.log10(T) / 4.0
+        if ghist is not None:
+            gk = np.asarray(ghist, dtype=np.float32)[:, k, :].astype(np.float64)  # [8][3]
+            out[k, nf + 9:nf + 9 + 3 * N_GHIST] = 0.5 * np.clip(gk, -8.0, 8.0).reshape(-1)
     return bf16(out)

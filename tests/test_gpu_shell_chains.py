@@ -1,6 +1,7 @@
 """Per-shell SO(3) chain moves and the learned (network) proposal on the device
-against the oracle: the isotropic chain's trajectory, the network proposal with a
-constant head reducing to the isotropic one, and the logged features, steps and
+against the oracle: the isotropic chain's trajectory, the per-launch gradient
+estimates that feed the network, the network proposal with a constant head reducing
+to the isotropic one, and the logged features, two-sided drift steps and
 Metropolis-Hastings ratios of a random network recomputed on the CPU."""
 import math
 
@@ -73,7 +74,7 @@ def test_isotropic_shell_chain_matches_oracle(setup):
 
 def _constant_head_params(net, s_const):
     P = np.zeros(net.n_params, dtype=np.float32)
-    P[-3:] = math.atanh((s_const - om.S_MID) / om.S_HALF)  # b4[3:6]: s = s_const, mu = 0
+    P[-3:] = math.atanh((s_const - om.S_MID) / om.S_HALF)  # b4[3:6]: s = s_const, u = 0
     return P
 
 
@@ -103,6 +104,49 @@ def test_constant_network_reduces_to_isotropic(setup):
     net.close()
 
 
+def _gather(ch, positions, K, stride):
+    import torch
+    dev = torch.device("cuda")
+    n = len(positions)
+    idx = torch.tensor(positions, dtype=torch.int64, device=dev)
+    X = torch.empty((n * K, stride), dtype=torch.bfloat16, device=dev)
+    V = torch.empty((n * K, 3), dtype=torch.float32, device=dev)
+    M = torch.empty((n, 7), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    ch.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
+    torch.cuda.synchronize()
+    return X.float().cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64), M.cpu().numpy()
+
+
+def test_gradient_history_matches_oracle(setup):
+    """Each launch's per-shell gradient estimate (from its candidates' energy changes and
+    whitened steps) enters the next launch's feature rows: recomputed on the CPU from the
+    logged candidates of the first launch."""
+    basis, e64, start, p = setup
+    nch, B = 2, 8
+    L, LMAX, K = p["L"], p["LMAX"], p["K"]
+    T0, decay = 2.0, 0.995
+    ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, 1.05, decay, SEED, ncand=B)
+    ch.set_move(tp3.TP3_MOVE_SHELL_SO3, 0.3)
+    ch.enable_move_log(4)
+    ch.run(2)
+    stride = (n_in_for(L) + 31) // 32 * 32
+    nf = (L + 1) ** 2
+    X1, V1, M1 = _gather(ch, list(range(nch * B)), K, stride)
+    X2, _, _ = _gather(ch, [nch * B + c * B for c in range(nch)], K, stride)
+    for c in range(nch):
+        dE = M1[c * B:(c + 1) * B, 0]
+        w = V1[c * B * K:(c + 1) * B * K].reshape(B, K, 3)  # isotropic steps: w = v / sigma
+        e = oc.gradient_estimate(dE, T0 * decay, w)
+        assert np.abs(e).max() > 1e-3  # a real signal, not a zero history
+        got = X2[c * K:(c + 1) * K, nf + 9:nf + 12]  # newest launch first
+        ref = 0.5 * np.clip(e, -8, 8)
+        np.testing.assert_allclose(got, ref, rtol=2 ** -7, atol=1e-4)
+        # older launches: zeros (two launches run, the first saw an empty history)
+        assert np.all(X2[c * K:(c + 1) * K, nf + 12:nf + 33] == 0.0)
+    ch.close()
+
+
 def test_learned_moves_match_oracle(setup):
     import torch
     basis, e64, start, p = setup
@@ -111,7 +155,7 @@ def test_learned_moves_match_oracle(setup):
     n_in = n_in_for(L)
     net = ProposalMLP(basis, n_in, hidden=128, max_rows=((nch * B * K + 127) // 128) * 128, seed=2)
     params = om.init_params(n_in, 128, 11)
-    # moderate relative steps (|mu^| small, s^ near 0): the reverse density stays well
+    # moderate steps (s^ near 0, drifts of a few sigma): the reverse density stays well
     # conditioned, so one-ulp BF16 differences between the device's and the oracle's
     # features of x' move the ratio by far less than the tolerance
     nW4 = 6 * 128
@@ -123,21 +167,21 @@ def test_learned_moves_match_oracle(setup):
     ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, 1.05, decay, SEED, ncand=B)
     ch.set_move(tp3.TP3_MOVE_LEARNED, sigma0, p_net, net)
     ch.enable_move_log(4)
+    # plant a gradient history (the snapshot's last block: [nch][8][K][3] float32)
+    blob = bytearray(ch.snapshot())
+    ng = nch * 8 * K * 3
+    ghist = np.random.default_rng(8).normal(size=(nch, 8, K, 3)).astype(np.float32)
+    blob[len(blob) - 4 * ng:] = ghist.tobytes()
+    ch.restore(bytes(blob))
     ch.run(1)
     n = ch.move_log_count()
     assert n == nch * B
-    dev = torch.device("cuda")
-    idx = torch.arange(n, dtype=torch.int64, device=dev)
     stride = (n_in + 31) // 32 * 32
-    X = torch.empty((n * K, stride), dtype=torch.bfloat16, device=dev)
-    V = torch.empty((n * K, 3), dtype=torch.float32, device=dev)
-    M = torch.empty((n, 6), dtype=torch.float32, device=dev)
-    ch.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
-    torch.cuda.synchronize()
-    X, V, M = X.float().cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64), M.cpu().numpy()
+    X, V, M = _gather(ch, list(range(n)), K, stride)
     hist = np.zeros(8)
     P64 = params.astype(np.float64)
     E0 = e64(start)
+    dev = torch.device("cuda")
 
     def dev_head(feats):  # the device network on given feature rows
         d_x = torch.tensor(feats, dtype=torch.bfloat16, device=dev)
@@ -147,39 +191,46 @@ def test_learned_moves_match_oracle(setup):
         o = out.cpu().numpy().astype(np.float64)
         return o[:, :3], o[:, 3:]
 
+    n_net = 0
     for c in range(nch):
         for i in range(B):
             j = c * B + i
             T = T0
             for _ in range(i + 1):
                 T *= decay
-            feats = om.shell_features(start, L, LMAX, hist, T, stride)
+            feats = om.shell_features(start, L, LMAX, hist, T, stride, ghist[c])
             Xd = X[j * K:(j + 1) * K]
             # features agree to one BF16 rounding
             assert np.all(np.abs(Xd - feats) <= 2 ** -7 * np.abs(feats) + 1e-30)
             z, u = oc.shell_steps(SEED, i, c, K)
             comp = 1.0 if u < p_net else 0.0
             assert M[j, 3] == comp
+            n_net += int(comp)
             v = V[j * K:(j + 1) * K]
             # network vs oracle network (FP64 accumulation, same BF16 roundings)
-            mu_o, s_o = om.head(om.forward(P64, feats, n_in, 128)[0])
-            mu, s = dev_head(Xd)  # the rows the chain used
-            np.testing.assert_allclose(mu, mu_o, atol=3e-3)
-            np.testing.assert_allclose(s, s_o, atol=3e-3)
+            u_o, s_o = om.head(om.forward(P64, feats, n_in, 128)[0])
+            uh, sh = dev_head(Xd)  # the rows the chain used
+            np.testing.assert_allclose(uh, u_o, atol=3e-3)
+            np.testing.assert_allclose(sh, s_o, atol=3e-3)
             sig_i = sigma0
             for _ in range(i):  # candidate i assumes i rejections: sigma / f^i
                 sig_i /= 1.05
             assert M[j, 5] == pytest.approx(sig_i, rel=1e-6)
             v = v * M[j, 5]  # the log holds v / sigma_i
-            mu, s = oc.shell_params(mu, s, sig_i)
-            vref = mu + np.exp(s) * z if comp else sig_i * z
+            m, s = oc.shell_params(uh, sh, sig_i)
+            if comp:
+                a = 1.0 if oc.u01(oc.philox4x32_10((i, c, 3, 0), (SEED & oc.M32, SEED >> 32))[1]) >= 0.5 else -1.0
+                vref = a * m + np.exp(s) * z
+            else:
+                vref = sig_i * z
             np.testing.assert_allclose(v, vref, rtol=1e-5, atol=1e-6)
             # Metropolis-Hastings ratio of the mixture, reverse density at x'
             x2 = oc.rotate_shells(start, v, L, LMAX)
-            mu2, s2 = oc.shell_params(*dev_head(om.shell_features(x2, L, LMAX, hist, T, stride)), sig_i)
-            lr = oc.mixture_log_ratio(v, mu, s, mu2, s2, sig_i, p_net)
+            m2, s2 = oc.shell_params(*dev_head(om.shell_features(x2, L, LMAX, hist, T, stride, ghist[c])), sig_i)
+            lr = oc.mixture_log_ratio(v, m, s, m2, s2, sig_i, p_net)
             assert M[j, 4] == pytest.approx(lr, abs=0.05 + 0.01 * abs(lr))
             assert M[j, 0] == pytest.approx(e64(x2) - E0, abs=5e-7 * abs(E0))
+    assert 0 < n_net < nch * B
     ch.close()
     net.close()
 

@@ -27,15 +27,22 @@
 // TP3_MOVE_SHELL_SO3 rotates every shell k by its own exp([v_k]x) with the isotropic
 // axis-angle step v_k ~ N(0, sigma^2 I3) (sigma adapted like the reference's step
 // sizes), applied with the Wigner-D rotation of rotateStructure
-// (src/spherical_harmonics.jl:572-603) to every even l.  TP3_MOVE_LEARNED draws a
-// candidate from the mixture p * q_net + (1 - p) * q_iso, where q_net samples
-// v_k ~ N(mu_k, diag(exp(2 s_k))) with (mu_k, s_k) the proposal network's output for
-// shell k's features at the current state, and accepts it with the
-// Metropolis-Hastings rule u < exp(-dE/T) q(x | x') / q(x' | x): the reverse density
-// evaluates the network at the proposed state x' for the step -v (the rotation
-// densities include the preimages |v| + 2 pi n of the exponential map).  The network
-// sees the chain's recent dE/T history and the candidate's temperature as fixed
-// parameters of the step, so every step is an exact MH step for exp(-E/T).
+// (src/spherical_harmonics.jl:572-603) to every even l.  Each launch also estimates
+// the energy gradient of every shell's rotation from its B candidates, which all
+// start from the same state: e_k = (1/B) sum_i ((dE_i - mean dE) / T) w_ik with w_ik
+// the candidate's whitened step noise (the Gaussian-smoothing estimator, E[dE w] =
+// sigma g to first order); the last kMlpGHist launches' e_k are network features.
+// TP3_MOVE_LEARNED draws a candidate from the mixture p * q_net + (1 - p) * q_iso,
+// where q_net takes the network's outputs (u_k, s_k) at the current state and draws
+// v_k = sigma (a m_k + exp(s_k - mean s) z_k) with a = +-1 equally likely and
+// m_k = sqrt(gamma) u_k / sqrt(sum |u|^2 + eps^2): a two-sided step along the
+// network's gradient estimate, whose density is symmetric in a.  The candidate is
+// accepted with the Metropolis-Hastings rule u < exp(-dE/T) q(x | x') / q(x' | x): the
+// reverse density evaluates the network at the proposed state x' for the step -v
+// (the rotation densities include the preimages |v| + 2 pi n of the exponential map).
+// The network's history inputs (the chain's recent dE/T and gradient estimates) and
+// the candidate's temperature are fixed parameters of the step, so every step is an
+// exact MH step for exp(-E/T).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -51,8 +58,11 @@
 namespace {
 
 using tp3::kFeatScale;
+using tp3::drift_factor;
+using tp3::kMlpGHist;
 using tp3::kMlpHist;
 using tp3::kMlpOutPad;
+using tp3::mlp_grad_feature;
 using tp3::mlp_head;
 using tp3::mlp_hist_feature;
 using tp3::mlp_temp_feature;
@@ -85,6 +95,7 @@ struct MoveMeta {  // one logged candidate of a per-shell move
   float comp;      // 1 = drawn from the network, 0 = isotropic
   float lr;        // log q(x | x') - log q(x' | x) (0 without the network)
   float sig;       // the candidate's isotropic step size sigma_i
+  float tgt;       // (dE - mean over the launch's candidates of dE) / T
 };
 
 __host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -261,6 +272,15 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
     double* sg = sigma + (size_t)c * nl;
     double sig_i = sg[0];  // sigma_0 / f^i of candidate i (per-shell moves)
     st.last = -1;
+    double dEmean = 0.0;
+    if (meta) {
+      int nf = 0;
+      for (int i = 0; i < B; ++i) {
+        const double d = Ecand[(size_t)c * B + i] - E0;
+        if (isfinite(d)) { dEmean += d; ++nf; }
+      }
+      dEmean = nf > 0 ? dEmean / nf : 0.0;
+    }
     for (int i = 0; i < B; ++i) {
       if (i > 0) sig_i /= f;
       const long long s = s0 + i;  // this step's index (0-based)
@@ -285,6 +305,7 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
         mm.comp = comp ? (float)comp[(size_t)c * B + i] : 0.f;
         mm.lr = lr ? (float)lr[(size_t)c * B + i] : 0.f;
         mm.sig = (float)sig_i;
+        mm.tgt = (float)((dE - dEmean) / T);
         meta[((size_t)(launch % meta_cap) * nch + c) * B + i] = mm;
       }
       if (st.last >= 0) continue;  // past the taken step: logged only
@@ -326,6 +347,7 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
 __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ coef, int src_per_chain, int nch, int nb,
                                                   int B, int K, int LMAX, int L, const ChainState* __restrict__ cs,
                                                   double decay, const float* __restrict__ hist,
+                                                  const float* __restrict__ ghist,
                                                   __nv_bfloat16* __restrict__ X, int xs,
                                                   __nv_bfloat16* __restrict__ logf,
                                                   const long long* __restrict__ launch_ctr, int log_cap) {
@@ -372,6 +394,10 @@ __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ co
     if (t < nf) v = sx[t] * scale;
     else if (t < nf + kMlpHist) v = mlp_hist_feature((double)hc[t - nf]);
     else if (t == nf + kMlpHist) v = tf;
+    else if (t < nf + kMlpHist + 1 + 3 * kMlpGHist) {
+      const int q = t - nf - kMlpHist - 1, lag = q / 3, d = q - 3 * lag;
+      v = mlp_grad_feature(ghist[(((size_t)c * kMlpGHist + lag) * K + k) * 3 + d]);
+    }
     const __nv_bfloat16 b = __float2bfloat16_rn(v);
     if (xr) xr[t] = b;
     if (lr) lr[t] = b;
@@ -379,9 +405,10 @@ __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ co
 }
 
 // The network proposes relative to the candidate's isotropic step size sigma_i: for
-// head outputs (mu^_k, s^_k) of the K shells, mu_k = sigma_i mu^_k and
-// s_k = log sigma_i + s^_k - mean_k s^_k, so the network sets how the step is shared
-// between shells and directions while the chain's adapted sigma sets its size.
+// head outputs (u_k, s^_k) of the K shells, the drift is m_k = sigma_i f u_k with
+// f = drift_factor(sum_k |u_k|^2) and the log-scale s_k = log sigma_i + s^_k - mean_k s^_k,
+// so the network sets the direction of the step and how its noise is shared between
+// shells and axes while the chain's adapted sigma sets its size.
 __device__ inline void shell_scale_mean(const double (*hs)[3], int K, double m[3]) {
   m[0] = m[1] = m[2] = 0.0;
   for (int k = 0; k < K; ++k)
@@ -389,23 +416,39 @@ __device__ inline void shell_scale_mean(const double (*hs)[3], int K, double m[3
   for (int d = 0; d < 3; ++d) m[d] /= K;
 }
 
-__device__ inline void shell_params(const double hmu[3], const double hs[3], const double m[3], double sg, double ls,
-                                    double mu[3], double s[3]) {
+__device__ inline double shell_drift_factor(const double (*hu)[3], int K) {
+  double uu = 0.0;
+  for (int k = 0; k < K; ++k)
+    for (int d = 0; d < 3; ++d) uu += hu[k][d] * hu[k][d];
+  return drift_factor(uu);
+}
+
+__device__ inline void shell_params(const double hu[3], const double hs[3], const double m[3], double sg, double df,
+                                    double ls, double mu[3], double s[3]) {
   for (int d = 0; d < 3; ++d) {
-    mu[d] = sg * hmu[d];
+    mu[d] = sg * df * hu[d];
     s[d] = ls + hs[d] - m[d];
   }
 }
 
+__device__ inline double logaddexp(double a, double b) {
+  const double m = a > b ? a : b;
+  if (m == -INFINITY) return m;
+  return m + log(exp(a - m) + exp(b - m));
+}
+
 // Per-shell proposal.  grid: nch * B (candidate (chain, i)); block 128.
 // O (nullable): raw network outputs at the current state, rows (chain, i, shell).
-// Writes the candidate's coefficients, its steps v [cand][K][3], the component drawn,
-// and lq[cand] = (log q_net(x'|x), log q_iso(x'|x)) summed over shells.
+// Writes the candidate's coefficients, its steps v [cand][K][3], its whitened step
+// noise w [cand][K][3] (float), the component drawn, and
+// lq[cand] = (log q(x'|x) of the network's drift +m, of -m, of the isotropic step),
+// each summed over shells.
 __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict__ state, double2* __restrict__ cand,
                                                        const ChainState* __restrict__ cs,
                                                        const double* __restrict__ sigma, int nl, int B, int K, int LMAX,
                                                        int L, double f, uint64_t seed, const float* __restrict__ O,
-                                                       double p_net, double* __restrict__ vout, int* __restrict__ comp,
+                                                       double p_net, double* __restrict__ vout,
+                                                       float* __restrict__ wout, int* __restrict__ comp,
                                                        double* __restrict__ lq, const double* __restrict__ delta,
                                                        const int* __restrict__ doff, float* __restrict__ vlog,
                                                        const long long* __restrict__ launch_ctr, int log_cap, int nch,
@@ -413,8 +456,8 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   __shared__ double2 xs[4][2 * tp3::kMaxRotL + 1], ys[4][2 * tp3::kMaxRotL + 1];
   if (rag) L = rag[blockIdx.x].L;
   __shared__ double eul[kMaxShells][3];
-  __shared__ double red[2][128];
-  __shared__ double hmu[kMaxShells][3], hs[kMaxShells][3];
+  __shared__ double red[3][128];
+  __shared__ double hu[kMaxShells][3], hs[kMaxShells][3];
   const int cid = blockIdx.x / B, i = blockIdx.x % B;
   const int ncoef = LMAX * LMAX;
   const double2* src = state + (size_t)cid * K * ncoef;
@@ -425,46 +468,54 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   uint32_t pc[4] = {(uint32_t)step, (uint32_t)cid, (uint32_t)kPurposeComponent, 0u};
   philox4x32_10(pc, (uint32_t)seed, (uint32_t)(seed >> 32));
   const bool use_net = O != nullptr && u01(pc[0]) < p_net;
+  const double a = u01(pc[1]) < 0.5 ? -1.0 : 1.0;  // side of the network's two-sided drift
   const double ls = log(sg);
-  double smean[3] = {0, 0, 0};
+  double smean[3] = {0, 0, 0}, df = 0.0;
   if (O) {
     for (int k = threadIdx.x; k < K; k += blockDim.x)
-      mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hmu[k], hs[k]);
+      mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hu[k], hs[k]);
     __syncthreads();
     shell_scale_mean(hs, K, smean);
+    df = shell_drift_factor(hu, K);
   }
-  double lnet = 0.0, liso = 0.0;
+  double lp = 0.0, lm = 0.0, liso = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double z[4];
     normals4(seed, step, cid, kPurposeShell, k, z);
-    double mu[3] = {0, 0, 0}, s[3], v[3];
-    if (O) shell_params(hmu[k], hs[k], smean, sg, ls, mu, s);
-    for (int d = 0; d < 3; ++d) v[d] = use_net ? mu[d] + exp(s[d]) * z[d] : sg * z[d];
+    double mu[3] = {0, 0, 0}, s[3] = {ls, ls, ls}, v[3], w[3];
+    if (O) shell_params(hu[k], hs[k], smean, sg, df, ls, mu, s);
+    for (int d = 0; d < 3; ++d) {
+      v[d] = use_net ? a * mu[d] + exp(s[d]) * z[d] : sg * z[d];
+      w[d] = use_net ? z[d] * exp(ls - s[d]) : z[d];
+    }
     const double si[3] = {ls, ls, ls}, zero[3] = {0, 0, 0};
     liso += rot_logdens(v, zero, si);
-    if (O) lnet += rot_logdens(v, mu, s);
+    if (O) {
+      const double mneg[3] = {-mu[0], -mu[1], -mu[2]};
+      lp += rot_logdens(v, mu, s);
+      lm += rot_logdens(v, mneg, s);
+    }
     double* vo = vout + ((size_t)blockIdx.x * K + k) * 3;
-    vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
+    float* wo = wout + ((size_t)blockIdx.x * K + k) * 3;
+    for (int d = 0; d < 3; ++d) { vo[d] = v[d]; wo[d] = (float)w[d]; }
     if (vlog) {
       float* vl = vlog + (((size_t)(*launch_ctr % log_cap) * nch * B + blockIdx.x) * K + k) * 3;
       vl[0] = (float)v[0]; vl[1] = (float)v[1]; vl[2] = (float)v[2];
     }
     tp3::axis_angle_euler(v[0], v[1], v[2], eul[k][0], eul[k][1], eul[k][2]);
   }
-  red[0][threadIdx.x] = lnet;
-  red[1][threadIdx.x] = liso;
+  red[0][threadIdx.x] = lp;
+  red[1][threadIdx.x] = lm;
+  red[2][threadIdx.x] = liso;
   for (int e = threadIdx.x; e < K * ncoef; e += blockDim.x) dst[e] = src[e];
   __syncthreads();
   for (int h = 64; h > 0; h >>= 1) {
-    if (threadIdx.x < h) {
-      red[0][threadIdx.x] += red[0][threadIdx.x + h];
-      red[1][threadIdx.x] += red[1][threadIdx.x + h];
-    }
+    if (threadIdx.x < h)
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    lq[(size_t)blockIdx.x * 2] = red[0][0];
-    lq[(size_t)blockIdx.x * 2 + 1] = red[1][0];
+    for (int q = 0; q < 3; ++q) lq[(size_t)blockIdx.x * 3 + q] = red[q][0];
     comp[blockIdx.x] = use_net ? 1 : 0;
   }
   // rotate every even l >= 2 of every shell (l = 0 is invariant)
@@ -477,47 +528,81 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   }
 }
 
-__device__ inline double logaddexp(double a, double b) {
-  const double m = a > b ? a : b;
-  if (m == -INFINITY) return m;
-  return m + log(exp(a - m) + exp(b - m));
-}
-
 // grid: nch * B; block 64.  O2: raw network outputs at the proposed states.
-// lr[cand] = log q(x | x') - log q(x' | x) for the mixture p q_net + (1 - p) q_iso.
+// lr[cand] = log q(x | x') - log q(x' | x) for the mixture p q_net + (1 - p) q_iso,
+// q_net = (q(. ; +m) + q(. ; -m)) / 2.
 __global__ void k_mh_ratio(const float* __restrict__ O2, const double* __restrict__ v, const double* __restrict__ lq,
                            int K, double p_net, const ChainState* __restrict__ cs, const double* __restrict__ sigma,
                            int nl, int B, double f, double* __restrict__ lr) {
-  __shared__ double red[64];
-  __shared__ double hmu[kMaxShells][3], hs[kMaxShells][3];
+  __shared__ double red[2][64];
+  __shared__ double hu[kMaxShells][3], hs[kMaxShells][3];
   const int cid = blockIdx.x / B, i = blockIdx.x % B;
   double sg = sigma[(size_t)cid * nl];
   for (int t = 0; t < i; ++t) sg /= f;
   const double ls = log(sg);
   for (int k = threadIdx.x; k < K; k += blockDim.x)
-    mlp_head(O2 + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hmu[k], hs[k]);
+    mlp_head(O2 + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hu[k], hs[k]);
   __syncthreads();
   double smean[3];
   shell_scale_mean(hs, K, smean);
-  double acc = 0.0;
+  const double df = shell_drift_factor(hu, K);
+  double rp = 0.0, rm = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double mu[3], s[3];
-    shell_params(hmu[k], hs[k], smean, sg, ls, mu, s);
+    shell_params(hu[k], hs[k], smean, sg, df, ls, mu, s);
     const double* vk = v + ((size_t)blockIdx.x * K + k) * 3;
     const double rv[3] = {-vk[0], -vk[1], -vk[2]};
-    acc += rot_logdens(rv, mu, s);
+    const double mneg[3] = {-mu[0], -mu[1], -mu[2]};
+    rp += rot_logdens(rv, mu, s);
+    rm += rot_logdens(rv, mneg, s);
   }
-  red[threadIdx.x] = acc;
+  red[0][threadIdx.x] = rp;
+  red[1][threadIdx.x] = rm;
   __syncthreads();
   for (int h = 32; h > 0; h >>= 1) {
-    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    if (threadIdx.x < h) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + h];
+      red[1][threadIdx.x] += red[1][threadIdx.x + h];
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double fnet = lq[(size_t)blockIdx.x * 2], fiso = lq[(size_t)blockIdx.x * 2 + 1], rnet = red[0];
+    const double* q = lq + (size_t)blockIdx.x * 3;
+    const double ln2 = 0.6931471805599453;
+    const double fnet = logaddexp(q[0], q[1]) - ln2, fiso = q[2];
+    const double rnet = logaddexp(red[0][0], red[1][0]) - ln2;
     const double lp = log(p_net), lq1 = p_net < 1.0 ? log1p(-p_net) : -INFINITY;
     // the isotropic density is symmetric: q_iso(x | x') = q_iso(x' | x)
     lr[blockIdx.x] = logaddexp(lp + rnet, lq1 + fiso) - logaddexp(lp + fnet, lq1 + fiso);
+  }
+}
+
+// Gradient estimate of the launch from its B candidates (all drawn at the chain's
+// start state): e_k = (1/n) sum_i ((dE_i - mean dE) / T1) w_ik over the n candidates
+// with a finite energy, T1 = the first candidate's temperature; shifted into the
+// chain's history ghist [nch][kMlpGHist][K][3] (newest first).  Runs before k_select
+// (reads the start energy and temperature).  grid: nch; block 128.
+__global__ void k_grad_hist(const ChainState* __restrict__ cs, const double* __restrict__ Ecand,
+                            const float* __restrict__ w, int B, int K, double decay, float* __restrict__ ghist) {
+  const int c = blockIdx.x;
+  const double E0 = cs[c].E, T1 = cs[c].T * decay;
+  double mean = 0.0;
+  int nf = 0;
+  for (int i = 0; i < B; ++i) {
+    const double d = Ecand[(size_t)c * B + i] - E0;
+    if (isfinite(d)) { mean += d; ++nf; }
+  }
+  mean = nf > 0 ? mean / nf : 0.0;
+  float* g = ghist + (size_t)c * kMlpGHist * K * 3;
+  for (int q = threadIdx.x; q < K * 3; q += blockDim.x) {
+    double e = 0.0;
+    for (int i = 0; i < B; ++i) {
+      const double d = Ecand[(size_t)c * B + i] - E0;
+      if (isfinite(d)) e += (d - mean) * (double)w[((size_t)c * B + i) * K * 3 + q];
+    }
+    e = nf > 0 ? e / (nf * T1) : 0.0;
+    for (int t = kMlpGHist - 1; t > 0; --t) g[(size_t)t * K * 3 + q] = g[(size_t)(t - 1) * K * 3 + q];
+    g[q] = (float)e;
   }
 }
 
@@ -542,12 +627,8 @@ __global__ void k_log_gather(const long long* __restrict__ idx, int K, int nch, 
   for (int t = threadIdx.x; t < xs; t += blockDim.x) X[(size_t)row * xs + t] = t == tcol ? tb : f[t];
   if (threadIdx.x < 3) V[(size_t)row * 3 + threadIdx.x] = vlog[((size_t)pos * K + k) * 3 + threadIdx.x] / mm.sig;
   if (k == 0 && threadIdx.x == 0) {
-    M[(size_t)j * 6 + 0] = mm.dE;
-    M[(size_t)j * 6 + 1] = mm.T;
-    M[(size_t)j * 6 + 2] = mm.acc;
-    M[(size_t)j * 6 + 3] = mm.comp;
-    M[(size_t)j * 6 + 4] = mm.lr;
-    M[(size_t)j * 6 + 5] = mm.sig;
+    float* mr = M + (size_t)j * 7;
+    mr[0] = mm.dE; mr[1] = mm.T; mr[2] = mm.acc; mr[3] = mm.comp; mr[4] = mm.lr; mr[5] = mm.sig; mr[6] = mm.tgt;
   }
 }
 
@@ -578,6 +659,7 @@ struct tp3_chains {
   double* d_sigma = nullptr;
   LogRow* d_log = nullptr;
   float* d_hist = nullptr;      // [nch][kMlpHist] dE/T history, newest last
+  float* d_ghist = nullptr;     // [nch][kMlpGHist][K][3] per-shell gradient estimates, newest first
   tp3::RagInfo* d_rag = nullptr;  // [nch*B] per-candidate limits of ragged chains (null: the context's shape)
   int* d_lkh = nullptr;           // [nch*B][3] (L, K, histogram) per candidate
   cudaGraph_t graph = nullptr;
@@ -590,7 +672,8 @@ struct tp3_chains {
   double p_net = 0.0;
   tp3_mlp* net = nullptr;
   double* d_v = nullptr;        // [nch*B][K][3] axis-angle steps
-  double* d_lq = nullptr;       // [nch*B][2] forward log densities (network, isotropic)
+  double* d_lq = nullptr;       // [nch*B][3] forward log densities (network +m, -m, isotropic)
+  float* d_w = nullptr;         // [nch*B][K][3] whitened step noise
   double* d_lr = nullptr;       // [nch*B] log q(x|x') - log q(x'|x)
   int* d_comp = nullptr;        // [nch*B] component drawn
   // move log (training data): ring of mlog_cap launches
@@ -608,7 +691,7 @@ void chains_free(tp3_chains* h) {
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   cudaFree(h->d_state); cudaFree(h->d_cand); cudaFree(h->d_Ecand); cudaFree(h->d_cs); cudaFree(h->d_sigma);
-  cudaFree(h->d_log); cudaFree(h->d_hist); cudaFree(h->d_v); cudaFree(h->d_lq); cudaFree(h->d_lr); cudaFree(h->d_comp);
+  cudaFree(h->d_log); cudaFree(h->d_hist); cudaFree(h->d_ghist); cudaFree(h->d_w); cudaFree(h->d_v); cudaFree(h->d_lq); cudaFree(h->d_lr); cudaFree(h->d_comp);
   cudaFree(h->d_launch); cudaFree(h->d_lfeat); cudaFree(h->d_lv); cudaFree(h->d_lmeta);
   cudaFree(h->d_rag); cudaFree(h->d_lkh);
 }
@@ -630,19 +713,21 @@ int chains_enqueue(tp3_chains* h) {
     __nv_bfloat16* X = net ? tp3::mlp_input(h->net) : nullptr;
     if (net || mlog)
       k_features<<<h->nch * (net ? h->B : 1) * h->K, 128, 0, c->stream>>>(
-          h->d_state, 1, h->nch, net ? h->B : 1, h->B, h->K, h->LMAX, h->L, h->d_cs, h->decay, h->d_hist, X, h->xs,
-          mlog ? h->d_lfeat : nullptr, lctr, h->mlog_cap);
+          h->d_state, 1, h->nch, net ? h->B : 1, h->B, h->K, h->LMAX, h->L, h->d_cs, h->decay, h->d_hist, h->d_ghist,
+          X, h->xs, mlog ? h->d_lfeat : nullptr, lctr, h->mlog_cap);
     if (net) {
       if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
     }
     k_propose_shell<<<n, 128, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX,
-                                              h->L, h->f, h->seed, O, h->p_net, h->d_v, h->d_comp, h->d_lq, c->d_delta,
+                                              h->L, h->f, h->seed, O, h->p_net, h->d_v, h->d_w, h->d_comp, h->d_lq,
+                                              c->d_delta,
                                               c->d_doff, mlog ? h->d_lv : nullptr, lctr, h->mlog_cap, h->nch,
                                               h->d_rag);
     if (net) {
       k_features<<<n * h->K, 128, 0, c->stream>>>(h->d_cand, 0, h->nch, h->B, h->B, h->K, h->LMAX, h->L, h->d_cs,
-                                                   h->decay, h->d_hist, X, h->xs, nullptr, lctr, h->mlog_cap);
+                                                   h->decay, h->d_hist, h->d_ghist, X, h->xs, nullptr, lctr,
+                                                   h->mlog_cap);
       if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
       k_mh_ratio<<<n, 64, 0, c->stream>>>(O, h->d_v, h->d_lq, h->K, h->p_net, h->d_cs, h->d_sigma, h->nl, h->B, h->f,
@@ -652,6 +737,7 @@ int chains_enqueue(tp3_chains* h) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "propose");
   if (int r = tp3::ctx_run_energy(c, n, h->d_cand, h->d_Ecand, h->d_rag)) return r;
+  if (shell) k_grad_hist<<<h->nch, 128, 0, c->stream>>>(h->d_cs, h->d_Ecand, h->d_w, h->B, h->K, h->decay, h->d_ghist);
   k_select<<<(h->nch + 127) / 128, 128, 0, c->stream>>>(
       h->d_cs, h->d_sigma, h->d_Ecand, h->nch, h->nl, h->B, h->f, h->decay, h->seed, h->d_log, h->logcap,
       shell ? 0 : h->nl - 1, net ? h->d_lr : nullptr, h->d_hist, shell ? h->d_comp : nullptr,
@@ -741,6 +827,8 @@ static int chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coe
       (e = cudaMalloc(&h->d_sigma, (size_t)nchains * h->nl * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_hist, (size_t)nchains * kMlpHist * sizeof(float))) != cudaSuccess ||
       (e = cudaMemset(h->d_hist, 0, (size_t)nchains * kMlpHist * sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_ghist, (size_t)nchains * kMlpGHist * h->K * 3 * sizeof(float))) != cudaSuccess ||
+      (e = cudaMemset(h->d_ghist, 0, (size_t)nchains * kMlpGHist * h->K * 3 * sizeof(float))) != cudaSuccess ||
       (log_capacity > 0 && (e = cudaMalloc(&h->d_log, (size_t)nchains * log_capacity * sizeof(LogRow))) != cudaSuccess)) {
     chains_free(h);
     delete h;
@@ -894,8 +982,9 @@ int tp3_chains_snapshot(tp3_chains* h, void* buf, size_t capacity, size_t* bytes
   const size_t ncs = (size_t)h->nch * sizeof(ChainState);
   const size_t nsg = (size_t)h->nch * h->nl * sizeof(double);
   const size_t nhs = (size_t)h->nch * kMlpHist * sizeof(float);
+  const size_t ngh = (size_t)h->nch * kMlpGHist * h->K * 3 * sizeof(float);
   const size_t hdr = 8 * sizeof(int64_t);
-  const size_t need = hdr + nst + ncs + nsg + nhs;
+  const size_t need = hdr + nst + ncs + nsg + nhs + ngh;
   *bytes = need;
   if (!buf) return TP3_OK;
   if (capacity < need) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot buffer too small");
@@ -909,7 +998,8 @@ int tp3_chains_snapshot(tp3_chains* h, void* buf, size_t capacity, size_t* bytes
   if ((e = cudaMemcpy(p + hdr, h->d_state, nst, cudaMemcpyDeviceToHost)) != cudaSuccess ||
       (e = cudaMemcpy(p + hdr + nst, h->d_cs, ncs, cudaMemcpyDeviceToHost)) != cudaSuccess ||
       (e = cudaMemcpy(p + hdr + nst + ncs, h->d_sigma, nsg, cudaMemcpyDeviceToHost)) != cudaSuccess ||
-      (e = cudaMemcpy(p + hdr + nst + ncs + nsg, h->d_hist, nhs, cudaMemcpyDeviceToHost)) != cudaSuccess)
+      (e = cudaMemcpy(p + hdr + nst + ncs + nsg, h->d_hist, nhs, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(p + hdr + nst + ncs + nsg + nhs, h->d_ghist, ngh, cudaMemcpyDeviceToHost)) != cudaSuccess)
     return tp3::ctx_cuda_fail(c, e, "snapshot copy");
   return TP3_OK;
 }
@@ -922,8 +1012,9 @@ int tp3_chains_restore(tp3_chains* h, const void* buf, size_t bytes) {
   const size_t ncs = (size_t)h->nch * sizeof(ChainState);
   const size_t nsg = (size_t)h->nch * h->nl * sizeof(double);
   const size_t nhs = (size_t)h->nch * kMlpHist * sizeof(float);
+  const size_t ngh = (size_t)h->nch * kMlpGHist * h->K * 3 * sizeof(float);
   const size_t hdr = 8 * sizeof(int64_t);
-  if (bytes != hdr + nst + ncs + nsg + nhs) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot size does not match these chains");
+  if (bytes != hdr + nst + ncs + nsg + nhs + ngh) return tp3::ctx_fail(c, TP3_ERR_ARG, "snapshot size does not match these chains");
   int64_t head[8];
   std::memcpy(head, buf, hdr);
   double f, decay;
@@ -938,6 +1029,7 @@ int tp3_chains_restore(tp3_chains* h, const void* buf, size_t bytes) {
   if (e == cudaSuccess) e = cudaMemcpy(h->d_cs, p + hdr + nst, ncs, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(h->d_sigma, p + hdr + nst + ncs, nsg, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(h->d_hist, p + hdr + nst + ncs + nsg, nhs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_ghist, p + hdr + nst + ncs + nsg + nhs, ngh, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "restore copy");
   return TP3_OK;
 }
@@ -956,7 +1048,8 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
     if (int r = tp3::ctx_ensure_rot_tables(c, h->L)) return r;
     const size_t nc = (size_t)h->nch * h->B;
     if (!h->d_v && ((e = cudaMalloc(&h->d_v, nc * h->K * 3 * sizeof(double))) != cudaSuccess ||
-                    (e = cudaMalloc(&h->d_lq, nc * 2 * sizeof(double))) != cudaSuccess ||
+                    (e = cudaMalloc(&h->d_lq, nc * 3 * sizeof(double))) != cudaSuccess ||
+                    (e = cudaMalloc(&h->d_w, nc * h->K * 3 * sizeof(float))) != cudaSuccess ||
                     (e = cudaMalloc(&h->d_lr, nc * sizeof(double))) != cudaSuccess ||
                     (e = cudaMalloc(&h->d_comp, nc * sizeof(int))) != cudaSuccess)) {
       cudaGetLastError();
@@ -970,7 +1063,7 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
     if (!net) return tp3::ctx_fail(c, TP3_ERR_ARG, "learned moves need a network");
     if (!(p_net > 0.0 && p_net <= 1.0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "p_net must be in (0, 1]");
     if (tp3::mlp_n_in_of(net) != tp3::mlp_n_in(h->L))
-      return tp3::ctx_fail(c, TP3_ERR_ARG, "network input width is not (L+1)^2 + 9");
+      return tp3::ctx_fail(c, TP3_ERR_ARG, "network input width is not (L+1)^2 + 33");
     if (tp3::mlp_max_rows(net) < h->nch * h->B * h->K)
       return tp3::ctx_fail(c, TP3_ERR_ARG, "network max_rows < chains x candidates x shells");
   }

@@ -59,7 +59,7 @@ struct PairBlock {
   int lt_base;             // l-triple index of (l1, l2, l3min); the block's l-triples are consecutive
   int wofs;                // offset of the block in wtab (16-byte aligned)
   int eofs;                // offset of the block's per-m3 table in eofs[]
-  int nl3p;                // nl3 rounded up to 4 (row length of the 3j table)
+  int nl3p;                // nl3 rounded up to 2 (row length of the 3j table: whole float2s)
   int wcount;              // floats in the block's 3j table (multiple of 4)
 };
 

@@ -251,29 +251,62 @@ __global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ X, int R, int
   }
 }
 
-// Weighted Gaussian NLL of the logged axis-angle steps and its gradient wrt the raw
-// outputs.  grid ceil(R/128), block 128.  dO [R][16] bf16 and dOt [16][ldt] bf16
-// (columns / rows 6..15 zero); part[block] = sum of w NLL over the block.
+// Regression of the logged energy changes on the steps: for candidate j (rows
+// jK..jK+K-1, one per shell) r_j = t_j - sum_k u_k . V_k with (t_j, lambda_j) = tw[j],
+// V = v / sigma the logged step; resid[j] = lambda_j r_j, part[block] = sum of
+// lambda_j r_j^2 / 2.  grid ceil(nc / 128), block 128.
+__global__ void k_reg_residual(const float* __restrict__ O, const float* __restrict__ V,
+                               const float2* __restrict__ tw, int K, int nc, float* __restrict__ resid,
+                               double* __restrict__ part) {
+  __shared__ double red[128];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double l = 0.0;
+  if (j < nc) {
+    double p = 0.0;
+    for (int k = 0; k < K; ++k) {
+      const size_t r = (size_t)j * K + k;
+      for (int d = 0; d < 3; ++d) p += (double)O[r * kMlpOutPad + d] * (double)V[r * 3 + d];
+    }
+    const float2 t = tw[j];
+    const double res = (double)t.x - p;
+    resid[j] = (float)((double)t.y * res);
+    l = 0.5 * (double)t.y * res * res;
+  }
+  red[threadIdx.x] = l;
+  __syncthreads();
+  for (int h = 64; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Gradient of the loss wrt the raw outputs: the regression term on u (resid
+// nullable: none) and the weighted zero-mean Gaussian NLL of the logged steps V on
+// the log-scales s, sum_d w [s_d + V_d^2 exp(-2 s_d) / 2 + log(2 pi) / 2].
+// grid ceil(R/128), block 128.  dO [R][16] bf16 and dOt [16][ldt] bf16 (columns /
+// rows 6..15 zero); part[block] = sum of w NLL over the block.
 __global__ void k_head_loss(const float* __restrict__ O, int R, const float* __restrict__ vlog,
-                            const float* __restrict__ w, __nv_bfloat16* __restrict__ dO, __nv_bfloat16* __restrict__ dOt,
-                            int ldt, double* __restrict__ part) {
+                            const float* __restrict__ w, const float* __restrict__ resid, int K, int nc,
+                            __nv_bfloat16* __restrict__ dO, __nv_bfloat16* __restrict__ dOt, int ldt,
+                            double* __restrict__ part) {
   __shared__ double red[128];
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   double nll = 0.0;
   if (r < R) {
     const float* o = O + (size_t)r * kMlpOutPad;
     const double wr = w[r];
+    const double rj = (resid && r / K < nc) ? (double)resid[r / K] : 0.0;
     float g[kMlpOutPad];
     for (int j = 0; j < kMlpOutPad; ++j) g[j] = 0.f;
     for (int d = 0; d < 3; ++d) {
-      const double tm = tanh((double)o[d]), ts = tanh((double)o[3 + d]);
-      const double mu = kMuScale * tm, s = kSMid + kSHalf * ts;
-      const double e = (double)vlog[(size_t)r * 3 + d] - mu;
+      const double ts = tanh((double)o[3 + d]);
+      const double s = kSMid + kSHalf * ts;
+      const double e = (double)vlog[(size_t)r * 3 + d];
       const double is2 = exp(-2.0 * s);
       nll += s + 0.5 * e * e * is2 + 0.9189385332046727;  // 0.5 log(2 pi)
-      const double dmu = -e * is2, ds = 1.0 - e * e * is2;
-      g[d] = (float)(wr * dmu * kMuScale * (1.0 - tm * tm));
-      g[3 + d] = (float)(wr * ds * kSHalf * (1.0 - ts * ts));
+      g[d] = (float)(-rj * e);
+      g[3 + d] = (float)(wr * (1.0 - e * e * is2) * kSHalf * (1.0 - ts * ts));
     }
     nll *= wr;
     for (int j = 0; j < kMlpOutPad; ++j) {
@@ -329,14 +362,14 @@ __global__ void k_pack_weights(const float* __restrict__ W, int out, int in, __n
   if (Wt) Wt[(size_t)k * ldt + o] = b;
 }
 
-// raw outputs -> (mu, s) rows of 6; grid ceil(R/128), block 128
+// raw outputs -> (u, s) rows of 6; grid ceil(R/128), block 128
 __global__ void k_head_map(const float* __restrict__ O, int R, float* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
-  double mu[3], s[3];
-  mlp_head(O + (size_t)r * kMlpOutPad, mu, s);
+  double u[3], s[3];
+  mlp_head(O + (size_t)r * kMlpOutPad, u, s);
   for (int d = 0; d < 3; ++d) {
-    out[(size_t)r * 6 + d] = (float)mu[d];
+    out[(size_t)r * 6 + d] = (float)u[d];
     out[(size_t)r * 6 + 3 + d] = (float)s[d];
   }
 }
@@ -371,7 +404,8 @@ struct tp3_mlp {
   float* O = nullptr;                            // [max_rows][16]
   __nv_bfloat16 *dO = nullptr, *dOt = nullptr;   // [max_rows][16], [16][max_rows]
   __nv_bfloat16 *P = nullptr, *Q = nullptr, *Tt = nullptr;  // [max_rows][H] x2, [H][max_rows]
-  double* d_part = nullptr;                      // loss partials [max_rows / 128]
+  double* d_part = nullptr;                      // loss partials [2][max_rows / 128] (NLL, regression)
+  float* d_resid = nullptr;                      // weighted regression residual per candidate [max_rows]
   int* d_err = nullptr;
   // tensor maps: forward F1..F4, backward B1..B7
   CUtensorMap fA[4], fB[4], bA[7], bB[7];
@@ -417,7 +451,7 @@ GemmArgs args(int M, int N, int K) {
 void mlp_free(tp3_mlp* n) {
   void* ps[] = {n->d_par, n->d_grad, n->d_m, n->d_v, n->W1, n->W2, n->W3, n->W4, n->W2t, n->W3t, n->W4t, n->X, n->Xt,
                 n->Hh[0], n->Hh[1], n->Hh[2], n->Ht[0], n->Ht[1], n->Ht[2], n->O, n->dO, n->dOt, n->P, n->Q, n->Tt,
-                n->d_part, n->d_err};
+                n->d_part, n->d_resid, n->d_err};
   for (void* p : ps) cudaFree(p);
 }
 
@@ -455,14 +489,21 @@ cudaError_t forward(tp3_mlp* n, int R, bool with_t) {
   return gemm(n, n->fA[3], n->fB[3], g);
 }
 
-// loss and gradient into d_grad for rows [0, R), R a multiple of 128
-cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w) {
+// loss and gradient into d_grad for rows [0, R), R a multiple of 128; tw (nullable):
+// per-candidate regression targets and weights of candidates of K rows each
+cudaError_t backward(tp3_mlp* n, int R, const float* v, const float* w, const float* tw, int K) {
   cudaError_t e;
   cudaStream_t s = n->ctx->stream;
   const int H = n->H, MR = n->max_rows;
   dim3 tg((n->n_in_pad + 31) / 32, (R + 31) / 32), tb(32, 8);
   k_transpose_bf16<<<tg, tb, 0, s>>>(n->X, R, n->n_in_pad, n->n_in_pad, n->Xt, MR);
-  k_head_loss<<<R / 128, 128, 0, s>>>(n->O, R, v, w, n->dO, n->dOt, MR, n->d_part);
+  const int nc = R / K;
+  if (tw) {
+    k_reg_residual<<<(nc + 127) / 128, 128, 0, s>>>(n->O, v, reinterpret_cast<const float2*>(tw), K, nc, n->d_resid,
+                                                   n->d_part + MR / 128);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  k_head_loss<<<R / 128, 128, 0, s>>>(n->O, R, v, w, tw ? n->d_resid : nullptr, K, nc, n->dO, n->dOt, MR, n->d_part);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   float* gW[4];
   float* gb[4];
@@ -584,7 +625,8 @@ int tp3_mlp_create(tp3_ctx* c, int n_in, int hidden, int max_rows, uint64_t seed
   A((void**)&n->O, (size_t)MR * tp3::kMlpOutPad * 4);
   A((void**)&n->dO, (size_t)MR * tp3::kMlpOutPad * bf); A((void**)&n->dOt, (size_t)tp3::kMlpOutPad * MR * bf);
   A((void**)&n->P, (size_t)MR * H * bf); A((void**)&n->Q, (size_t)MR * H * bf); A((void**)&n->Tt, (size_t)H * MR * bf);
-  A((void**)&n->d_part, (size_t)(MR / 128) * sizeof(double)); A((void**)&n->d_err, sizeof(int));
+  A((void**)&n->d_part, (size_t)(2 * MR / 128) * sizeof(double)); A((void**)&n->d_err, sizeof(int));
+  A((void**)&n->d_resid, (size_t)MR * sizeof(float));
   if (e != cudaSuccess) {
     tp3::mlp_free(n);
     delete n;
@@ -702,36 +744,42 @@ int tp3_mlp_forward_device(tp3_mlp* n, int rows, const void* d_x, void* d_out) {
   return TP3_OK;
 }
 
-static int mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w, double* loss) {
+static int mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w,
+                         const float* d_target, int shells, double* loss) {
   tp3_ctx* c = n->ctx;
   if (rows % 128 != 0) return tp3::ctx_fail(c, TP3_ERR_ARG, "training rows must be a multiple of 128");
-  if (!d_v || !d_w) return tp3::ctx_fail(c, TP3_ERR_ARG, "NULL targets or weights");
+  if (!d_v || !d_w) return tp3::ctx_fail(c, TP3_ERR_ARG, "NULL steps or weights");
+  if (shells < 1 || shells > rows) return tp3::ctx_fail(c, TP3_ERR_ARG, "shells per candidate out of range");
   if (int r = mlp_load_input(n, rows, d_x)) return r;
   cudaError_t e = cudaMemsetAsync(n->d_err, 0, sizeof(int), c->stream);
   if (e == cudaSuccess) e = tp3::forward(n, rows, true);
-  if (e == cudaSuccess) e = tp3::backward(n, rows, d_v, d_w);
+  if (e == cudaSuccess) e = tp3::backward(n, rows, d_v, d_w, d_target, shells);
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "mlp backward");
   if (loss) {
-    std::vector<double> part(rows / 128);
+    const int nb = rows / 128, nr = d_target ? (rows / shells + 127) / 128 : 0;
+    std::vector<double> part(nb), rpart(nr > 0 ? nr : 1);
     int err = 0;
-    if ((e = cudaMemcpyAsync(part.data(), n->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream)) !=
+    if ((e = cudaMemcpyAsync(part.data(), n->d_part, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream)) !=
             cudaSuccess ||
+        (nr > 0 && (e = cudaMemcpyAsync(rpart.data(), n->d_part + n->max_rows / 128, nr * sizeof(double),
+                                        cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) ||
         (e = cudaMemcpyAsync(&err, n->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
       return tp3::ctx_cuda_fail(c, e, "mlp loss read");
     if (err) return tp3::ctx_fail(c, err, "a bounded wait in the mlp GEMM ran out");
-    double s = 0.0;
-    for (double p : part) s += p;
-    *loss = s;
+    double sum = 0.0;
+    for (double p : part) sum += p;
+    for (int b = 0; b < nr; ++b) sum += rpart[b];
+    *loss = sum;
   }
   return TP3_OK;
 }
 
-int tp3_mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w, double* loss,
-                      float* grad_host) {
+int tp3_mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w,
+                      const float* d_target, int shells, double* loss, float* grad_host) {
   if (!n) return TP3_ERR_ARG;
   double l = 0.0;
-  if (int r = mlp_loss_grad(n, rows, d_x, d_v, d_w, &l)) return r;
+  if (int r = mlp_loss_grad(n, rows, d_x, d_v, d_w, d_target, shells, &l)) return r;
   if (loss) *loss = l;
   if (grad_host) {
     tp3_ctx* c = n->ctx;
@@ -742,10 +790,10 @@ int tp3_mlp_loss_grad(tp3_mlp* n, int rows, const void* d_x, const float* d_v, c
   return TP3_OK;
 }
 
-int tp3_mlp_train_step(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w, float lr,
-                       double* loss) {
+int tp3_mlp_train_step(tp3_mlp* n, int rows, const void* d_x, const float* d_v, const float* d_w,
+                       const float* d_target, int shells, float lr, double* loss) {
   if (!n) return TP3_ERR_ARG;
-  if (int r = mlp_loss_grad(n, rows, d_x, d_v, d_w, loss)) return r;
+  if (int r = mlp_loss_grad(n, rows, d_x, d_v, d_w, d_target, shells, loss)) return r;
   tp3_ctx* c = n->ctx;
   n->adam_t += 1;
   const float b1 = 0.9f, b2 = 0.999f;

@@ -1,11 +1,13 @@
 // Learned proposal network: constants and device helpers shared by the network
 // (mlp.cu) and the chain moves that sample from it (chains.cu).
 //
-// Per shell the network maps a feature row to the mean mu and log-scale s of a
-// Gaussian axis-angle step v ~ N(mu, diag(exp(2 s))):
-//     mu_d = kMuScale * tanh(o_d),  s_d = kSMid + kSHalf * tanh(o_{3+d}),  d = 0..2
-// from the raw outputs o of the last layer, so |mu| < 0.5 rad and
-// exp(s) lies in (9e-4, 2.7) rad.
+// Per shell the network maps a feature row to a drift direction u (3) and a
+// log-scale s (3) of the shell's axis-angle step, from the raw outputs o of the
+// last layer:
+//     u_d = o_d,  s_d = kSMid + kSHalf * tanh(o_{3+d}),  d = 0..2
+// so exp(s) lies in (9e-4, 2.7).  u estimates sigma g_k / T (g_k: the energy
+// gradient of a rotation of shell k, sigma: the isotropic step size, T: the
+// temperature); the proposal steps along +-u (both signs equally likely).
 //
 // Feature row of shell k of a state (kMlpInPad bf16 columns):
 //   [0, (L+1)^2)            real SH coefficients x_lm (l = 0..L, u = -l..l; x = U c,
@@ -13,6 +15,8 @@
 //                           the shell's norm and multiplied by kFeatScale
 //   [(L+1)^2, +8)           the chain's last 8 values of dE / T, clipped to +-10, / 10
 //   [(L+1)^2 + 8]           log10(T) / 4 of the candidate's temperature
+//   [(L+1)^2 + 9, +24)      the shell's gradient estimates of the chain's last 8
+//                           launches (3 each, newest first), clipped to +-8, / 2
 //   rest                    zero
 #pragma once
 #include <cuda_runtime.h>
@@ -22,14 +26,18 @@
 namespace tp3 {
 
 constexpr int kMlpHist = 8;         // history values per chain
-constexpr int kMlpOut = 6;          // mu (3), s (3)
+constexpr int kMlpGHist = 8;        // launches of per-shell gradient estimates in a feature row
+constexpr int kMlpOut = 6;          // u (3), s (3)
 constexpr int kMlpOutPad = 16;      // last layer padded to the smallest MMA N
-constexpr double kMuScale = 0.5;
 constexpr double kSMid = -3.0;
 constexpr double kSHalf = 4.0;
 constexpr float kFeatScale = 8.0f;
+// drift of a network step: a sqrt(kDriftGamma) u / sqrt(|u|^2 + kDriftEps^2) in units of
+// sigma, a = +-1, |u|^2 summed over the candidate's shells
+constexpr double kDriftGamma = 16.0;
+constexpr double kDriftEps = 0.1;
 
-__host__ __device__ inline int mlp_n_in(int L) { return (L + 1) * (L + 1) + kMlpHist + 1; }
+__host__ __device__ inline int mlp_n_in(int L) { return (L + 1) * (L + 1) + kMlpHist + 1 + 3 * kMlpGHist; }
 __host__ __device__ inline int mlp_n_in_pad(int L) { return (mlp_n_in(L) + 31) / 32 * 32; }
 
 __host__ __device__ inline float mlp_hist_feature(double dE_over_T) {
@@ -40,6 +48,13 @@ __host__ __device__ inline float mlp_hist_feature(double dE_over_T) {
 }
 
 __host__ __device__ inline float mlp_temp_feature(double T) { return (float)(log10(T > 1e-300 ? T : 1e-300) / 4.0); }
+
+__host__ __device__ inline float mlp_grad_feature(float e) {
+  float x = e;
+  if (!(x == x)) x = 0.f;
+  x = x > 8.f ? 8.f : (x < -8.f ? -8.f : x);
+  return 0.5f * x;
+}
 
 // log of the density of the rotation exp([v]x) under the axis-angle Gaussian
 // N(mu, diag(exp(2 s))), up to the Haar factor 1 / (2 (1 - cos|v|)) that is common to
@@ -69,11 +84,17 @@ __host__ __device__ inline double rot_logdens(const double v[3], const double mu
   return mx + log(acc);
 }
 
-__host__ __device__ inline void mlp_head(const float* o, double mu[3], double s[3]) {
+__host__ __device__ inline void mlp_head(const float* o, double u[3], double s[3]) {
   for (int d = 0; d < 3; ++d) {
-    mu[d] = kMuScale * tanh((double)o[d]);
+    u[d] = (double)o[d];
     s[d] = kSMid + kSHalf * tanh((double)o[3 + d]);
   }
+}
+
+// drift factor sqrt(gamma) / sqrt(|u|^2 + eps^2) of a candidate whose shells' u have
+// squared norm uu
+__host__ __device__ inline double drift_factor(double uu) {
+  return sqrt(kDriftGamma) / sqrt(uu + kDriftEps * kDriftEps);
 }
 
 }  // namespace tp3

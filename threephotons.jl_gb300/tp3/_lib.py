@@ -93,8 +93,10 @@ SIGNATURES = {
     "tp3_mlp_set_params": (c_int, [c_void_p, c_void_p, c_int64]),
     "tp3_mlp_input_buffer": (c_int, [c_void_p, P(c_void_p), P(c_int)]),
     "tp3_mlp_forward_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
-    "tp3_mlp_loss_grad": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, P(c_double), c_void_p]),
-    "tp3_mlp_train_step": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, ctypes.c_float, P(c_double)]),
+    "tp3_mlp_loss_grad": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, P(c_double),
+                                  c_void_p]),
+    "tp3_mlp_train_step": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.c_float,
+                                   P(c_double)]),
     "tp3_selftest_timeout": (c_int, [c_void_p, ctypes.c_longlong]),
     "tp3_profile_enable": (c_int, [c_void_p, c_int]),
     "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),

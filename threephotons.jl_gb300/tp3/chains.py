@@ -132,7 +132,8 @@ class Chains:
 
     def move_log_gather(self, n: int, d_idx: int, d_x: int, d_v: int, d_meta: int) -> None:
         """Device pointers: idx int64[n]; x bf16[n*K][stride]; v float[n*K][3] (steps / sigma_i);
-        meta float[n][6] (dE, T, accepted, drawn-from-network, log MH ratio, sigma_i)."""
+        meta float[n][7] (dE, T, accepted, drawn-from-network, log MH ratio, sigma_i,
+        (dE - mean dE over the launch's candidates) / T)."""
         check(self._lib.tp3_chains_move_log_gather(self._h, n, ctypes.c_void_p(d_idx), ctypes.c_void_p(d_x),
                                                    ctypes.c_void_p(d_v), ctypes.c_void_p(d_meta)), self.basis.ctx)
 
@@ -144,7 +145,10 @@ class Chains:
 
     def close(self) -> None:
         if self._h:
-            self._lib.tp3_chains_destroy(self._h)
+            # chains live on their context: when it is already gone (both collected
+            # together at interpreter exit) the handle is dropped, not freed
+            if getattr(self.basis, "_ctx", None):
+                self._lib.tp3_chains_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -17,8 +17,9 @@ from ._lib import TP3Error, check, load
 
 
 def n_in_for(L: int) -> int:
-    """Feature width per shell: (L+1)^2 real SH coefficients, 8 history values, log T."""
-    return (L + 1) * (L + 1) + 9
+    """Feature width per shell: (L+1)^2 real SH coefficients, 8 history values, log T,
+    8 launches x 3 gradient estimates."""
+    return (L + 1) * (L + 1) + 9 + 24
 
 
 def n_in_pad(n_in: int) -> int:
@@ -46,7 +47,10 @@ class ProposalMLP:
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            self._lib.tp3_mlp_destroy(self._h)
+            # a network lives on its context: when the context is already gone (both
+            # collected together at interpreter exit) the handle is dropped, not freed
+            if getattr(self._basis, "_ctx", None):
+                self._lib.tp3_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -67,23 +71,30 @@ class ProposalMLP:
         check(self._lib.tp3_mlp_set_params(self._h, p.ctypes.data, self.n_params), self._basis.ctx)
 
     def forward_device(self, rows: int, d_x: int, d_out: int) -> None:
-        """(mu, s) per row into d_out (rows x 6 float32)."""
+        """(u, s) per row into d_out (rows x 6 float32)."""
         check(self._lib.tp3_mlp_forward_device(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_out)),
               self._basis.ctx)
 
-    def loss_grad(self, rows: int, d_x: int, d_v: int, d_w: int, want_grad: bool = True):
+    def loss_grad(self, rows: int, d_x: int, d_v: int, d_w: int, d_t: int = 0, shells: int = 1,
+                  want_grad: bool = True):
+        """Loss (regression of the targets d_t = (t, lambda) per candidate of `shells` rows
+        on the steps, plus the weighted NLL of the steps under the log-scales) and its
+        gradient (host float32) when want_grad."""
         loss = ctypes.c_double()
         g = np.empty(self.n_params, dtype=np.float32) if want_grad else None
         check(self._lib.tp3_mlp_loss_grad(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_v),
-                                          ctypes.c_void_p(d_w), ctypes.byref(loss),
-                                          g.ctypes.data if g is not None else None), self._basis.ctx)
+                                          ctypes.c_void_p(d_w), ctypes.c_void_p(d_t or None), shells,
+                                          ctypes.byref(loss), g.ctypes.data if g is not None else None),
+              self._basis.ctx)
         return loss.value, g
 
-    def train_step(self, rows: int, d_x: int, d_v: int, d_w: int, lr: float, want_loss: bool = False):
+    def train_step(self, rows: int, d_x: int, d_v: int, d_w: int, lr: float, d_t: int = 0, shells: int = 1,
+                   want_loss: bool = False):
         loss = ctypes.c_double()
         check(self._lib.tp3_mlp_train_step(self._h, rows, ctypes.c_void_p(d_x), ctypes.c_void_p(d_v),
-                                           ctypes.c_void_p(d_w), ctypes.c_float(lr),
-                                           ctypes.byref(loss) if want_loss else None), self._basis.ctx)
+                                           ctypes.c_void_p(d_w), ctypes.c_void_p(d_t or None), shells,
+                                           ctypes.c_float(lr), ctypes.byref(loss) if want_loss else None),
+              self._basis.ctx)
         return loss.value if want_loss else None
 
 
@@ -92,7 +103,7 @@ class ProposalMLP:
 # ---------------------------------------------------------------------------
 
 def move_weights(meta):
-    """Training weight of a logged candidate (torch tensor [n, 6] -> [n]): accepted moves,
+    """NLL weight of a logged candidate (torch tensor [n, 7] -> [n]): accepted moves,
     counted more the more they lowered the energy (1 + min(-dE/T, 5) for dE < 0)."""
     import torch
     dE, T, acc = meta[:, 0], meta[:, 1], meta[:, 2]
@@ -100,11 +111,24 @@ def move_weights(meta):
     return acc * (1.0 + gain)
 
 
+TARGET_CLIP = 30.0
+
+
+def move_targets(meta):
+    """Regression target of a logged candidate: its energy change relative to the
+    launch's mean, over T (meta column 6), clipped to +-TARGET_CLIP so that the rare
+    far-uphill candidates do not dominate the squared loss."""
+    import torch
+    return torch.clamp(meta[:, 6], min=-TARGET_CLIP, max=TARGET_CLIP)
+
+
 def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr: float = 1e-3, seed: int = 0,
                  holdout: float = 0.05, log_every: int = 0):
-    """Adam steps on the weighted NLL of logged steps, batches of whole candidates
-    (K rows each) drawn uniformly from the move log.  Returns (train losses, held-out
-    loss before, held-out loss after); the held-out candidates are never trained on."""
+    """Adam steps on the training loss of logged candidates, batches of whole candidates
+    (K rows each) drawn uniformly from the move log: the mean squared residual of the
+    energy-change targets regressed on the steps through the drift heads u, plus the
+    weighted NLL of the steps under the log-scale heads.  Returns (train losses,
+    held-out loss before, held-out loss after); held-out candidates are never trained on."""
     import torch
     dev = torch.device("cuda")
     K = chains.basis.K
@@ -122,7 +146,8 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
     X = torch.zeros((rows, net.stride), dtype=torch.bfloat16, device=dev)
     V = torch.zeros((rows, 3), dtype=torch.float32, device=dev)
     W = torch.zeros(rows, dtype=torch.float32, device=dev)
-    M = torch.zeros((nb, 6), dtype=torch.float32, device=dev)
+    Tg = torch.zeros((rows // K, 2), dtype=torch.float32, device=dev)
+    M = torch.zeros((nb, 7), dtype=torch.float32, device=dev)
 
     def fill(idx_cpu):
         n = idx_cpu.numel()
@@ -133,6 +158,9 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
         w = move_weights(M[:n])
         W.zero_()
         W[: n * K] = (w / torch.clamp(w.sum(), min=1e-12)).repeat_interleave(K)
+        Tg.zero_()
+        Tg[:n, 0] = move_targets(M[:n])
+        Tg[:n, 1] = 1.0 / n
         if n * K < rows:
             X[n * K:].zero_()
             V[n * K:].zero_()
@@ -143,7 +171,7 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
         for a in range(0, nh, nb):
             part = hold[a:a + nb]
             fill(part)
-            l, _ = net.loss_grad(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), want_grad=False)
+            l, _ = net.loss_grad(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), Tg.data_ptr(), K, want_grad=False)
             tot += l * part.numel()
             wsum += part.numel()
         return tot / max(wsum, 1)
@@ -154,7 +182,7 @@ def train_on_log(net: ProposalMLP, chains, steps: int, batch_candidates: int, lr
         pick = train[torch.randint(0, train.numel(), (nb,), generator=g)]
         fill(pick)
         want = log_every and (it % log_every == 0 or it == steps - 1)
-        l = net.train_step(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), lr, want_loss=bool(want))
+        l = net.train_step(rows, X.data_ptr(), V.data_ptr(), W.data_ptr(), lr, Tg.data_ptr(), K, want_loss=bool(want))
         if want:
             losses.append((it, l))
     after = heldout_loss()
