@@ -222,7 +222,10 @@ int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
  * (u_k, s_k) draws a = +-1 (equally likely) and
  *     v_k = sigma_i (a sqrt(16) u_k / sqrt(sum_k |u_k|^2 + 0.01) + exp(s_k - mean_k s_k) z_k),
  * z_k ~ N(0, I3) (whitened noise exp(-(s_k - mean s)) z_k): a two-sided drift along
- * the network's gradient estimate.  The Metropolis-Hastings ratio of the mixture
+ * the network's gradient estimate.  Per-shell steps draw z (and a) from a stream keyed
+ * by the chain's launch count, so every launch's candidates carry fresh noise and a
+ * per-shell chain's trajectory depends on the candidates per launch (the reference
+ * move's draws are keyed by the step and do not).  The Metropolis-Hastings ratio of the mixture
  * density (the network part a two-component mixture over a, evaluated at x' for the
  * reverse step with the network re-run there) corrects the acceptance.  The network
  * must have n_in = (L+1)^2 + 33 and max_rows >= chains x candidates x K.

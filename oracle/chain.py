@@ -120,8 +120,9 @@ def run_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, initi
 
 # ---------------------------------------------------------------------------
 # Per-shell SO(3) moves (no reference counterpart: the learned-proposal experiment).
-# Stream: purpose 3 index 0 = component uniform, purpose 4 index k = the three
-# normals of shell k's axis-angle step.
+# Stream: purpose 3 index 0 (counter step) = component uniform; the step noise of
+# candidate i of a launch = purpose 5 + 16 i, index k (counter launch) = the three
+# normals of shell k; index 64 = the network step's side.
 # ---------------------------------------------------------------------------
 
 def rodrigues(v) -> np.ndarray:
@@ -146,11 +147,16 @@ def rotate_shells(coeff: np.ndarray, v: np.ndarray, L: int, LMAX: int) -> np.nda
     return out
 
 
-def shell_steps(seed: int, step: int, chain: int, K: int):
-    """Unit normals z[K][3] and the component uniform of one candidate."""
-    z = np.array([normals4(seed, step, chain, 4, k)[:3] for k in range(K)])
-    u = u01(philox4x32_10((step & M32, chain, 3, 0), _key(seed))[0])
-    return z, u
+def component_uniform(seed: int, step: int, chain: int) -> float:
+    """The uniform that picks the network (u < p_net) or the isotropic step."""
+    return u01(philox4x32_10((step & M32, chain, 3, 0), _key(seed))[0])
+
+
+def shell_noise(seed: int, launch: int, chain: int, i: int, K: int):
+    """Unit normals z[K][3] of candidate i of a launch and the network step's side a = +-1."""
+    z = np.array([normals4(seed, launch, chain, 5 + 16 * i, k)[:3] for k in range(K)])
+    c = philox4x32_10((launch & M32, chain, 5 + 16 * i, 64), _key(seed))
+    return z, (-1.0 if u01(c[0]) < 0.5 else 1.0)
 
 
 def rot_logdens(v, mu, s) -> float:
@@ -218,29 +224,38 @@ def gradient_estimate(dE, T1: float, w) -> np.ndarray:
 
 
 def run_shell_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, sigma0: float,
-                    stepsizefactor: float, temperature_decay: float, seed: int, chain: int, nsteps: int):
-    """Sequential chain with the isotropic per-shell move; rows as run_chain."""
+                    stepsizefactor: float, temperature_decay: float, seed: int, chain: int, nlaunches: int,
+                    ncand: int):
+    """Chain with the isotropic per-shell move, run as launches of ncand speculative
+    candidates (candidate i of a launch assumes i rejections: sigma / f^i, T decay^(i+1),
+    noise of its own launch-keyed stream); a launch takes its first accepted candidate
+    or ncand rejections.  Rows as run_chain, one per step up to the taken one."""
     state = coeff0.copy()
     E = energy_fn(state)
     T, sigma = T0, sigma0
     rows = []
     K = coeff0.shape[0]
-    for s in range(nsteps):
-        T *= temperature_decay
-        z, _ = shell_steps(seed, s, chain, K)
-        cand = rotate_shells(state, sigma * z, L, LMAX)
-        En = energy_fn(cand)
-        dE = En - E
-        ap = math.exp(-dE / T) if -dE / T < 700 else float("inf")
-        u = u01(philox4x32_10((s & M32, chain, 2, 0), _key(seed))[0])
-        acc = dE < 0.0 or (dE > 0.0 and u < ap)
-        sign = 0.0
-        if acc:
-            sign = 1.0 if dE < 0.0 else -1.0
-            sigma *= stepsizefactor
-            E = En
-            state = cand
-        else:
-            sigma /= stepsizefactor
-        rows.append([s + 1, sign, En, E, dE, T, ap, sigma])
+    step = 0
+    for launch in range(nlaunches):
+        for i in range(ncand):
+            T *= temperature_decay
+            z, _ = shell_noise(seed, launch, chain, i, K)
+            cand = rotate_shells(state, sigma * z, L, LMAX)
+            En = energy_fn(cand)
+            dE = En - E
+            ap = math.exp(-dE / T) if -dE / T < 700 else float("inf")
+            u = u01(philox4x32_10((step & M32, chain, 2, 0), _key(seed))[0])
+            acc = dE < 0.0 or (dE > 0.0 and u < ap)
+            sign = 0.0
+            if acc:
+                sign = 1.0 if dE < 0.0 else -1.0
+                sigma *= stepsizefactor
+                E = En
+                state = cand
+            else:
+                sigma /= stepsizefactor
+            step += 1
+            rows.append([step, sign, En, E, dE, T, ap, sigma])
+            if acc:
+                break
     return state, E, T, sigma, np.array(rows)

@@ -67,7 +67,7 @@ def test_isotropic_shell_chain_matches_oracle(setup):
     assert all(ch.state()["steps"] > 0)
     for c in range(nch):
         rows = ch.log(c)
-        _, _, _, _, ref = oc.run_shell_chain(e64, start, p["L"], p["LMAX"], T0, sigma0, f, decay, SEED, c, len(rows))
+        _, _, _, _, ref = oc.run_shell_chain(e64, start, p["L"], p["LMAX"], T0, sigma0, f, decay, SEED, c, launches, B)
         assert _agree(rows, ref, ref[0][3], c) >= min(len(rows), 3)
     ch.close()
 
@@ -78,29 +78,28 @@ def _constant_head_params(net, s_const):
     return P
 
 
-def test_constant_network_reduces_to_isotropic(setup):
+def test_constant_network_proposes_isotropic_steps(setup):
+    """A network with u = 0 and constant log-scales proposes the isotropic step (its own
+    launch-keyed normals times sigma_i) and its Metropolis-Hastings ratio is exactly one."""
     basis, e64, start, p = setup
-    nch, B, launches = 4, 4, 6
+    nch, B = 4, 4
     L, K = p["L"], p["K"]
-    s_const = math.log(0.2)
     net = ProposalMLP(basis, n_in_for(L), hidden=64, max_rows=((nch * B * K + 127) // 128) * 128, seed=1)
-    P = _constant_head_params(net, s_const)
-    net.set_params(P)
-    sigma_dev = math.exp(om.S_MID + om.S_HALF * math.tanh(float(P[-1])))  # the step size the head gives
-    runs = []
-    for kind in (tp3.TP3_MOVE_SHELL_SO3, tp3.TP3_MOVE_LEARNED):
-        ch = Chains(basis, np.repeat(start[None], nch, axis=0), 2.0, 0.1, 1.0, 0.995, SEED, ncand=B,
-                    log_capacity=64)
-        ch.set_move(kind, sigma_dev, 1.0, net if kind == tp3.TP3_MOVE_LEARNED else None)
-        ch.run(launches)
-        runs.append([ch.log(c) for c in range(nch)])
-        ch.close()
+    net.set_params(_constant_head_params(net, math.log(0.2)))
+    sigma0 = 0.2
+    ch = Chains(basis, np.repeat(start[None], nch, axis=0), 2.0, 0.1, 1.05, 0.995, SEED, ncand=B)
+    ch.set_move(tp3.TP3_MOVE_LEARNED, sigma0, 1.0, net)
+    ch.enable_move_log(4)
+    ch.run(1)
+    stride = (n_in_for(L) + 31) // 32 * 32
+    _, V, M = _gather(ch, list(range(nch * B)), K, stride)
+    assert np.all(M[:, 3] == 1.0) and np.all(M[:, 4] == 0.0)
     for c in range(nch):
-        a, b = runs[0][c], runs[1][c]
-        n = min(len(a), len(b))
-        assert n >= launches
-        np.testing.assert_array_equal(a[:n, 1], b[:n, 1])
-        np.testing.assert_allclose(a[:n, 2], b[:n, 2], rtol=1e-9)
+        for i in range(B):
+            z, _ = oc.shell_noise(SEED, 0, c, i, K)
+            j = c * B + i
+            np.testing.assert_allclose(V[j * K:(j + 1) * K], z, rtol=1e-6, atol=1e-6)
+    ch.close()
     net.close()
 
 
@@ -202,8 +201,8 @@ def test_learned_moves_match_oracle(setup):
             Xd = X[j * K:(j + 1) * K]
             # features agree to one BF16 rounding
             assert np.all(np.abs(Xd - feats) <= 2 ** -7 * np.abs(feats) + 1e-30)
-            z, u = oc.shell_steps(SEED, i, c, K)
-            comp = 1.0 if u < p_net else 0.0
+            comp = 1.0 if oc.component_uniform(SEED, i, c) < p_net else 0.0
+            z, a = oc.shell_noise(SEED, 0, c, i, K)
             assert M[j, 3] == comp
             n_net += int(comp)
             v = V[j * K:(j + 1) * K]
@@ -219,7 +218,6 @@ def test_learned_moves_match_oracle(setup):
             v = v * M[j, 5]  # the log holds v / sigma_i
             m, s = oc.shell_params(uh, sh, sig_i)
             if comp:
-                a = 1.0 if oc.u01(oc.philox4x32_10((i, c, 3, 0), (SEED & oc.M32, SEED >> 32))[1]) >= 0.5 else -1.0
                 vref = a * m + np.exp(s) * z
             else:
                 vref = sig_i * z
@@ -237,9 +235,10 @@ def test_learned_moves_match_oracle(setup):
 
 def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
     """The full learned-proposal protocol at the small configuration: the plain
-    annealer's logged moves train the network on the device (held-out NLL falls), and
-    the learned annealer's time to the plain annealer's final median energy is measured
-    and reported (the gain itself is a measured quantity, not asserted)."""
+    annealer's logged moves train the network on the device (held-out loss falls), and
+    the learned annealer reaches the plain annealer's final median energy in fewer
+    launches (the wall-clock ratio is reported: at this size the network's forward
+    passes cost about as much as the scoring)."""
     from tp3.learned import learned_vs_plain
     p = config1["params"]
     basis = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
@@ -251,6 +250,7 @@ def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
     assert res["train"]["heldout_nll_after"] < res["train"]["heldout_nll_before"]
     assert math.isfinite(res["learned"]["median_E"]) and math.isfinite(res["plain"]["final_median_E"])
     assert 0.05 < res["learned"]["accept_rate"] < 0.95
+    assert res["learned"]["reached"] and res["learned"]["launches"] < res["plain"]["launches"]
     with capsys.disabled():
         print(f"\n[learned proposal, L8 K8 N16] plain: {res['plain']['launches']} launches "
               f"{res['plain']['seconds']:.3f} s -> median E {res['plain']['final_median_E']:.4f}; learned: "

@@ -19,7 +19,8 @@
 // for the same random numbers (a rejected step leaves the state unchanged).
 //
 // Randomness is Philox4x32-10 keyed by the run seed with counter
-// (step, chain, purpose, index), so a step's draws do not depend on the batching.
+// (step, chain, purpose, index), so a step's draws do not depend on the batching
+// (the per-shell moves below key their step noise by the launch instead).
 // All of it (proposal, scoring, Metropolis test, state update) runs on the device
 // from one captured CUDA graph per launch.
 //
@@ -72,7 +73,7 @@ constexpr int kPurposeAngle = 0;
 constexpr int kPurposePlane = 1;
 constexpr int kPurposeAccept = 2;
 constexpr int kPurposeComponent = 3;
-constexpr int kPurposeShell = 4;
+constexpr int kPurposeNoise = 5;  // + 16 i for candidate i: per-shell steps, keyed by the launch
 constexpr int kMaxShells = 64;
 constexpr int kMaxL = 62;  // even l <= 62: 2l+1 <= 125 real coefficients per block
 
@@ -81,8 +82,8 @@ struct ChainState {
   double T;
   long long step;
   long long accepted;
-  int last;  // index of the candidate taken by the last launch, -1 if none
-  int pad;
+  int last;      // index of the candidate taken by the last launch, -1 if none
+  int launches;  // launches run (keys the network steps' random stream)
 };
 
 struct LogRow {  // one evaluated step (the columns of det.out, src/determination.jl:512-514)
@@ -336,6 +337,7 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
         if (!meta) break;
       }
     }
+    st.launches += 1;
     cs[c] = st;
   }
 }
@@ -468,7 +470,17 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   uint32_t pc[4] = {(uint32_t)step, (uint32_t)cid, (uint32_t)kPurposeComponent, 0u};
   philox4x32_10(pc, (uint32_t)seed, (uint32_t)(seed >> 32));
   const bool use_net = O != nullptr && u01(pc[0]) < p_net;
-  const double a = u01(pc[1]) < 0.5 ? -1.0 : 1.0;  // side of the network's two-sided drift
+  // Per-shell steps draw their noise (and a network step its side) from a stream keyed
+  // by the launch, not the step: the speculative candidates of one launch are
+  // re-proposed at the same step numbers by the next, and the gradient-history inputs
+  // are built from the previous launches' noise, so step-keyed draws would repeat noise
+  // that the history (and the drift built on it) already depends on.  Each taken step
+  // still sees a fresh draw, so the chain is a sequential chain with its own stream.
+  const int launch = cs[cid].launches;
+  const int pnet_i = kPurposeNoise + 16 * i;
+  uint32_t pa[4] = {(uint32_t)launch, (uint32_t)cid, (uint32_t)pnet_i, (uint32_t)kMaxShells};
+  philox4x32_10(pa, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const double a = u01(pa[0]) < 0.5 ? -1.0 : 1.0;  // side of the network's two-sided drift
   const double ls = log(sg);
   double smean[3] = {0, 0, 0}, df = 0.0;
   if (O) {
@@ -481,7 +493,7 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   double lp = 0.0, lm = 0.0, liso = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double z[4];
-    normals4(seed, step, cid, kPurposeShell, k, z);
+    normals4(seed, launch, cid, pnet_i, k, z);
     double mu[3] = {0, 0, 0}, s[3] = {ls, ls, ls}, v[3], w[3];
     if (O) shell_params(hu[k], hs[k], smean, sg, df, ls, mu, s);
     for (int d = 0; d < 3; ++d) {
@@ -872,7 +884,7 @@ static int chains_create(tp3_ctx* ctx, int nchains, int ncand, const double* coe
   std::vector<ChainState> cs(nchains);
   std::vector<double> sig((size_t)nchains * h->nl);
   for (int i = 0; i < nchains; ++i) {
-    cs[i].E = E0[i]; cs[i].T = T0[i]; cs[i].step = 0; cs[i].accepted = 0; cs[i].last = -1; cs[i].pad = 0;
+    cs[i].E = E0[i]; cs[i].T = T0[i]; cs[i].step = 0; cs[i].accepted = 0; cs[i].last = -1; cs[i].launches = 0;
     // stepsizes[l] = initial_stepsize * (l - 1), l = 2:2:L (src/determination.jl:295)
     for (int il = 0; il < h->nl; ++il) sig[(size_t)i * h->nl + il] = il == 0 ? 0.0 : initial_stepsize * (2 * il - 1);
   }
