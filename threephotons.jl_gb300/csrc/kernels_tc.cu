@@ -447,8 +447,16 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_warp(
     }
     __syncwarp();
     // ---- phase 2: T for (k1, k2 in the quad, k3-quad rb <= q, l3) ----
+    // A unit has only nl3 (q + 1) items; when they fill less than the warp, g = 2 or 4
+    // lanes share an item, each summing every g-th m3, and combine by shuffles.
     const int nI2 = nl3 * (q + 1);
-    for (int it = lane; it < nI2; it += 32) {
+    int lg = 0;
+    while (lg < 2 && (nI2 << (lg + 1)) <= 32) ++lg;
+    const int g = 1 << lg, nI2g = nI2 << lg;
+    for (int base = 0; base < nI2g; base += 32) {
+      const int itl = base + lane;
+      const bool active = itl < nI2g;
+      const int it = active ? itl >> lg : 0, seg = itl & (g - 1);
       const int s = nl3 - 1 - it / (q + 1);  // largest l3 first
       const int rb = it % (q + 1);
       const int l3 = l3min + 2 * s;
@@ -466,15 +474,23 @@ __global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_warp(
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-      for (int m3 = sym ? 1 : -l3; m3 <= l3; ++m3) {
-        float2 x[4], y[4];
+      if (active) {
+        for (int m3 = (sym ? 1 : -l3) + seg; m3 <= l3; m3 += g) {
+          float2 x[4], y[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) { x[i] = drow[i][m3]; y[i] = crow[i][m3]; }
+          for (int i = 0; i < 4; ++i) { x[i] = drow[i][m3]; y[i] = crow[i][m3]; }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, acc[i][j]));
+        }
+      }
+      for (int o = 1; o < g; o <<= 1)
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(x[i].x, y[j].x, fmaf(-x[i].y, y[j].y, acc[i][j]));
-      }
+          for (int j = 0; j < 4; ++j) acc[i][j] += __shfl_xor_sync(0xffffffffu, acc[i][j], o);
+      if (!active || seg != 0) continue;
       if (sym) {
         float2 x[4], y[4];
 #pragma unroll
