@@ -102,14 +102,15 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * TF32 x3) with each coupling form that fits (0: one-kernel pair coupling, 512 threads
  * and up to 225 KB of shared memory per CTA; 2: the same with 256 threads and 110 KB so
  * two CTAs share an SM; 3: warp-local one-kernel coupling, warps taking (k1, k2-quad)
- * units from a counter with no CTA barrier; 1: two-kernel split coupling through
+ * units from a counter with no CTA barrier, 512 threads; 4: the warp-local coupling
+ * with 256 threads and 110 KB, two CTAs per SM; 1: two-kernel split coupling through
  * global memory) -- selects
  * the fastest for this context and records it for the shape (L, LMAX, N, K, lambda,
  * dq) in the process, where TP3_MODE_AUTO finds it.  report (nullable): up to *nreport
  * rows of (mode, coupling form, ms per proposal); *nreport returns the number of
  * variants.  Synchronises. */
 int tp3_autotune(tp3_ctx* ctx, int n, double* report, int* nreport);
-/* Force a coupling form of the tensor-core path (0 to 3 as above). */
+/* Force a coupling form of the tensor-core path (0 to 4 as above). */
 int tp3_set_coupling(tp3_ctx* ctx, int form);
 /* Pre-size scratch for batches of up to n proposals (otherwise sized on first use). */
 int tp3_reserve(tp3_ctx* ctx, int n);

@@ -234,6 +234,10 @@ std::string setup_tc(tp3_ctx* c) {
     tc.w_smem_w = base + (size_t)wmax * 4 + dw <= limit;
     tc.couple_smem_w = base + (tc.w_smem_w ? (size_t)wmax * 4 : 0) + dw;
     tc.warp_ok = tc.couple_smem_w <= limit && b.K <= 64;
+    const size_t dw2 = (size_t)8 * 4 * tc.SDp * sizeof(float2);
+    tc.w_smem_w2 = base + (size_t)wmax * 4 + dw2 <= limit_s;
+    tc.couple_smem_w2 = base + (tc.w_smem_w2 ? (size_t)wmax * 4 : 0) + dw2;
+    tc.warp2_ok = tc.couple_smem_w2 <= limit_s && b.K <= 64;
   }
   // split coupling: D offsets, L2-sized sub-batches, balanced (pair block, m3 range) units
   const int npairs = b.K * (b.K + 1) / 2;
@@ -540,13 +544,15 @@ int check_ctx(tp3_ctx* c) {
 }
 
 // Coupling form of the tensor-core path: 0 one-kernel, 1 split, 2 one-kernel small
-// tiling; a form this shape cannot run falls back to one that it can.
+// tiling, 3 warp-local (512 threads), 4 warp-local (256 threads, two CTAs per SM); a
+// form this shape cannot run falls back to one that it can.
 void apply_coupling(tp3_ctx* c, int form) {
   TcTables& tc = c->tc;
   tc.use_small = form == 2 && tc.small_ok;
   tc.use_warp = form == 3 && tc.warp_ok;
-  tc.split = (form == 1 && tc.split_ok) || (!tc.fused_ok && !tc.use_warp);
-  if (tc.split) tc.use_small = tc.use_warp = false;
+  tc.use_warp2 = form == 4 && tc.warp2_ok;
+  tc.split = (form == 1 && tc.split_ok) || (!tc.fused_ok && !tc.use_warp && !tc.use_warp2);
+  if (tc.split) tc.use_small = tc.use_warp = tc.use_warp2 = false;
 }
 
 // Folded, slab-normalised histogram of Kh shells (slabs with k1 < Kh; the rest zero)
@@ -862,6 +868,7 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
       if (c->tc.fused_ok) vars.push_back({m, 0});
       if (c->tc.small_ok) vars.push_back({m, 2});
       if (c->tc.warp_ok) vars.push_back({m, 3});
+      if (c->tc.warp2_ok) vars.push_back({m, 4});
       if (c->tc.split_ok) vars.push_back({m, 1});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
@@ -962,8 +969,8 @@ int tp3_set_coupling(tp3_ctx* c, int form) {
   if (int r = check_ctx(c)) return r;
   if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
   const bool ok = (form == 0 && c->tc.fused_ok) || (form == 1 && c->tc.split_ok) || (form == 2 && c->tc.small_ok) ||
-                  (form == 3 && c->tc.warp_ok);
-  if (!ok) return fail(c, form < 0 || form > 3 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
+                  (form == 3 && c->tc.warp_ok) || (form == 4 && c->tc.warp2_ok);
+  if (!ok) return fail(c, form < 0 || form > 4 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
   apply_coupling(c, form);
   return TP3_OK;
 }

@@ -87,6 +87,9 @@ struct TcTables {
   bool use_warp = false;
   bool w_smem_w = false;
   size_t couple_smem_w = 0;
+  // the warp-local coupling at 256 threads, two CTAs per SM
+  bool warp2_ok = false, use_warp2 = false, w_smem_w2 = false;
+  size_t couple_smem_w2 = 0;
   // split coupling (kernels_couple.cu)
   bool split = false;            // use the two-kernel coupling
   bool split_ok = false;         // the two-kernel coupling fits this shape

@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, co
 // Phase 2: item = (k1, l3, 4 x 4 tile of (k2, k3)) with k3 <= k2.
 // grid: (n_pb, n); block kCoupleThreads.
 constexpr int kCoupleThreads = 512;
+constexpr int kCoupleThreadsSmall = 256;  // the two-CTA-per-SM tilings
 
 template <int MAXS, bool W_SMEM, int THREADS>
 __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_pair(
@@ -330,8 +331,8 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_pa
 // then contracts D with every k3-quad <= q (phase 2: lanes own (l3, k3-quad) items and
 // read the unit's D rows as broadcasts).  Both phases synchronise only the warp.
 // grid: (n_pb, n); block kCoupleThreads.
-template <int MAXS, bool W_SMEM>
-__global__ void __launch_bounds__(kCoupleThreads, 1) k_couple_warp(
+template <int MAXS, bool W_SMEM, int THREADS>
+__global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_warp(
     const float2* __restrict__ cc, int K, int nc, int ncp, const int* __restrict__ coff,
     const PairBlock* __restrict__ pbs, const int* __restrict__ eofs, const float* __restrict__ wtab, int SDp,
     int SDhp, int wsmem, int klp, int KP, const int* __restrict__ symflags, void* __restrict__ Thi,
@@ -803,9 +804,11 @@ cudaError_t tc_configure() {
   TP3_CP_ATTR(4, false) TP3_CP_ATTR(8, false) TP3_CP_ATTR(10, false) TP3_CP_ATTR(12, false)
   TP3_CP_ATTR(16, false)
 #undef TP3_CP_ATTR
-#define TP3_CW_ATTR(S, W)                                                                               \
-  if ((e = cudaFuncSetAttribute(k_couple_warp<S, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != \
-      cudaSuccess)                                                                                      \
+#define TP3_CW_ATTR(S, W)                                                                                    \
+  if ((e = cudaFuncSetAttribute(k_couple_warp<S, W, kCoupleThreads>,                                         \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||          \
+      (e = cudaFuncSetAttribute(k_couple_warp<S, W, kCoupleThreadsSmall>,                                    \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, css)) != cudaSuccess)           \
     return e;
   TP3_CW_ATTR(4, true) TP3_CW_ATTR(8, true) TP3_CW_ATTR(10, true) TP3_CW_ATTR(12, true) TP3_CW_ATTR(16, true)
   TP3_CW_ATTR(4, false) TP3_CW_ATTR(8, false) TP3_CW_ATTR(10, false) TP3_CW_ATTR(12, false)
@@ -823,13 +826,20 @@ cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, con
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s, const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
-  if (tc.use_warp && tc.warp_ok) {
-#define TP3_CW_LAUNCH(S, W)                                                                                 \
-  k_couple_warp<S, W><<<grid, kCoupleThreads, tc.couple_smem_w, s>>>(cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs,  \
-                                                                     tc.eofs, tc.wtab, tc.SDp, tc.SDhp, tc.wsmem, \
-                                                                     t.klp, tc.KP, sym, Thi, Tlo, tf32, T32,      \
-                                                                     t.n_ltp, rag)
-    if (tc.w_smem_w) {
+  const bool w2 = tc.use_warp2 && tc.warp2_ok;
+  if ((tc.use_warp && tc.warp_ok) || w2) {
+    const size_t smw = w2 ? tc.couple_smem_w2 : tc.couple_smem_w;
+    const bool wsw = w2 ? tc.w_smem_w2 : tc.w_smem_w;
+#define TP3_CW_LAUNCH(S, W)                                                                                       \
+  if (w2)                                                                                                         \
+    k_couple_warp<S, W, kCoupleThreadsSmall><<<grid, kCoupleThreadsSmall, smw, s>>>(                              \
+        cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.SDp, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, \
+        Tlo, tf32, T32, t.n_ltp, rag);                                                                            \
+  else                                                                                                            \
+    k_couple_warp<S, W, kCoupleThreads><<<grid, kCoupleThreads, smw, s>>>(                                        \
+        cc, t.K, t.nc, tc.ncp, tc.coff, tc.pbs, tc.eofs, tc.wtab, tc.SDp, tc.SDhp, tc.wsmem, t.klp, tc.KP, sym, Thi, \
+        Tlo, tf32, T32, t.n_ltp, rag)
+    if (wsw) {
       if (tc.maxs <= 4) TP3_CW_LAUNCH(4, true);
       else if (tc.maxs <= 8) TP3_CW_LAUNCH(8, true);
       else if (tc.maxs <= 10) TP3_CW_LAUNCH(10, true);
