@@ -340,6 +340,8 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
   extern __shared__ __align__(16) float smf[];
   __shared__ int s_next, s_total;
   __shared__ int s_ustart[64];  // first unit index of each k1 (units ordered by k1 descending)
+  __shared__ int s_eofs[64];    // the block's per-m3 3j row offsets (2 M + 1 <= 61)
+  __shared__ int s_coff[32];    // coefficient offset of each even order
   const int prop = blockIdx.y;
   int Kp = K;
   const PairBlock pb = pbs[blockIdx.x];
@@ -371,6 +373,9 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
     float4* s4 = reinterpret_cast<float4*>(sw);
     for (int i = threadIdx.x; i < pb.wcount / 4; i += blockDim.x) s4[i] = w4[i];
   }
+  for (int e = threadIdx.x; e <= 2 * pb.M; e += blockDim.x) s_eofs[e] = eofs[pb.eofs + e];
+  // orders used by this block: l1, l2 and l3 <= M (all <= L, so coff has entries up to L / 2)
+  for (int e = threadIdx.x; e <= max(max(pb.l1, pb.l2), pb.M) >> 1; e += blockDim.x) s_coff[e] = coff[e];
   if (threadIdx.x == 0) {
     int u = 0;
     for (int k1 = Kp - 1; k1 >= 0; --k1) {
@@ -383,9 +388,14 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
   __syncthreads();
   const float* wsrc = W_SMEM ? sw : wblk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this proposal's T rows (klp x KP elements, within int range per proposal)
+  const size_t tbase = (size_t)prop * klp * KP;
+  void* ThiP = tf32out ? (void*)((float*)Thi + tbase) : (void*)((__nv_bfloat16*)Thi + tbase);
+  void* TloP = tf32out ? (void*)((float*)Tlo + tbase) : (void*)((__nv_bfloat16*)Tlo + tbase);
+  float* T32P = T32 ? T32 + (size_t)prop * klp * ldT32 : nullptr;
   float2* Dw = sD + (size_t)warp * 4 * rowD;
   const int l1 = pb.l1, l2 = pb.l2, nl3 = pb.nl3, nl3p = pb.nl3p, l3min = pb.l3min, M = pb.M;
-  const int off1 = coff[l1 >> 1] + l1, off2 = coff[l2 >> 1] + l2;
+  const int off1 = s_coff[l1 >> 1] + l1, off2 = s_coff[l2 >> 1] + l2;
   const int nm3 = sym ? M + 1 : 2 * M + 1;
   for (;;) {
     int u = 0;
@@ -400,12 +410,14 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
     // ---- phase 1: D[i][l3][m3] for the unit's pairs (k1, 4q + i) ----
     const int nI = nm3 * np;
     for (int it = lane; it < nI; it += 32) {
-      const int eo = it / np, i = it - eo * np;
+      // it / np for np in 1..4 without a division (exact for it < 2^15)
+      const int eo = np == 4 ? it >> 2 : (np == 2 ? it >> 1 : (np == 1 ? it : (it * 43691) >> 17));
+      const int i = it - eo * np;
       const int m3 = sym ? eo : ((eo & 1) ? -((eo + 1) >> 1) : (eo >> 1));
       const int e = m3 + M;
       const int k2 = 4 * q + i;
       const int m1lo = max(-l1, -l2 - m3), m1hi = min(l1, l2 - m3);
-      const float* wp = wsrc + eofs[pb.eofs + e];
+      const float* wp = wsrc + s_eofs[e];
       const float2* c1 = sc + k1 * ncp + off1;
       const float2* c2 = sc + k2 * ncp + off2 - m3;
       float ar[MAXS], ai[MAXS];
@@ -454,15 +466,19 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
     int lg = 0;
     while (lg < 2 && (nI2 << (lg + 1)) <= 32) ++lg;
     const int g = 1 << lg, nI2g = nI2 << lg;
+    // it / (q + 1) as a multiply-shift: exact for it < 2^16 / (q + 1) (it < 16 * 16 here)
+    const int d1 = q + 1, rcp = (65536 + d1 - 1) / d1;
+    const int t3 = k1 * (k1 + 1) * (k1 + 2) / 6;  // first shell triple of k1
     for (int base = 0; base < nI2g; base += 32) {
       const int itl = base + lane;
       const bool active = itl < nI2g;
       const int it = active ? itl >> lg : 0, seg = itl & (g - 1);
-      const int s = nl3 - 1 - it / (q + 1);  // largest l3 first
-      const int rb = it % (q + 1);
+      const int sq = (it * rcp) >> 16;
+      const int s = nl3 - 1 - sq;  // largest l3 first
+      const int rb = it - sq * d1;
       const int l3 = l3min + 2 * s;
       const int dofs = sym ? s * (l3min + s) : s * (2 * l3min + 2 * s - 1) + l3min + 2 * s;
-      const int off3 = coff[l3 >> 1] + l3;
+      const int off3 = s_coff[l3 >> 1] + l3;
       const float2* drow[4];
       const float2* crow[4];
 #pragma unroll
@@ -505,14 +521,15 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int k2 = 4 * q + i;
+        if (k2 > k1) continue;
+        const int row0 = t3 + k2 * (k2 + 1) / 2 + 4 * rb;  // shell triple (k1, k2, 4 rb)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const int k3 = 4 * rb + j;
-          if (k2 <= k1 && k3 <= k2) {
-            const int ki = ki_index(k1, k2, k3);
+          if (4 * rb + j <= k2) {
+            const int ki = row0 + j;
             const float v = acc[i][j];
-            store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + lt, v, tf32out);
-            if (T32) T32[((size_t)prop * klp + ki) * ldT32 + lt] = v;
+            store_split(ThiP, TloP, (size_t)(ki * KP + lt), v, tf32out);
+            if (T32P) T32P[ki * ldT32 + lt] = v;
           }
         }
       }
