@@ -423,6 +423,7 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
       float ar[MAXS], ai[MAXS];
 #pragma unroll
       for (int s = 0; s < MAXS; ++s) { ar[s] = 0.f; ai[s] = 0.f; }
+#pragma unroll 2
       for (int m1 = m1lo; m1 <= m1hi; ++m1) {
         const float2 a = c1[m1];
         const float2 b = c2[-m1];
@@ -492,6 +493,7 @@ __global__ void __launch_bounds__(THREADS, kCoupleThreads / THREADS) k_couple_wa
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
       if (active) {
+#pragma unroll 2
         for (int m3 = (sym ? 1 : -l3) + seg; m3 <= l3; m3 += g) {
           float2 x[4], y[4];
 #pragma unroll
