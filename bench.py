@@ -415,7 +415,8 @@ def main():
         step()
         ends[i].record(stream)
     torch.cuda.synchronize()
-    n_prof, ms_prof = basis.profile_read()
+    n_prof, ms_prof = basis.profile_read(0)
+    n_prof_c, ms_prof_c = basis.profile_read(1)
     basis.profile_enable(False)
     if ws > 1:
         torch.distributed.barrier()
@@ -465,6 +466,36 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch", "peak_source": f"{peak_src} bf16 dense burst",
                 "kernel": "angular contraction + fused Bayes", "kernel_ms_per_launch": per_launch_ms,
                 "algorithmic_flop_per_proposal": W_b}
+
+    # per-stage rooflines: the coupling (SIMT FP32) against the measured FFMA peak, the
+    # angular contraction against the BF16 tensor peak
+    stages = None
+    if n_prof_c > 0:
+        # W_a = 10 P2 basislen + 4 S klength (pair-factorised coupling), S = sum over the
+        # l-triples (even l <= L, triangle) of 2 l3 + 1
+        trip = [(a, b, c) for a in range(0, L + 1, 2) for b in range(0, L + 1, 2) for c in range(0, L + 1, 2)
+                if abs(a - b) <= c <= a + b]
+        if len(trip) != n_lt:
+            raise SystemExit("l-triple count differs from the basis")
+        S = sum(2 * c + 1 for _, _, c in trip)
+        W_a = 10.0 * (K * (K + 1) / 2) * basis.basislen + 4.0 * S * klength
+        ms_c = ms_prof_c / n_prof_c
+        fp32_peak = basis.measure_fp32_peak()
+        ach_c = W_a * B / (ms_c / 1e3) / 1e12
+        cform = None
+        if tuning:
+            best = min((t for t in tuning if t["mode"] == MODE_NAMES.get(mode_used)), key=lambda t: t["ms_per_proposal"],
+                       default=None)
+            cform = best["coupling"] if best else None
+        elif args.coupling >= 0:
+            cform = COUPLING_NAMES.get(args.coupling)
+        stages = {"coupling": {"bound": "fp32", "kernel": f"coupling ({cform or 'default form'})",
+                               "ms_per_launch": ms_c, "algorithmic_flop_per_proposal": W_a, "achieved": ach_c,
+                               "peak": fp32_peak, "frac": ach_c / fp32_peak, "unit": "TFLOP/s",
+                               "peak_source": "measured FFMA (tp3_measure_fp32_peak, this run)"},
+                  "angular": {"bound": "tensor", "ms_per_launch": per_launch_ms, "algorithmic_flop_per_proposal": W_b,
+                              "achieved": achieved, "peak": peak, "frac": achieved / peak, "unit": "TFLOP/s",
+                              "peak_source": f"{peak_src} bf16 dense burst"}}
 
     # device-resident annealing chains: 64 chains x 16 speculative candidates per graph replay
     chains_info = None
@@ -521,7 +552,7 @@ def main():
                        "L": L, "K": K, "N": N, "LMAX": LMAX, "proposals_per_step": B,
                        "mode": MODE_NAMES.get(mode_used, str(mode_used)), "autotune": tuning,
                        "l2": "flushed (512 MB write) between steps, outside the per-step events"},
-            "e2e": e2e, "roofline": roofline, "clocks": clocks, "chains": chains_info,
+            "e2e": e2e, "roofline": roofline, "stages": stages, "clocks": clocks, "chains": chains_info,
             "gpu_launches": kernels_per_step * args.steps}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(base, hist)

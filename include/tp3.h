@@ -372,12 +372,22 @@ int tp3_mlp_train_step(tp3_mlp* net, int rows, const void* d_x, const float* d_v
  * (tp3_sync, tp3_energy*, ...) reports TP3_ERR_TIMEOUT; the context stays usable. */
 int tp3_selftest_timeout(tp3_ctx* ctx, long long cycles);
 
-/* ---- per-launch timing of the dominant kernel ----------------------------- */
-/* When enabled, CUDA events bracket each launch of the angular + Bayes kernel on
- * the launching stream; tp3_profile_read returns the launch count and the summed
- * milliseconds (synchronising the stream) and resets both. */
+/* ---- per-launch timing of the stages ------------------------------------- */
+/* When enabled, CUDA events bracket each launch of the angular + Bayes kernel and
+ * (tensor-core modes) of the coupling kernel on the launching stream;
+ * tp3_profile_read_stage(stage 0 = angular, 1 = coupling) returns that stage's launch
+ * count and summed milliseconds (synchronising the stream) and resets both;
+ * tp3_profile_read is stage 0. */
 int tp3_profile_enable(tp3_ctx* ctx, int on);
 int tp3_profile_read(tp3_ctx* ctx, int64_t* launches, double* total_ms);
+int tp3_profile_read_stage(tp3_ctx* ctx, int stage, int64_t* launches, double* total_ms);
+
+/* ---- measured FP32 peak (the coupling stage's roofline denominator) ------------
+ * Times a kernel of independent FP32 FMA chains filling every SM (8 chains per
+ * thread, 2048 threads per SM) with CUDA events on the context stream and returns the
+ * best of three runs in TFLOP/s (2 flops per FMA).  Synchronises.  No reference
+ * counterpart. */
+int tp3_measure_fp32_peak(tp3_ctx* ctx, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -440,20 +440,22 @@ int ensure_cap(tp3_ctx* c, int n) {
   return TP3_OK;
 }
 
-int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) {
+int prof_begin_in(tp3_ctx* c, std::vector<cudaEvent_t>& ev, size_t& used, cudaEvent_t* a, cudaEvent_t* b) {
   if (!c->prof) return 0;
-  if (c->ev_used + 2 > c->ev.size()) {
+  if (used + 2 > ev.size()) {
     cudaEvent_t e1, e2;
     if (cudaEventCreate(&e1) != cudaSuccess || cudaEventCreate(&e2) != cudaSuccess) return 0;
-    c->ev.push_back(e1);
-    c->ev.push_back(e2);
+    ev.push_back(e1);
+    ev.push_back(e2);
   }
-  *a = c->ev[c->ev_used];
-  *b = c->ev[c->ev_used + 1];
-  c->ev_used += 2;
+  *a = ev[used];
+  *b = ev[used + 1];
+  used += 2;
   cudaEventRecord(*a, c->stream);
   return 1;
 }
+
+int prof_begin(tp3_ctx* c, cudaEvent_t* a, cudaEvent_t* b) { return prof_begin_in(c, c->ev, c->ev_used, a, b); }
 
 // Gather + coupling stage for n proposals whose FP64 coefficients are in d_coeff.
 int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool compact = false,
@@ -464,6 +466,8 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
   if (is_tc(c->mode)) {
     if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream, rag)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
+    cudaEvent_t ca, cb;
+    const int pc = prof_begin_in(c, c->ev_c, c->ev_c_used, &ca, &cb);
     if (rag)  // ragged batches use the one-kernel coupling (it skips absent blocks and shells)
       e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, c->mode == TP3_MODE_TC_TF32X3,
                                   want_T32 ? c->d_T : nullptr, c->stream, rag);
@@ -474,6 +478,7 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
       e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, c->mode == TP3_MODE_TC_TF32X3,
                                   want_T32 ? c->d_T : nullptr, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "coupling");
+    if (pc) cudaEventRecord(cb, c->stream);
   } else {
     if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
     if ((e = tp3::launch_couple_direct(t, n, c->d_cc, c->d_T, c->stream)) != cudaSuccess)
@@ -822,6 +827,7 @@ void tp3_ctx_destroy(tp3_ctx* c) {
   cudaFree(c->d_err);
   cudaFreeHost(c->h_err);
   for (auto ev : c->ev) cudaEventDestroy(ev);
+  for (auto ev : c->ev_c) cudaEventDestroy(ev);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
 }
@@ -1230,23 +1236,31 @@ int tp3_profile_enable(tp3_ctx* c, int on) {
   if (int r = check_ctx(c)) return r;
   c->prof = on != 0;
   c->ev_used = 0;
+  c->ev_c_used = 0;
+  return TP3_OK;
+}
+
+int tp3_profile_read_stage(tp3_ctx* c, int stage, int64_t* launches, double* total_ms) {
+  if (int r = check_ctx(c)) return r;
+  if (!launches || !total_ms) return fail(c, TP3_ERR_ARG, "NULL pointer");
+  if (stage != 0 && stage != 1) return fail(c, TP3_ERR_ARG, "stage must be 0 (angular) or 1 (coupling)");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "profile sync");
+  std::vector<cudaEvent_t>& ev = stage == 0 ? c->ev : c->ev_c;
+  size_t& used = stage == 0 ? c->ev_used : c->ev_c_used;
+  double ms = 0.0;
+  for (size_t i = 0; i + 1 < used; i += 2) {
+    float f = 0.f;
+    if (cudaEventElapsedTime(&f, ev[i], ev[i + 1]) == cudaSuccess) ms += f;
+  }
+  *launches = (int64_t)(used / 2);
+  *total_ms = ms;
+  used = 0;
   return TP3_OK;
 }
 
 int tp3_profile_read(tp3_ctx* c, int64_t* launches, double* total_ms) {
-  if (int r = check_ctx(c)) return r;
-  if (!launches || !total_ms) return fail(c, TP3_ERR_ARG, "NULL pointer");
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "profile sync");
-  double ms = 0.0;
-  for (size_t i = 0; i + 1 < c->ev_used; i += 2) {
-    float f = 0.f;
-    if (cudaEventElapsedTime(&f, c->ev[i], c->ev[i + 1]) == cudaSuccess) ms += f;
-  }
-  *launches = (int64_t)(c->ev_used / 2);
-  *total_ms = ms;
-  c->ev_used = 0;
-  return TP3_OK;
+  return tp3_profile_read_stage(c, 0, launches, total_ms);
 }
 
 }  // extern "C"

@@ -76,10 +76,13 @@ struct tp3_ctx {
   double* d_delta = nullptr;
   int* d_doff = nullptr;
 
-  // profiling of the angular + Bayes kernel
+  // profiling: event pairs around each launch of the angular + Bayes kernel (ev) and
+  // of the coupling kernel of the tensor-core path (ev_c)
   bool prof = false;
   std::vector<cudaEvent_t> ev;  // pairs
   size_t ev_used = 0;
+  std::vector<cudaEvent_t> ev_c;
+  size_t ev_c_used = 0;
 };
 
 

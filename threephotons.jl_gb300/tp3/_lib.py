@@ -100,6 +100,8 @@ SIGNATURES = {
     "tp3_selftest_timeout": (c_int, [c_void_p, ctypes.c_longlong]),
     "tp3_profile_enable": (c_int, [c_void_p, c_int]),
     "tp3_profile_read": (c_int, [c_void_p, P(c_int64), P(c_double)]),
+    "tp3_profile_read_stage": (c_int, [c_void_p, c_int, P(c_int64), P(c_double)]),
+    "tp3_measure_fp32_peak": (c_int, [c_void_p, P(c_double)]),
 }
 
 _lib = None

@@ -266,11 +266,18 @@ class BasisTypeGB300:
     def profile_enable(self, on: bool) -> None:
         check(self._lib.tp3_profile_enable(self._ctx, int(on)), self._ctx)
 
-    def profile_read(self):
+    def profile_read(self, stage: int = 0):
+        """(launches, summed ms) of stage 0 (angular + Bayes) or 1 (coupling) since the last read."""
         n = ctypes.c_int64()
         ms = ctypes.c_double()
-        check(self._lib.tp3_profile_read(self._ctx, ctypes.byref(n), ctypes.byref(ms)), self._ctx)
+        check(self._lib.tp3_profile_read_stage(self._ctx, int(stage), ctypes.byref(n), ctypes.byref(ms)), self._ctx)
         return n.value, ms.value
+
+    def measure_fp32_peak(self) -> float:
+        """Measured FP32 FMA peak of the device in TFLOP/s (the coupling stage's roofline)."""
+        v = ctypes.c_double()
+        check(self._lib.tp3_measure_fp32_peak(self._ctx, ctypes.byref(v)), self._ctx)
+        return v.value
 
 
 def calculate_basis(L: int, LMAX: int, N: int, K: int, lambda_: float = 0.0, dq: float = 0.0,
