@@ -103,7 +103,8 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * and up to 225 KB of shared memory per CTA; 2: the same with 256 threads and 110 KB so
  * two CTAs share an SM; 3: warp-local one-kernel coupling, warps taking (k1, k2-quad)
  * units from a counter with no CTA barrier, 512 threads; 4: the warp-local coupling
- * with 256 threads and 110 KB, two CTAs per SM; 1: two-kernel split coupling through
+ * with 256 threads, two CTAs per SM in 110 KB each where that fits, else one with up
+ * to 225 KB; 1: two-kernel split coupling through
  * global memory) -- selects
  * the fastest for this context and records it for the shape (L, LMAX, N, K, lambda,
  * dq) in the process, where TP3_MODE_AUTO finds it.  report (nullable): up to *nreport

@@ -234,10 +234,13 @@ std::string setup_tc(tp3_ctx* c) {
     tc.w_smem_w = base + (size_t)wmax * 4 + dw <= limit;
     tc.couple_smem_w = base + (tc.w_smem_w ? (size_t)wmax * 4 : 0) + dw;
     tc.warp_ok = tc.couple_smem_w <= limit && b.K <= 64;
+    // 256 threads: two CTAs per SM when the layout fits 110 KB, else one CTA per SM
+    // with up to the full dynamic shared memory (large K and L, where 16 warps' D does not fit)
     const size_t dw2 = (size_t)8 * 4 * tc.SDp * sizeof(float2);
-    tc.w_smem_w2 = base + (size_t)wmax * 4 + dw2 <= limit_s;
+    const size_t lim2 = base + dw2 <= limit_s ? limit_s : limit;
+    tc.w_smem_w2 = base + (size_t)wmax * 4 + dw2 <= lim2;
     tc.couple_smem_w2 = base + (tc.w_smem_w2 ? (size_t)wmax * 4 : 0) + dw2;
-    tc.warp2_ok = tc.couple_smem_w2 <= limit_s && b.K <= 64;
+    tc.warp2_ok = tc.couple_smem_w2 <= lim2 && b.K <= 64;
   }
   // split coupling: D offsets, L2-sized sub-batches, balanced (pair block, m3 range) units
   const int npairs = b.K * (b.K + 1) / 2;

@@ -827,7 +827,7 @@ cudaError_t tc_configure() {
   if ((e = cudaFuncSetAttribute(k_couple_warp<S, W, kCoupleThreads>,                                         \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||          \
       (e = cudaFuncSetAttribute(k_couple_warp<S, W, kCoupleThreadsSmall>,                                    \
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, css)) != cudaSuccess)           \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)            \
     return e;
   TP3_CW_ATTR(4, true) TP3_CW_ATTR(8, true) TP3_CW_ATTR(10, true) TP3_CW_ATTR(12, true) TP3_CW_ATTR(16, true)
   TP3_CW_ATTR(4, false) TP3_CW_ATTR(8, false) TP3_CW_ATTR(10, false) TP3_CW_ATTR(12, false)
