@@ -213,8 +213,35 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads(), "kind": "port",
                              "sample": f"{args.steps} timed proposals (+{args.warmup} warm-up) of the workload"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["reference_cuda"] = reference_cuda_rate(ref, props, hist)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_cuda_rate(ref, props, hist, calls: int = 3):
+    """The reference's own GPU path for the same workload, beside its CPU path: the
+    unmodified src/cuda_kernel.cu kernel (PTX built from the reference sources where they
+    were present) scaling h_P into PA, FP32 SGEMM c3 = B PA, c3 to the host and the FP64
+    Bayes energy there (src/cuda.jl:74-108, src/correlations.jl:201).  Timed with the
+    per-call h_P upload the reference makes and with h_P kept on the device."""
+    try:
+        import torch
+        from oracle import refcuda
+        from oracle.c3 import energy_bayes
+        if not torch.cuda.is_available() or not refcuda.available():
+            return {"unavailable": "no GPU or the reference kernel's PTX was not built"}
+        timer = refcuda.RefCudaTimer(ref.b, ref.B32, ref.hP)
+        out = {"kernel": "src/cuda_kernel.cu calculate_coefficient_matrix (unmodified, PTX) + FP32 SGEMM (cuBLAS, "
+                         "TF32 off) + FP64 host Bayes", "unit": UNIT, "calls": calls}
+        for key, up in (("value", True), ("value_hP_resident", False)):
+            energy_bayes(timer.c3(props[0], up), hist, ref.K, ref.N)  # warm-up
+            t0 = time.perf_counter()
+            for i in range(calls):
+                energy_bayes(timer.c3(props[1 + i % (len(props) - 1)], up), hist, ref.K, ref.N)
+            out[key] = calls / (time.perf_counter() - t0)
+        return out
+    except Exception as exc:  # the baseline is informational: report why it is missing
+        return {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
 
 
 def _molecule_job(args):

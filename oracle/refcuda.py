@@ -99,3 +99,73 @@ def c3_reference_cuda(b: OracleBasis, coeff: np.ndarray, B32: np.ndarray, P32: n
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
     return c3.double().cpu().numpy()
+
+
+class RefCudaTimer:
+    """The same host sequence as c3_reference_cuda with the module and the read-only
+    tables (coefficient-independent: wignerlist, indices, PAcombos, B) kept on the device,
+    for timing repeated calls.  Each call uploads h_P again (src/cuda.jl:80 sends it with
+    every call because the kernel scales it in place into PA) or, with upload_hP=False,
+    restores it from a device copy; then the kernel, the SGEMM and the D2H of c3."""
+
+    def __init__(self, b: OracleBasis, B32: np.ndarray, P32: np.ndarray):
+        import torch
+        if not available():
+            raise FileNotFoundError(f"{PTX} not built")
+        torch.cuda.init()
+        self.torch = torch
+        self.dev = dev = torch.device("cuda")
+        self.b = b
+        K, LMAX = b.K, b.LMAX
+        self.numcoeff = LMAX * LMAX
+        combos = combolist(b)
+        self.ncombo = combos.shape[1]
+        assert combos[0:3].min() >= 1 and combos[0:3].max() <= K
+        assert combos[3].min() >= 1 and combos[3].max() <= b.klength
+        assert combos[7].min() >= 1 and (combos[7] + combos[8] - 1).max() <= b.basislen
+        assert b.indices[0:3].min() >= 1 and b.indices[0:3].max() <= self.numcoeff
+        assert P32.shape == (b.basislen, b.klength) and B32.shape == (2 * b.N * b.N, b.basislen)
+        self.d_w = torch.from_numpy(b.wignerlist.astype(np.float32)).to(dev)
+        self.d_idx = torch.from_numpy(np.ascontiguousarray(b.indices.T.astype(np.int32)).reshape(-1)).to(dev)
+        self.d_comb = torch.from_numpy(np.ascontiguousarray(combos.T.astype(np.int32)).reshape(-1)).to(dev)
+        self.h_P = np.asfortranarray(P32).T.copy().reshape(-1)               # column-major basislen x klength
+        self.d_P0 = torch.from_numpy(self.h_P).to(dev)                      # pristine copy (resident variant)
+        self.d_PA = torch.empty_like(self.d_P0)
+        self.Bm = torch.from_numpy(np.ascontiguousarray(B32)).to(dev)
+        cu = _driver()
+        self.mod = ctypes.c_void_p()
+        ptx = open(PTX, "rb").read() + b"\0"
+        if cu.cuModuleLoadData(ctypes.byref(self.mod), ptx) != 0:
+            raise RuntimeError("cuModuleLoadData failed")
+        self.fn = ctypes.c_void_p()
+        if cu.cuModuleGetFunction(ctypes.byref(self.fn), self.mod, b"calculate_coefficient_matrix") != 0:
+            raise RuntimeError("cuModuleGetFunction failed")
+        torch.cuda.synchronize()
+
+    def c3(self, coeff: np.ndarray, upload_hP: bool = True) -> np.ndarray:
+        torch, b = self.torch, self.b
+        c = np.ascontiguousarray(np.asarray(coeff)[: b.K], dtype=np.complex64)
+        d_coeff = torch.from_numpy(c.view(np.float32).reshape(-1)).to(self.dev)
+        if upload_hP:
+            self.d_PA.copy_(torch.from_numpy(self.h_P))
+        else:
+            self.d_PA.copy_(self.d_P0)
+        torch.cuda.synchronize()
+        args = [ctypes.c_void_p(d_coeff.data_ptr()), ctypes.c_int(self.numcoeff), ctypes.c_void_p(self.d_w.data_ptr()),
+                ctypes.c_void_p(self.d_idx.data_ptr()), ctypes.c_int(b.basislen),
+                ctypes.c_void_p(self.d_comb.data_ptr()), ctypes.c_int(self.ncombo),
+                ctypes.c_void_p(self.d_PA.data_ptr()), ctypes.c_int(b.klength)]
+        params = (ctypes.c_void_p * len(args))(*[ctypes.cast(ctypes.pointer(a), ctypes.c_void_p) for a in args])
+        cu = _driver()
+        if cu.cuLaunchKernel(self.fn, (self.ncombo + 1023) // 1024, 1, 1, 1024, 1, 1, 0, None, params, None) != 0:
+            raise RuntimeError("cuLaunchKernel failed")
+        if cu.cuCtxSynchronize() != 0:
+            raise RuntimeError("reference kernel failed")
+        PA = self.d_PA.view(b.klength, b.basislen).t()
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        try:
+            c3 = self.Bm @ PA
+        finally:
+            torch.backends.cuda.matmul.allow_tf32 = prev
+        return c3.cpu().numpy()
