@@ -633,8 +633,8 @@ int tp3_mlp_create(tp3_ctx* c, int n_in, int hidden, int max_rows, uint64_t seed
     cudaGetLastError();
     return tp3::ctx_fail(c, TP3_ERR_ALLOC, std::string("mlp allocation: ") + cudaGetErrorString(e));
   }
-  // He-uniform initial weights (last layer scaled by 0.01 so the first proposals are
-  // close to mu = 0, s = kSMid); zero biases
+  // He-uniform initial weights (last layer scaled by 0.01 so the first outputs are
+  // close to u = 0, s = kSMid); zero biases
   std::vector<float> par(off, 0.f);
   uint64_t st = seed ^ 0x6d6c7033ull;
   for (int l = 0; l < 4; ++l) {
