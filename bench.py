@@ -492,7 +492,9 @@ def main():
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch", "peak_source": f"{peak_src} bf16 dense burst",
                 "kernel": "angular contraction + fused Bayes", "kernel_ms_per_launch": per_launch_ms,
-                "algorithmic_flop_per_proposal": W_b}
+                "algorithmic_flop_per_proposal": W_b,
+                "note": "the tensor-core stage; the longest-running kernel is the SIMT FP32 coupling, whose "
+                        "roofline against the measured FP32 FMA peak is stages.coupling"}
 
     # per-stage rooflines: the coupling (SIMT FP32) against the measured FFMA peak, the
     # angular contraction against the BF16 tensor peak
