@@ -257,3 +257,29 @@ def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
               f"{res['learned']['launches']} launches {res['learned']['seconds_to_target']:.3f} s -> "
               f"{res['learned']['median_E']:.4f} (reached={res['learned']['reached']}, "
               f"time ratio={res['time_ratio']})")
+
+
+def test_learned_proposal_gain_at_production_shape(capsys):
+    """A shortened run of the benchmark's protocol at L18 K26 N32 (64 chains x 16
+    candidates: 300 logged launches, 600 Adam steps, 150 evaluation launches): the
+    learned annealer reaches the plain annealer's final median energy in well under its
+    wall-clock (the full protocol, bench.py --workload learned, measures about 0.25)."""
+    import os
+    import sys
+    from tp3.learned import learned_vs_plain
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    base = bench.molecule_coefficients()
+    basis = tp3.calculate_basis(bench.L, bench.LMAX, bench.N, bench.K)
+    try:
+        basis.set_histogram(bench.build_histogram(basis, base))
+        basis.set_mode(tp3.TP3_MODE_TC_BF16X3)
+        res = learned_vs_plain(basis, base, collect_launches=300, train_steps=600, eval_launches=150, seed=31)
+    finally:
+        basis.close()
+    assert res["learned"]["reached"]
+    assert res["time_ratio"] < 0.75, res["time_ratio"]
+    with capsys.disabled():
+        print(f"\n[learned proposal, L18 K26 N32, shortened] plain {res['plain']['seconds']:.2f} s -> "
+              f"{res['plain']['final_median_E']:.3f}; learned {res['learned']['seconds_to_target']:.2f} s "
+              f"({res['learned']['launches']} launches), time ratio {res['time_ratio']:.3f}")
