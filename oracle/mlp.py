@@ -113,11 +113,13 @@ def init_params(n_in: int, H: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride: int, ghist=None) -> np.ndarray:
+def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride: int, ghist=None,
+                   L_used: int = None) -> np.ndarray:
     """Feature rows (K x stride, BF16 values) of a state's shells: (L+1)^2 real SH
     coefficients x = Umat(l) c_l scaled to norm 8, the 8 history values dE/T clipped to
     +-10 and divided by 10, log10(T)/4, the shell's gradient estimates of the last 8
-    launches (ghist [8][K][3], newest first; FP32, clipped to +-8 and halved), zeros."""
+    launches (ghist [8][K][3], newest first; FP32, clipped to +-8 and halved), zeros.
+    L_used (a ragged chain's own L <= L): coefficient columns of orders above it are zero."""
     from .sh import Umat, seanindex
     K = coeff.shape[0]
     nf = (L + 1) ** 2
@@ -126,6 +128,9 @@ def shell_features(coeff: np.ndarray, L: int, LMAX: int, hist, T: float, stride:
     for k in range(K):
         x = []
         for l in range(L + 1):
+            if L_used is not None and l > L_used:
+                x.extend([0.0] * (2 * l + 1))
+                continue
             idx = [seanindex(l, m, LMAX) - 1 for m in range(-l, l + 1)]
             x.extend((Umat(l) @ coeff[k, idx]).real)
         x = np.asarray(x, dtype=np.float32).astype(np.float64)

@@ -111,3 +111,79 @@ def test_ragged_chains_follow_per_shape_chains(world):
         assert agree >= min(n, 3)
         sep.close()
     rag.close()
+
+
+def test_learned_moves_on_ragged_chains_match_oracle(world):
+    """Learned moves on chains of different (L, K) in one context: each chain's feature
+    rows carry its own orders only, its steps rotate its own orders, and the logged
+    features, two-sided steps, Metropolis-Hastings ratios and energy changes match the
+    oracle (per-shape contexts score the moved structures)."""
+    import torch
+    from tp3.learned import ProposalMLP, n_in_for
+    from oracle import mlp as om
+    big, ctxs, hists, mols = world
+    nch, B, seed = len(SHAPES), 4, 4242
+    n_in = n_in_for(LBIG)
+    stride = (n_in + 31) // 32 * 32
+    net = ProposalMLP(big, n_in, hidden=64, max_rows=((nch * B * KBIG + 127) // 128) * 128, seed=3)
+    params = om.init_params(n_in, 64, 5)
+    params[-6 - 6 * 64:-6] *= 0.3
+    params[-6:-3] = 0.0
+    params[-3:] = math.atanh((0.0 - om.S_MID) / om.S_HALF)
+    net.set_params(params)
+    starts = np.stack([m[:KBIG] for m in mols])
+    T0, sigma0, decay, p_net = 0.5, 0.3, 0.99, 0.8
+    ch = Chains(big, starts, T0, math.pi / 8, 1.05, decay, seed, ncand=B,
+                shapes=[(L, K, h) for h, (L, K) in enumerate(SHAPES)])
+    ch.set_move(tp3.TP3_MOVE_LEARNED, sigma0, p_net, net)
+    ch.enable_move_log(2)
+    ch.run(1)
+    n = ch.move_log_count()
+    assert n == nch * B
+    dev = torch.device("cuda")
+    idx = torch.arange(n, dtype=torch.int64, device=dev)
+    X = torch.empty((n * KBIG, stride), dtype=torch.bfloat16, device=dev)
+    V = torch.empty((n * KBIG, 3), dtype=torch.float32, device=dev)
+    M = torch.empty((n, 7), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    ch.move_log_gather(n, idx.data_ptr(), X.data_ptr(), V.data_ptr(), M.data_ptr())
+    torch.cuda.synchronize()
+    X, V, M = X.float().cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64), M.cpu().numpy()
+
+    def dev_head(feats):
+        d_x = torch.tensor(feats, dtype=torch.bfloat16, device=dev)
+        out = torch.empty((feats.shape[0], 6), dtype=torch.float32, device=dev)
+        net.forward_device(feats.shape[0], d_x.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        o = out.cpu().numpy().astype(np.float64)
+        return o[:, :3], o[:, 3:]
+
+    hist0, ghist0 = np.zeros(8), np.zeros((8, KBIG, 3))
+    nf = (LBIG + 1) ** 2
+    for c, (L, K) in enumerate(SHAPES):
+        start = starts[c]
+        E0 = ctxs[c].energy_batch(start[None, :K])[0]
+        for i in range(B):
+            j = c * B + i
+            T = T0 * decay ** (i + 1)
+            feats = om.shell_features(start, LBIG, LMAX, hist0, T, stride, ghist0, L_used=L)
+            Xd = X[j * KBIG:(j + 1) * KBIG]
+            assert np.all(np.abs(Xd - feats) <= 2 ** -7 * np.abs(feats) + 1e-30)
+            assert np.all(Xd[:, (L + 1) ** 2:nf] == 0.0)  # orders above the chain's L
+            comp = 1.0 if oc.component_uniform(seed, i, c) < p_net else 0.0
+            assert M[j, 3] == comp
+            z, a = oc.shell_noise(seed, 0, c, i, KBIG)
+            sig_i = sigma0 / 1.05 ** i
+            v = V[j * KBIG:(j + 1) * KBIG] * M[j, 5]
+            m, s = oc.shell_params(*dev_head(Xd), sig_i)
+            vref = a * m + np.exp(s) * z if comp else sig_i * z
+            np.testing.assert_allclose(v, vref, rtol=1e-5, atol=1e-6)
+            x2 = oc.rotate_shells(start, v, L, LMAX)
+            m2, s2 = oc.shell_params(*dev_head(om.shell_features(x2, LBIG, LMAX, hist0, T, stride, ghist0,
+                                                                 L_used=L)), sig_i)
+            lr = oc.mixture_log_ratio(v, m, s, m2, s2, sig_i, p_net)
+            assert M[j, 4] == pytest.approx(lr, abs=0.05 + 0.01 * abs(lr))
+            E2 = ctxs[c].energy_batch(x2[None, :K])[0]
+            assert M[j, 0] == pytest.approx(E2 - E0, abs=2e-6 * abs(E0))
+    ch.close()
+    net.close()

@@ -345,14 +345,17 @@ __global__ void k_select(ChainState* __restrict__ cs, double* __restrict__ sigma
 // Feature rows of the proposal network (layout in mlp.h).  grid: nch * nb * K blocks
 // (row = (chain, candidate i < nb, shell)), block 128.  coef: per-row source set,
 // src_per_chain ? state[chain] : cand[chain * B + i].  X (nullable): rows of stride
-// xs; logf (nullable): the i = 0 rows also go to the launch's log slot.
+// xs; logf (nullable): the i = 0 rows also go to the launch's log slot.  rag
+// (nullable, ragged chains): a chain's coefficient features stop at its own L (the
+// columns of higher orders, which its model does not have, are zero).
 __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ coef, int src_per_chain, int nch, int nb,
                                                   int B, int K, int LMAX, int L, const ChainState* __restrict__ cs,
                                                   double decay, const float* __restrict__ hist,
                                                   const float* __restrict__ ghist,
                                                   __nv_bfloat16* __restrict__ X, int xs,
                                                   __nv_bfloat16* __restrict__ logf,
-                                                  const long long* __restrict__ launch_ctr, int log_cap) {
+                                                  const long long* __restrict__ launch_ctr, int log_cap,
+                                                  const tp3::RagInfo* __restrict__ rag) {
   __shared__ float red[4];
   __shared__ float sx[(kMaxL + 1) * (kMaxL + 1)];
   const int row = blockIdx.x;
@@ -360,6 +363,7 @@ __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ co
   const int ncoef = LMAX * LMAX;
   const double2* src = coef + ((size_t)(src_per_chain ? c : c * B + i) * K + k) * ncoef;
   const int nf = (L + 1) * (L + 1);
+  const int Lc = rag ? rag[(size_t)c * B + i].L : L;  // the chain's own orders
   const double r2 = 0.7071067811865476;
   float ss = 0.f;
   for (int t = threadIdx.x; t < nf; t += blockDim.x) {
@@ -367,7 +371,9 @@ __global__ void __launch_bounds__(128) k_features(const double2* __restrict__ co
     while ((l + 1) * (l + 1) <= t) ++l;
     const int u = t - l * l - l;  // -l..l
     double x;
-    if (u == 0) {
+    if (l > Lc) {
+      x = 0.0;
+    } else if (u == 0) {
       x = src[tp3::sean0(l, 0, LMAX)].x;
     } else if (u > 0) {  // (c_u + (-1)^u c_-u) / sqrt2
       const double2 a = src[tp3::sean0(l, u, LMAX)], b = src[tp3::sean0(l, -u, LMAX)];
@@ -726,7 +732,7 @@ int chains_enqueue(tp3_chains* h) {
     if (net || mlog)
       k_features<<<h->nch * (net ? h->B : 1) * h->K, 128, 0, c->stream>>>(
           h->d_state, 1, h->nch, net ? h->B : 1, h->B, h->K, h->LMAX, h->L, h->d_cs, h->decay, h->d_hist, h->d_ghist,
-          X, h->xs, mlog ? h->d_lfeat : nullptr, lctr, h->mlog_cap);
+          X, h->xs, mlog ? h->d_lfeat : nullptr, lctr, h->mlog_cap, h->d_rag);
     if (net) {
       if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
@@ -739,7 +745,7 @@ int chains_enqueue(tp3_chains* h) {
     if (net) {
       k_features<<<n * h->K, 128, 0, c->stream>>>(h->d_cand, 0, h->nch, h->B, h->B, h->K, h->LMAX, h->L, h->d_cs,
                                                    h->decay, h->d_hist, h->d_ghist, X, h->xs, nullptr, lctr,
-                                                   h->mlog_cap);
+                                                   h->mlog_cap, h->d_rag);
       if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "features");
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
       k_mh_ratio<<<n, 64, 0, c->stream>>>(O, h->d_v, h->d_lq, h->K, h->p_net, h->d_cs, h->d_sigma, h->nl, h->B, h->f,
@@ -1071,7 +1077,6 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
     if ((e = cudaGetLastError()) != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "set sigma0");
   }
   if (kind == TP3_MOVE_LEARNED) {
-    if (h->d_rag) return tp3::ctx_fail(c, TP3_ERR_UNSUPPORTED, "learned moves need chains of one shape");
     if (!net) return tp3::ctx_fail(c, TP3_ERR_ARG, "learned moves need a network");
     if (!(p_net > 0.0 && p_net <= 1.0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "p_net must be in (0, 1]");
     if (tp3::mlp_n_in_of(net) != tp3::mlp_n_in(h->L))
