@@ -246,7 +246,8 @@ def learned_vs_plain(basis, base: np.ndarray, nchains: int = 64, ncand: int = 16
     """The learned-proposal experiment on the basis's histogram (set beforehand):
     1. the plain annealer (isotropic per-shell steps) logs its moves from Haar-rotated
        starts (collect_launches x nchains x ncand candidates);
-    2. the network is trained on the device on the weighted NLL of those moves;
+    2. the network is trained on the device on those moves (regression of their energy
+       changes on the steps through the drift heads, NLL of the steps under the log-scales);
     3. from fresh starts (another seed), the plain annealer runs eval_launches launches;
        its final median energy is the target;
     4. the learned annealer (mixture p_net network / isotropic, MH-corrected) runs from
