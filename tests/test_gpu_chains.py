@@ -1,8 +1,8 @@
 """Device-resident annealing chains vs the sequential FP64 oracle chain.
 
-North-star correctness part 4: seeded plain chains reproduce the reference
-method's accept/reject sequence except at steps whose decision lies within the
-energy tolerance (|dE| or |dE + T log u| below 1e-6 |E| + 1e-9).
+Seeded plain chains reproduce the reference method's accept/reject sequence
+except at steps whose decision lies within the energy tolerance (|dE| or
+|dE + T log u| below 1e-6 |E| + 1e-9).
 """
 import math
 

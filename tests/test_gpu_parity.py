@@ -1,6 +1,6 @@
 """GPU parity of libtp3 against the oracle, called through the C ABI.
 
-Tolerances (spec correctness parts 1-3):
+Tolerances:
   c3 relative L1 vs the reference-form restatement   <= 1e-5  (tests/test_cuda.jl:15)
   energy relative vs the reference-form restatement  <= 1e-6  (tests/test_cuda.jl:34)
   c3 max / RMS error vs the FP64 oracle are asserted below stated bounds.

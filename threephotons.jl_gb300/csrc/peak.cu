@@ -1,5 +1,5 @@
 // Measured FP32 FMA peak of the device: the roofline denominator of the coupling
-// stage (SIMT FP32), which the measured peaks (HBM copy, BF16 GEMM) do not
+// stage (SIMT FP32), which measured copy bandwidth and BF16 GEMM peaks do not
 // cover.  Every thread runs 8 independent FMA chains; the grid fills every SM with
 // 2048 threads.  No reference counterpart.
 #include <cuda_runtime.h>
