@@ -29,6 +29,24 @@ def test_header_symbols_exported():
     assert set(syms) == set(_lib.SIGNATURES), "ctypes table out of sync with include/tp3.h"
 
 
+def test_julia_shim_binds_declared_symbols():
+    """Every ccall of the Julia shim names an entry point that include/tp3.h declares and
+    libtp3.so exports, with as many argument types as the declaration has parameters."""
+    shim = os.path.join(os.path.dirname(HEADER), "..", "threephotons.jl_gb300", "julia", "ThreePhotonsGB300.jl")
+    src = open(shim).read()
+    calls = re.findall(r"ccall\(\(:(tp3_[A-Za-z0-9_]+), libtp3\), *\w+, *\(([^)]*)\)", src)
+    assert len(calls) >= 20
+    header = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    lib = tp3.load()
+    for name, argtypes in calls:
+        assert hasattr(lib, name), name
+        m = re.search(r"\b" + name + r"\s*\(([^)]*)\)", header)
+        assert m, name
+        nparams = 0 if m.group(1).strip() in ("", "void") else len(m.group(1).split(","))
+        nargs = len([a for a in argtypes.split(",") if a.strip()])
+        assert nargs == nparams, (name, nargs, nparams)
+
+
 def test_status_strings():
     for s in range(0, 10):
         assert _lib.status_string(s)

@@ -14,7 +14,10 @@ module ThreePhotonsGB300
 import ThreePhotons: AbstractBasisType, SphericalHarmonicsVolume, FullCorrelation_parallized, energy,
                      Umat, C3, num_coeff
 
-export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_run, GB300_chains_state
+export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_run, GB300_chains_state,
+       GB300_energy_batch, GB300_set_mode, GB300_autotune, GB300_chains_log, GB300_chains_snapshot,
+       GB300_chains_restore, GB300_chains_coeff, GB300_chains_destroy, GB300_chains_set_move,
+       GB300_chains_enable_move_log, GB300_mlp_create, GB300_mlp_destroy
 
 const libtp3 = joinpath(@__DIR__, "..", "lib", "libtp3.so")
 
@@ -117,6 +120,33 @@ end
 energy(intensity::SphericalHarmonicsVolume, basis::BasisTypeGB300, c3ref::C3, measure::String="Bayes",
        negativity_factor::Float64=0.0) = energy(intensity, basis, c3ref, 1:basis.K, measure, negativity_factor)
 
+"""Energies of many structures in one launch sequence (the 50 energies of
+calculate_temperature, src/determination.jl:244-261; tp3_energy_batch)."""
+function GB300_energy_batch(intensities::Vector{SphericalHarmonicsVolume}, basis::BasisTypeGB300, c3ref::C3)
+    set_histogram!(basis, c3ref)
+    coeff = cat(3, [pack(s, basis) for s in intensities]...)   # LMAX^2 x K x n, column-major
+    E = zeros(Float64, length(intensities))
+    check(ccall((:tp3_energy_batch, libtp3), Int32, (Ptr{Void}, Int32, Ptr{Complex{Float64}}, Ptr{Float64}),
+                basis.ctx, length(intensities), coeff, E), basis.ctx)
+    return E
+end
+
+"""Evaluation mode: 0 plain FP32, 1 tensor-core BF16 hi/lo x3, 2 TF32 hi/lo x3, -1 the
+fastest one recorded by the autotuner for this shape (tp3_set_mode)."""
+GB300_set_mode(basis::BasisTypeGB300, mode::Int) =
+    check(ccall((:tp3_set_mode, libtp3), Int32, (Ptr{Void}, Int32), basis.ctx, mode), basis.ctx)
+
+"""Time every evaluation variant on n synthetic proposals and keep the fastest
+(tp3_autotune); rows (mode, coupling form, ms per proposal)."""
+function GB300_autotune(basis::BasisTypeGB300, n::Int=64)
+    cap = 32
+    rep = zeros(Float64, 3, cap)
+    nrep = Ref{Int32}(cap)
+    check(ccall((:tp3_autotune, libtp3), Int32, (Ptr{Void}, Int32, Ptr{Float64}, Ref{Int32}),
+                basis.ctx, n, rep, nrep), basis.ctx)
+    return rep[:, 1:min(nrep[], cap)]
+end
+
 # ---- device-resident chains (rotate_all_at_once on the GPU) ---------------------------
 function GB300_chains_create(basis::BasisTypeGB300, starts::Vector{SphericalHarmonicsVolume}, T0::Vector{Float64},
                              initial_stepsize::Float64, stepsizefactor::Float64, temperature_decay::Float64,
@@ -133,6 +163,62 @@ end
 
 GB300_chains_run(basis::BasisTypeGB300, h::Ptr{Void}, launches::Int) =
     check(ccall((:tp3_chains_run, libtp3), Int32, (Ptr{Void}, Int32), h, launches), basis.ctx)
+
+GB300_chains_destroy(h::Ptr{Void}) = ccall((:tp3_chains_destroy, libtp3), Void, (Ptr{Void},), h)
+
+"""The last steps of one chain (the det.out columns of src/determination.jl:512-514):
+8 x n rows of step, sign, E_new, E, dE, T, acceptance probability, sigma_L."""
+function GB300_chains_log(basis::BasisTypeGB300, h::Ptr{Void}, chain::Int, capacity::Int)
+    rows = zeros(Float64, 8, capacity)
+    n = Ref{Int64}(0)
+    check(ccall((:tp3_chains_log, libtp3), Int32, (Ptr{Void}, Int32, Ptr{Float64}, Ref{Int64}),
+                h, chain, rows, n), basis.ctx)
+    return rows[:, 1:n[]]
+end
+
+"""Current coefficients of n chains (LMAX^2 x K x n)."""
+function GB300_chains_coeff(basis::BasisTypeGB300, h::Ptr{Void}, n::Int)
+    c = Array{Complex{Float64}}(num_coeff(basis.LMAX), basis.K, n)
+    check(ccall((:tp3_chains_coeff, libtp3), Int32, (Ptr{Void}, Ptr{Complex{Float64}}), h, c), basis.ctx)
+    return c
+end
+
+"""Checkpoint of the chain set (the role of saveState, src/determination.jl:264-267)."""
+function GB300_chains_snapshot(basis::BasisTypeGB300, h::Ptr{Void})
+    nbytes = Ref{Csize_t}(0)
+    check(ccall((:tp3_chains_snapshot, libtp3), Int32, (Ptr{Void}, Ptr{Void}, Csize_t, Ref{Csize_t}),
+                h, C_NULL, 0, nbytes), basis.ctx)
+    buf = zeros(UInt8, nbytes[])
+    check(ccall((:tp3_chains_snapshot, libtp3), Int32, (Ptr{Void}, Ptr{UInt8}, Csize_t, Ref{Csize_t}),
+                h, buf, length(buf), nbytes), basis.ctx)
+    return buf
+end
+
+GB300_chains_restore(basis::BasisTypeGB300, h::Ptr{Void}, buf::Vector{UInt8}) =
+    check(ccall((:tp3_chains_restore, libtp3), Int32, (Ptr{Void}, Ptr{UInt8}, Csize_t), h, buf, length(buf)),
+          basis.ctx)
+
+"""Move of a chain set: 0 the reference's get_MC_step, 1 per-shell SO(3) steps, 2 the
+learned mixture (network `net` with probability p_net), Metropolis-Hastings corrected."""
+GB300_chains_set_move(basis::BasisTypeGB300, h::Ptr{Void}, kind::Int, sigma0::Float64, p_net::Float64=0.0,
+                      net::Ptr{Void}=C_NULL) =
+    check(ccall((:tp3_chains_set_move, libtp3), Int32, (Ptr{Void}, Int32, Float64, Float64, Ptr{Void}),
+                h, kind, sigma0, p_net, net), basis.ctx)
+
+GB300_chains_enable_move_log(basis::BasisTypeGB300, h::Ptr{Void}, launches::Int) =
+    check(ccall((:tp3_chains_enable_move_log, libtp3), Int32, (Ptr{Void}, Int32), h, launches), basis.ctx)
+
+"""The proposal network (n_in = (L+1)^2 + 33 features per shell); trained from Python or
+any binding of tp3_mlp_train_step."""
+function GB300_mlp_create(basis::BasisTypeGB300, hidden::Int, max_rows::Int, seed::UInt64)
+    n_in = (basis.L + 1)^2 + 33
+    h = Ref{Ptr{Void}}(C_NULL)
+    check(ccall((:tp3_mlp_create, libtp3), Int32, (Ptr{Void}, Int32, Int32, Int32, UInt64, Ref{Ptr{Void}}),
+                basis.ctx, n_in, hidden, max_rows, seed, h), basis.ctx)
+    return h[]
+end
+
+GB300_mlp_destroy(net::Ptr{Void}) = ccall((:tp3_mlp_destroy, libtp3), Void, (Ptr{Void},), net)
 
 function GB300_chains_state(basis::BasisTypeGB300, h::Ptr{Void}, n::Int)
     E = zeros(n); T = zeros(n); steps = zeros(Int64, n); acc = zeros(Int64, n)
