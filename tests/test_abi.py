@@ -34,8 +34,8 @@ def test_julia_shim_binds_declared_symbols():
     libtp3.so exports, with as many argument types as the declaration has parameters."""
     shim = os.path.join(os.path.dirname(HEADER), "..", "threephotons.jl_gb300", "julia", "ThreePhotonsGB300.jl")
     src = open(shim).read()
-    calls = re.findall(r"ccall\(\(:(tp3_[A-Za-z0-9_]+), libtp3\), *\w+, *\(([^)]*)\)", src)
-    assert len(calls) >= 20
+    calls = re.findall(r"ccall\(\(:(tp3_[A-Za-z0-9_]+), libtp3\),\s*\w+,\s*\(([^)]*)\)", src)
+    assert len(calls) == src.count("ccall(("), "a ccall the pattern does not parse"
     header = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     lib = tp3.load()
     for name, argtypes in calls:
