@@ -257,11 +257,12 @@ int tp3_chains_graph(const tp3_chains* chains, int* captured);
 
 /* ---- scoring without device allocation ------------------------------------ */
 /* No counterpart in the reference.  Bayes energy of a model correlation that is
- * already in device memory, for callers that cannot allocate device memory at the
- * time they score: code recording the step into a CUDA graph by stream capture,
- * runtimes whose device memory belongs to their own pooling allocator, and loops
- * that must not stall on cudaMalloc's device synchronisation.  The call allocates
- * nothing and needs no context:
+ * already in device memory, for callers that may not allocate device memory at the
+ * time they score: a Julia host whose CUDA.jl memory pool owns the device memory (a
+ * foreign cudaMalloc can fail against the pool and synchronises the device inside the
+ * annealing loop), runtimes that work within a device-memory budget granted up front,
+ * and loops that must not stall on cudaMalloc/cudaFree's implicit synchronisation.
+ * The call allocates nothing and needs no context:
  *   d_c3   [klength][2N^2] float, device: c3 in tp3_c3's layout;
  *   d_qhat [klength][2N^2] float, device: histogram slabs, each L1-normalised;
  *   d_E    1 double, device: the energy (src/correlations.jl:201-226);
@@ -269,12 +270,16 @@ int tp3_chains_graph(const tp3_chains* chains, int* captured);
  * klength = K(K+1)(K+2)/6 must be <= 65536 (K <= 72): per-slab partials go to a
  * fixed 512 KiB array in the library's device memory that every GPU which loads
  * the library keeps until the process exits; larger K is rejected with
- * TP3_ERR_ARG.  The first call on each device looks up that array's address
- * (cudaGetSymbolAddress); make that first call before any stream capture.  All
- * calls share the array: calls whose kernels overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller.  Each call
- * writes every entry it reads, so no clearing is needed.  Asynchronous; errors in
- * the arguments return at once (detail in tp3_last_error(NULL)). */
+ * TP3_ERR_ARG.  Set-up: the first call in each CUDA context looks up that array's
+ * device address (cudaGetSymbolAddress, which also loads the library's module into
+ * the context); make that first call before any stream capture.  The address is
+ * looked up again when the calling thread's current context changes (a device reset
+ * makes a new one).  All calls share the array: calls whose kernels overlap on the
+ * GPU (other streams, other host threads) race on it and must be serialised by the
+ * caller.  Each call writes every entry it reads, so no clearing is needed.
+ * Asynchronous; errors in the arguments return at once, and a CUDA error left
+ * pending by earlier work is reported as such without launching (detail in
+ * tp3_last_error(NULL)). */
 int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, int K, int N, double* d_E, void* stream);
 
 /* ---- triplet histograms of photon pictures (src/datagen.jl:228-277) ---------- */

@@ -1,22 +1,22 @@
 // Bayes energy of a model correlation already in device memory, computed without
 // allocating any device memory.
 //
-// Who needs this: code that scores proposals from a place where cudaMalloc is not
-// available or not allowed, for example a caller that records the whole annealing
-// step into a CUDA graph by stream capture (an allocation during capture breaks the
-// capture), a host runtime whose device memory is owned by its own pooling
-// allocator (Julia's or PyTorch's caching allocators; a foreign cudaMalloc can fail
-// under their pool or fragment it), or a real-time loop that must not stall on the
-// implicit device synchronisation of cudaMalloc/cudaFree.  Such a caller passes its
-// own device buffers for inputs and output; the per-slab scratch lives in the
-// file-scope array below, which every GPU that loads this library holds until the
-// process exits.
+// Who needs this: callers that hold no right to allocate device memory at the moment
+// they score a proposal.  A Julia host whose CUDA.jl memory pool owns the device
+// memory is one: a foreign cudaMalloc may find the pool has taken nearly all of HBM,
+// and cudaMalloc/cudaFree synchronise the device in the middle of the annealing loop.
+// A host runtime with a fixed device-memory budget granted up front, or a real-time
+// loop that must not stall on those implicit synchronisations, is another.  Such a
+// caller passes its own device buffers for inputs and output; the per-slab scratch
+// lives in the file-scope array below, which every GPU that loads this library holds
+// until the process exits.
 //
 // The computation is the per-slab Bayes term and the deterministic compensated sum
 // of the tensor-core path (the slab-energy epilogue and k_finalize_slabs), fed from a
 // stored c3 instead of the accumulator in TMEM:
 //   E = sum_ki tf(k1,k2,k3) * (Qs * log(sum_g p) - sum_g q^ log p),  p = max(c3, 1e-30),
 //   Qs = sum_g q^  (q^ = the L1-normalised histogram slab).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -35,8 +35,46 @@ constexpr int kMaxDevices = 64;
 // Shared by every call on a device; each call overwrites every entry it later reads.
 static __device__ __align__(256) double g_slab_energy[kNoAllocMaxSlabs];
 
+// Device address of g_slab_energy per device ordinal, with the unique id of the
+// context it was resolved in: a device reset (or a switch to another context on the
+// same device) loads the module anew, possibly at another address, so the address is
+// looked up again whenever the current context's id differs.
+struct ScratchSlot {
+  unsigned long long ctx_id;
+  double* ptr;
+};
 std::mutex g_mu;
-double* g_scratch[kMaxDevices] = {};
+ScratchSlot g_scratch[kMaxDevices] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+bool g_ctx_fns_tried = false;
+
+// Unique id of the calling thread's current context (0 when there is none or the
+// driver does not provide the query).  Called with g_mu held.
+unsigned long long current_ctx_id() {
+  if (!g_ctx_fns_tried) {
+    g_ctx_fns_tried = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_current = (CtxGetCurrentFn)f1;
+      g_ctx_id = (CtxGetIdFn)f2;
+    }
+  }
+  if (!g_ctx_current || !g_ctx_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (g_ctx_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
   s = a + b;
@@ -130,23 +168,37 @@ extern "C" int tp3_bayes_energy_noalloc(const float* d_c3, const float* d_qhat, 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(TP3_ERR_NO_DEVICE, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(TP3_ERR_NO_DEVICE, "device ordinal out of range");
+  // an error left by the caller's earlier work would otherwise surface after this
+  // call's launches and be reported as theirs: report it as what it is, uncleared
+  e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return noalloc_fail(TP3_ERR_CUDA, std::string("an earlier CUDA error is pending (left uncleared): ") +
+                                          cudaGetErrorString(e));
   double* scratch = nullptr;
   {
-    // first call on a device: resolve the device address of the static array
+    // set-up on the first call in each context: resolve the device address of the
+    // static array (cudaGetSymbolAddress loads the module into the current context)
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev]) {
-      e = cudaGetSymbolAddress((void**)&g_scratch[dev], g_slab_energy);
+    ScratchSlot& slot = g_scratch[dev];
+    const unsigned long long id = current_ctx_id();
+    if (!slot.ptr || id == 0 || slot.ctx_id != id) {
+      double* p = nullptr;
+      e = cudaGetSymbolAddress((void**)&p, g_slab_energy);
       if (e != cudaSuccess) {
-        g_scratch[dev] = nullptr;
+        slot.ptr = nullptr;
         return noalloc_fail(TP3_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       }
+      slot.ptr = p;
+      slot.ctx_id = id != 0 ? id : current_ctx_id();  // the context exists now
     }
-    scratch = g_scratch[dev];
+    scratch = slot.ptr;
   }
   cudaStream_t s = (cudaStream_t)stream;
   k_bayes_slab_noalloc<<<(unsigned)klength, 256, 0, s>>>(d_c3, d_qhat, (int)klength, (int)G, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(TP3_ERR_CUDA, std::string("slab launch: ") + cudaGetErrorString(e));
   k_sum_slabs_noalloc<<<1, 256, 0, s>>>(scratch, (int)klength, d_E);
   e = cudaGetLastError();
-  if (e != cudaSuccess) return noalloc_fail(TP3_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return noalloc_fail(TP3_ERR_CUDA, std::string("sum launch: ") + cudaGetErrorString(e));
   return TP3_OK;
 }
