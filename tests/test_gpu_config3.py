@@ -63,7 +63,7 @@ def _perturb(coeff, rng, real):
     c[l,-m] = (-1)^m conj(c[l,m]) of a real intensity (the fast real-function path),
     real=False leaves a general complex set (the general path)."""
     from tp3.structure import seanindex0
-    x = coeff * (1.0 + 0.05 * rng.normal(size=coeff.shape)) + 0.05j * np.abs(coeff) * rng.normal(size=coeff.shape)
+    x = coeff * (1.0 + 0.2 * rng.normal(size=coeff.shape)) + 0.2j * np.abs(coeff) * rng.normal(size=coeff.shape)
     if real:
         for l in range(0, LMAX):
             i0 = seanindex0(l, 0, LMAX)
@@ -73,11 +73,13 @@ def _perturb(coeff, rng, real):
     return x
 
 
+@pytest.mark.parametrize("form", [3, 5])
 @pytest.mark.parametrize("mode", [tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3])
-def test_ragged_config3_energies_match_fp64_oracle(world, mode):
+def test_ragged_config3_energies_match_fp64_oracle(world, mode, form):
     import torch
     big, mols, hists, oracles = world
     big.set_mode(mode)
+    big.set_coupling(form)
     rng = np.random.default_rng(5 + mode)
     props, lkh, ref = [], [], []
     for h, ((L, K), coeff) in enumerate(zip(SHAPES, mols)):
@@ -98,7 +100,8 @@ def test_ragged_config3_energies_match_fp64_oracle(world, mode):
     E = d_E.cpu().numpy()
     rel = np.abs(E - np.array(ref)) / np.abs(np.array(ref))
     assert rel.max() <= 1e-6, list(zip(lkh, rel))
-    # the perturbed proposals differ from the molecules by far more than the tolerance
+    # the perturbed proposals move the energy by far more than the tolerance (the Bayes
+    # energy is stationary at the histogram's own structure, so it moves at second order)
     for h in range(len(SHAPES)):
         assert abs(ref[3 * h + 1] - ref[3 * h]) > 1e-5 * abs(ref[3 * h])
         assert abs(ref[3 * h + 2] - ref[3 * h]) > 1e-5 * abs(ref[3 * h])

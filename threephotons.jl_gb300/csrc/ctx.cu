@@ -360,6 +360,44 @@ std::string setup_tc(tp3_ctx* c) {
       (e = upload(c, Fhi32, &tc.Fhi32)) != cudaSuccess || (e = upload(c, Flo32, &tc.Flo32)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
+  // folded-row coupling: two tilings (8 warps in up to 225 KB, one CTA per SM; 4 warps in
+  // up to 110 KB, two CTAs per SM), each with the largest per-warp D buffer that fits
+  if ((e = tp3::fold_configure()) != cudaSuccess) return std::string("fold coupling: ") + cudaGetErrorString(e);
+  {
+    int rows_gen = 0;  // D rows of the largest block, general path (all l3 in one chunk)
+    for (const auto& pb : pbs) {
+      int r = 0;
+      for (int s3 = 0; s3 < pb.nl3; ++s3) r += 2 * (pb.l3min + 2 * s3) + 1;
+      rows_gen = std::max(rows_gen, r);
+    }
+    const int ps = (b.K + 5 + 31) / 32 * 32;
+    const struct { int nw; size_t budget; } fvs[2] = {{8, (size_t)tp3::kCoupleMaxDynSmem},
+                                                      {4, (size_t)tp3::kCoupleSmallSmem}};
+    for (int v = 0; v < 2; ++v) {
+      tp3::FoldVariant& fv = tc.fold[v];
+      std::vector<tp3::FoldBlock> fbl;
+      std::vector<tp3::FoldRow> frows;
+      std::vector<float> fw;
+      std::vector<int2> fch;
+      int wmx = 0, cmx = 0;
+      if (!tp3::build_fold_tables(pbs, rows_gen, fbl, frows, fw, fch, wmx, cmx).empty()) continue;
+      const size_t fixed = tp3::fold_smem_bytes(0, ps, 0, wmx, cmx);
+      const size_t per_row = (size_t)(1 + fvs[v].nw) * ps * sizeof(float2);
+      if (fixed + per_row > fvs[v].budget) continue;
+      const int drows = (int)std::min<size_t>((size_t)rows_gen, (fvs[v].budget - fixed) / per_row);
+      if (!tp3::build_fold_tables(pbs, drows, fbl, frows, fw, fch, wmx, cmx).empty()) continue;
+      if ((e = upload(c, fbl, &fv.blks)) != cudaSuccess || (e = upload(c, frows, &fv.rows)) != cudaSuccess ||
+          (e = upload(c, fw, &fv.w)) != cudaSuccess || (e = upload(c, fch, &fv.chunks)) != cudaSuccess)
+        return std::string("fold coupling tables: ") + cudaGetErrorString(e);
+      fv.nw = fvs[v].nw;
+      fv.drows = drows;
+      fv.ps = ps;
+      fv.wmax = wmx;
+      fv.cmax = cmx;
+      fv.smem = tp3::fold_smem_bytes(fv.nw, ps, drows, wmx, cmx);
+      fv.ok = fv.smem <= fvs[v].budget;
+    }
+  }
   // the split coupling is kept for the autotuner and for shapes the fused kernel cannot hold
   tc.split_ok = tp3::couple_split_smem_d(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
              tp3::couple_split_smem_t(t, tc) <= (size_t)tp3::kCoupleMaxDynSmem &&
@@ -502,7 +540,7 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
   cudaError_t e;
   if (rag) {
     if (c->nhist == 0) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
-    if (!is_tc(c->mode) || !c->tc.fused_ok)
+    if (!is_tc(c->mode) || (!c->tc.fused_ok && c->tc.use_fold < 0))
       return fail(c, TP3_ERR_UNSUPPORTED, "ragged batches need a tensor-core mode with the one-kernel coupling");
   } else if (!c->has_hist) {
     return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
@@ -556,11 +594,12 @@ int check_ctx(tp3_ctx* c) {
 // form this shape cannot run falls back to one that it can.
 void apply_coupling(tp3_ctx* c, int form) {
   TcTables& tc = c->tc;
+  tc.use_fold = (form == 5 && tc.fold[0].ok) ? 0 : (form == 6 && tc.fold[1].ok) ? 1 : -1;
   tc.use_small = form == 2 && tc.small_ok;
   tc.use_warp = form == 3 && tc.warp_ok;
   tc.use_warp2 = form == 4 && tc.warp2_ok;
-  tc.split = (form == 1 && tc.split_ok) || (!tc.fused_ok && !tc.use_warp && !tc.use_warp2);
-  if (tc.split) tc.use_small = tc.use_warp = tc.use_warp2 = false;
+  tc.split = (form == 1 && tc.split_ok) || (!tc.fused_ok && !tc.use_warp && !tc.use_warp2 && tc.use_fold < 0);
+  if (tc.split) tc.use_small = tc.use_warp = tc.use_warp2 = false, tc.use_fold = -1;
 }
 
 // Folded, slab-normalised histogram of Kh shells (slabs with k1 < Kh; the rest zero)
@@ -879,6 +918,8 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
       if (c->tc.warp_ok) vars.push_back({m, 3});
       if (c->tc.warp2_ok) vars.push_back({m, 4});
       if (c->tc.split_ok) vars.push_back({m, 1});
+      if (c->tc.fold[0].ok) vars.push_back({m, 5});
+      if (c->tc.fold[1].ok) vars.push_back({m, 6});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
   const size_t nco = (size_t)b.K * b.LMAX * b.LMAX;
@@ -917,6 +958,8 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   const bool split0 = c->tc_ok ? c->tc.split : false;
   const bool small0 = c->tc_ok ? c->tc.use_small : false;
   const bool warp0 = c->tc_ok ? c->tc.use_warp : false;
+  const bool warp20 = c->tc_ok ? c->tc.use_warp2 : false;
+  const int fold0 = c->tc_ok ? c->tc.use_fold : -1;
   const bool prof0 = c->prof;
   c->prof = false;
   int best = -1, rc = TP3_OK;
@@ -947,7 +990,10 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   c->prof = prof0;
   if (rc != TP3_OK || best < 0) {
     c->mode = mode0;
-    if (c->tc_ok) { c->tc.split = split0; c->tc.use_small = small0; c->tc.use_warp = warp0; }
+    if (c->tc_ok) {
+      c->tc.split = split0; c->tc.use_small = small0; c->tc.use_warp = warp0;
+      c->tc.use_warp2 = warp20; c->tc.use_fold = fold0;
+    }
     return rc != TP3_OK ? rc : fail(c, TP3_ERR_UNSUPPORTED, "no variant ran");
   }
   c->mode = vars[best].first;
@@ -978,8 +1024,9 @@ int tp3_set_coupling(tp3_ctx* c, int form) {
   if (int r = check_ctx(c)) return r;
   if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
   const bool ok = (form == 0 && c->tc.fused_ok) || (form == 1 && c->tc.split_ok) || (form == 2 && c->tc.small_ok) ||
-                  (form == 3 && c->tc.warp_ok) || (form == 4 && c->tc.warp2_ok);
-  if (!ok) return fail(c, form < 0 || form > 4 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
+                  (form == 3 && c->tc.warp_ok) || (form == 4 && c->tc.warp2_ok) || (form == 5 && c->tc.fold[0].ok) ||
+                  (form == 6 && c->tc.fold[1].ok);
+  if (!ok) return fail(c, form < 0 || form > 6 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
   apply_coupling(c, form);
   return TP3_OK;
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 namespace tp3 {
 
@@ -63,8 +64,48 @@ struct PairBlock {
   int wcount;              // floats in the block's 3j table (multiple of 4)
 };
 
+// Folded-row coupling (kernels_fold.cu): per pair block, the 3j rows of every m3
+// with only the orders l3 >= |m3| stored, and the l3 chunks whose D rows fit one
+// warp's buffer.
+constexpr int kFoldMaxChunks = 8;
+constexpr int kFoldMaxRows = 32;  // m3 pairs of one block, <= M + 1 (M <= 30)
+struct FoldBlock {
+  int l1, l2, l3min, nl3, M, lt_base;
+  int row0;                  // first FoldRow of the block
+  int w0;                    // float offset of the block's 3j rows (16-byte aligned)
+  int wsym, wall;            // floats of the m3 >= 0 prefix and of all rows (multiples of 4)
+  int npair_sym, npair_all;  // m3 pairs of the prefix and in all
+  int ch_sym0, nch_sym;      // l3 chunks, real-function path (D rows of l3 + 1)
+  int ch_gen0, nch_gen;      // l3 chunks, general path (D rows of 2 l3 + 1)
+};
+// Rows come in pairs of m3 (m3a and m3b = m3a + 1 for m3a >= 0, m3a - 1 below), so a
+// lane forms two products per m1 from one c_k1 load; the pair's 3j values are stored
+// interleaved per column, (w_a, w_b), over the union of the two m1 ranges (zero where
+// a row's own range or order range does not reach; a partner beyond M is all zero).
+struct FoldRow {
+  int m3a;       // first m3 of the pair
+  int m1lo, n1;  // m1 = m1lo .. m1lo + n1 - 1 (union of the pair's ranges)
+  int s0a, s0b;  // first order index with l3 >= |m3| for each m3 (nl3 for an absent partner)
+  int c0, rs;    // first stored column (even) and columns per m1 (even)
+  int wofs;      // float offset of the pair's rows in the block's table (multiple of 4)
+};
+// One tiling of the folded-row coupling: nw warps per CTA, drows D rows per warp, ps
+// shell-pair slots per D row (>= K + 5, multiple of 32).
+struct FoldVariant {
+  bool ok = false;
+  int nw = 0, drows = 0, ps = 0, wmax = 0, cmax = 0;
+  size_t smem = 0;
+  const FoldBlock* blks = nullptr;
+  const FoldRow* rows = nullptr;
+  const float* w = nullptr;
+  const int2* chunks = nullptr;
+};
+
 // Device tables of the tensor-core path.
 struct TcTables {
+  // folded-row coupling: [0] 8 warps, one CTA per SM; [1] 4 warps, two CTAs per SM
+  FoldVariant fold[2];
+  int use_fold = -1;
   int n_pb = 0, maxs = 0, SDmax = 0;
   int ncp = 0, SDp = 0, pmax = 0, nchunks = 0, wsmem = 0;  // coupling kernel shared-memory layout
   bool w_smem = false;
@@ -149,6 +190,14 @@ cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, doubl
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
 size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
 cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);
+std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std::vector<FoldBlock>& blks,
+                              std::vector<FoldRow>& rows, std::vector<float>& w, std::vector<int2>& chunks,
+                              int& wmax, int& cmax);
+size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax);
+cudaError_t fold_configure();
+cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const FoldVariant& fv, int n, const float2* cc,
+                               const int* sym, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s,
+                               const RagInfo* rag = nullptr);
 cudaError_t launch_couple_split(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                 float2* Dg, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s);
 

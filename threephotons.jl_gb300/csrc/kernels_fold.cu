@@ -1,0 +1,475 @@
+// Stage (a) coupling, folded-row form: the reference's triple products
+//   T[(k1,k2,k3)][(l1,l2,l3)] = sum_j w_j Re(c_k1[l1,m1] c_k2[l2,m2] c_k3[l3,m3])
+// (src/correlations.jl:157-176; src/cuda_kernel.cu:31-37), pair-factorised as
+//   D[k1,k2][l3][m3] = sum_m1 w(l1 m1 l2 m2 l3 m3) c_k1[l1,m1] c_k2[l2,m2],  m2 = -m3 - m1
+//   T[(k1,k2,k3)][lt] = Re sum_m3 D[k1,k2][l3][m3] c_k3[l3,m3]
+// and laid out so that every warp instruction does full-width work.
+//
+// One CTA = one (l1, l2) pair block of one proposal.  Its warps take work units from a
+// shared counter; a unit is a folded pair of k1 rows, k1 = j and k1 = K-1-j, whose
+// (j + 1) + (K - j) = K + 1 shell pairs fill the warp's lanes (27 of 32 at K = 26).
+//   Phase 1: the warp walks pairs of m3 and, inside them, m1; every lane owns one shell
+//     pair and accumulates its D for both m3 and all the block's l3 at once (one complex
+//     product per m1 and m3, reused by every l3).  All lanes read the same 3j values (a
+//     16-byte broadcast holds two orders of both m3), the same two k1 rows of c_k1 and
+//     consecutive c_k2 entries (no bank conflicts); 3j columns of orders l3 < |m3| (zero)
+//     are not stored, so they are never multiplied.
+//   Phase 2: lanes own 4 x 4 tiles (4 shells k2 x 4 shells k3 <= k2) of one l3 and
+//     contract D with the staged c_k3 over m3; both operands come as 16-byte loads.
+// Both phases synchronise only the warp.  D lives in a per-warp shared-memory buffer of
+// `drows` rows (one row per (l3, m3), one slot per shell pair); a block whose D would not
+// fit is processed in chunks of l3 (each chunk recomputes the shell products).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tp3.h"
+#include "internal.h"
+#include "tables.h"
+
+namespace tp3 {
+namespace {
+
+__device__ __forceinline__ void fold_store_split(void* hi, void* lo, size_t i, float v, bool tf32) {
+  if (tf32) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float hf = __uint_as_float(h);
+    reinterpret_cast<float*>(hi)[i] = hf;
+    reinterpret_cast<float*>(lo)[i] = v - hf;
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    reinterpret_cast<__nv_bfloat16*>(hi)[i] = h;
+    reinterpret_cast<__nv_bfloat16*>(lo)[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
+// D row of order s inside a chunk starting at s_lo: rows of the orders before s,
+// (l3 + 1) per order for real functions (m3 = 0..l3), (2 l3 + 1) otherwise.
+__device__ __forceinline__ int fold_drow(int s, int s_lo, int l3min, bool sym) {
+  const int d = s - s_lo;
+  return sym ? d * (l3min + 1) + d * (s + s_lo - 1) : d * (2 * l3min + 1) + 2 * d * (s + s_lo - 1);
+}
+
+// Phase-1 inner loop for one m3 pair: n1 values of m1, NE 3j columns (even count).
+// c1 / c2 point at this lane's shells in rows m1lo and m2(m1lo) of the first m3; the
+// second m3's c_k2 row is dps away; rows are ps apart.  w holds (w_a, w_b) per column.
+template <int NE>
+__device__ __forceinline__ void fold_p1(const float2* __restrict__ c1, const float2* __restrict__ c2, int dps, int ps,
+                                        int n1, const float* __restrict__ w, int rs2, float* ar0, float* ai0,
+                                        float* ar1, float* ai1) {
+#pragma unroll
+  for (int j = 0; j < NE; ++j) { ar0[j] = 0.f; ai0[j] = 0.f; ar1[j] = 0.f; ai1[j] = 0.f; }
+#pragma unroll 2
+  for (int i = 0; i < n1; ++i) {
+    const float2 a = c1[i * ps];
+    const float2 b0 = c2[-i * ps];
+    const float2 b1 = c2[-i * ps + dps];
+    const float x0r = fmaf(a.x, b0.x, -a.y * b0.y), x0i = fmaf(a.x, b0.y, a.y * b0.x);
+    const float x1r = fmaf(a.x, b1.x, -a.y * b1.y), x1i = fmaf(a.x, b1.y, a.y * b1.x);
+    const float4* wr = reinterpret_cast<const float4*>(w + i * rs2);
+#pragma unroll
+    for (int j2 = 0; j2 < NE / 2; ++j2) {
+      const float4 wv = wr[j2];  // (w_a, w_b) of columns 2 j2 and 2 j2 + 1
+      ar0[2 * j2] = fmaf(wv.x, x0r, ar0[2 * j2]);
+      ai0[2 * j2] = fmaf(wv.x, x0i, ai0[2 * j2]);
+      ar1[2 * j2] = fmaf(wv.y, x1r, ar1[2 * j2]);
+      ai1[2 * j2] = fmaf(wv.y, x1i, ai1[2 * j2]);
+      ar0[2 * j2 + 1] = fmaf(wv.z, x0r, ar0[2 * j2 + 1]);
+      ai0[2 * j2 + 1] = fmaf(wv.z, x0i, ai0[2 * j2 + 1]);
+      ar1[2 * j2 + 1] = fmaf(wv.w, x1r, ar1[2 * j2 + 1]);
+      ai1[2 * j2 + 1] = fmaf(wv.w, x1i, ai1[2 * j2 + 1]);
+    }
+  }
+}
+
+template <int NE>
+__device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2, int dps, int ps, int n1,
+                                              const float* w, int rs2, bool valid, int a, int s0a, int s0b,
+                                              int s_hi, int s_lo, int l3min, int m3a, int m3b, bool sym, float2* Dw,
+                                              int slot) {
+  float ar0[NE], ai0[NE], ar1[NE], ai1[NE];
+  fold_p1<NE>(c1, c2, dps, ps, n1, w, rs2, ar0, ai0, ar1, ai1);
+  if (!valid) return;
+#pragma unroll
+  for (int j = 0; j < NE; ++j) {
+    const int s = a + j;
+    if (s >= s_lo && s < s_hi) {
+      const int l3 = l3min + 2 * s;
+      const int r = fold_drow(s, s_lo, l3min, sym);
+      if (s >= s0a) Dw[(r + (sym ? m3a : m3a + l3)) * ps + slot] = make_float2(ar0[j], ai0[j]);
+      if (s >= s0b) Dw[(r + (sym ? m3b : m3b + l3)) * ps + slot] = make_float2(ar1[j], ai1[j]);
+    }
+  }
+}
+
+// grid: (n_pb, n); block NW * 32; dynamic shared memory FoldVariant::smem.
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
+    const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff, const FoldBlock* __restrict__ blks,
+    const FoldRow* __restrict__ rows, const float* __restrict__ wtab, const int2* __restrict__ chunks, int ps,
+    int drows, int wmax, int cmax, int klp, int KP, const int* __restrict__ symflags, void* __restrict__ Thi,
+    void* __restrict__ Tlo, bool tf32out, float* __restrict__ T32, int ldT32, const RagInfo* __restrict__ rag) {
+  extern __shared__ __align__(16) float smf[];
+  __shared__ int s_next[kFoldMaxChunks];
+  __shared__ FoldRow s_rows[kFoldMaxRows];
+  // per-CTA constants, read once from global memory
+  __shared__ FoldBlock s_fb;
+  __shared__ int s_misc[4];  // sym, Kp, skip (absent orders of a ragged proposal), klen
+  __shared__ int s_coff[kFoldMaxRows];
+  __shared__ int2 s_chunks[kFoldMaxChunks];
+  const int prop = blockIdx.y;
+  if (threadIdx.x == 0) {
+    const FoldBlock b = blks[blockIdx.x];
+    s_fb = b;
+    int Kq = K, skip = 0, klen = 0;
+    if (rag) {
+      const RagInfo ri = rag[prop];
+      Kq = ri.K;
+      klen = ri.klen;
+      skip = (b.l1 > ri.L || b.l2 > ri.L) ? 1 : 0;
+    }
+    const int sy = symflags[prop] != 0;
+    s_misc[0] = sy;
+    s_misc[1] = Kq;
+    s_misc[2] = skip;
+    s_misc[3] = klen;
+    const int nch = sy ? b.nch_sym : b.nch_gen, ch0 = sy ? b.ch_sym0 : b.ch_gen0;
+    for (int c = 0; c < nch; ++c) s_chunks[c] = chunks[ch0 + c];
+  }
+  __syncthreads();
+  const FoldBlock fb = s_fb;
+  const int Kp = s_misc[1];
+  if (s_misc[2]) {
+    // absent orders: the block's l-triples are zero for this proposal's scored rows
+    const int klen = s_misc[3];
+    for (int i = threadIdx.x; i < klen * fb.nl3; i += blockDim.x) {
+      const int ki = i / fb.nl3, sj = i - ki * fb.nl3;
+      fold_store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + fb.lt_base + sj, 0.f, tf32out);
+      if (T32) T32[((size_t)prop * klp + ki) * ldT32 + fb.lt_base + sj] = 0.f;
+    }
+    return;
+  }
+  const bool sym = s_misc[0] != 0;
+  const int l1 = fb.l1, l2 = fb.l2, l3min = fb.l3min, M = fb.M;
+  // shared memory: C1 [2 l1 + 1][ps], C2 [2 l2 + 3][ps] (rows m2 = -l2 - 1 .. l2 + 1;
+  // shell index fastest), the block's 3j rows, cT [drows][ps] (the chunk's c_k3 rows,
+  // shell index fastest), D [NW][drows][ps]
+  float2* C1 = reinterpret_cast<float2*>(smf);
+  float2* C2 = C1 + (size_t)cmax * ps;
+  float* W = reinterpret_cast<float*>(C2 + (size_t)(cmax + 2) * ps);
+  float2* cT = reinterpret_cast<float2*>(W + wmax);
+  float2* Dall = cT + (size_t)drows * ps;
+  const float2* src = cc + (size_t)prop * K * nc;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  {
+    const int nl = (max(max(l1, l2), M) >> 1) + 1;  // even orders used by this block
+    if (threadIdx.x < nl) s_coff[threadIdx.x] = coff[threadIdx.x];
+  }
+  __syncthreads();
+  const int o1 = s_coff[l1 >> 1], o2 = s_coff[l2 >> 1];
+  // staging: one warp per coefficient row, one lane per shell (the loads of a thread are
+  // independent, so they overlap)
+  {
+    const int n1r = 2 * l1 + 1, n2r = 2 * l2 + 1;
+    for (int k0 = 0; k0 < ps; k0 += 32) {
+      const int k = k0 + lane;
+      const bool live = k < Kp;
+      const float2* sk = src + (size_t)(live ? k : 0) * nc;
+#pragma unroll 4
+      for (int m = warp; m < n1r; m += NW) C1[m * ps + k] = live ? sk[o1 + m] : make_float2(0.f, 0.f);
+      // C2 has a zero row at each end: the union m1 range of an m3 pair reaches one row
+      // past either end, where the pair's 3j value is zero
+#pragma unroll 4
+      for (int m = warp; m < n2r + 2; m += NW)
+        C2[m * ps + k] = (live && m >= 1 && m <= n2r) ? sk[o2 + m - 1] : make_float2(0.f, 0.f);
+    }
+    const int wn = (sym ? fb.wsym : fb.wall) / 4;
+    const float4* w4 = reinterpret_cast<const float4*>(wtab + fb.w0);
+    float4* s4 = reinterpret_cast<float4*>(W);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < wn; i += NW * 32) s4[i] = w4[i];
+    const int nr = sym ? fb.npair_sym : fb.npair_all;
+    for (int i = threadIdx.x; i < nr; i += NW * 32) s_rows[i] = rows[fb.row0 + i];
+  }
+  const int nch = sym ? fb.nch_sym : fb.nch_gen;
+  if (threadIdx.x < kFoldMaxChunks) s_next[threadIdx.x] = 0;
+
+  float2* Dw = Dall + (size_t)warp * drows * ps;
+  const size_t tbase = (size_t)prop * klp * KP;
+  void* ThiP = tf32out ? (void*)((float*)Thi + tbase) : (void*)((__nv_bfloat16*)Thi + tbase);
+  void* TloP = tf32out ? (void*)((float*)Tlo + tbase) : (void*)((__nv_bfloat16*)Tlo + tbase);
+  float* T32P = T32 ? T32 + (size_t)prop * klp * ldT32 : nullptr;
+  const int nunits = (Kp + 1) >> 1;
+  const int npairs = sym ? fb.npair_sym : fb.npair_all;
+
+  for (int ch = 0; ch < nch; ++ch) {
+    const int2 chk = s_chunks[ch];
+    const int s_lo = chk.x, s_hi = chk.y;
+    const int l3top = l3min + 2 * (s_hi - 1);
+    __syncthreads();  // the previous chunk's cT reads are done; C1 / C2 / W are staged
+    // cT rows of this chunk: c_k3[l3][m3] (m3 = 0 halved for real functions, whose T is
+    // twice the sum over m3 >= 0)
+    {
+      int r0 = 0;
+      for (int s = s_lo; s < s_hi; ++s) {
+        const int l3 = l3min + 2 * s;
+        const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
+        const int o3 = s_coff[l3 >> 1] + (sym ? l3 : 0);  // compact index of row r = 0
+        for (int k0 = 0; k0 < ps; k0 += 32) {
+          const int k = k0 + lane;
+          const bool live = k < Kp;
+          const float2* sk = src + (size_t)(live ? k : 0) * nc + o3;
+#pragma unroll 4
+          for (int r = warp; r < cnt; r += NW) {
+            float2 v = live ? sk[r] : make_float2(0.f, 0.f);
+            if (sym && r == 0) { v.x *= 0.5f; v.y *= 0.5f; }
+            cT[(r0 + r) * ps + k] = v;
+          }
+        }
+        r0 += cnt;
+      }
+    }
+    __syncthreads();
+    for (;;) {
+      int u = 0;
+      if (lane == 0) u = atomicAdd(&s_next[ch], 1);
+      u = __shfl_sync(0xffffffffu, u, 0);
+      if (u >= nunits) break;
+      const int k1a = u, k1b = Kp - 1 - u;
+      const bool two = k1b != k1a;
+      const int off2 = (u + 2) & ~1;  // slot of (k1b, 0): even, so shell quads are 16-byte aligned
+      const int nslots = two ? off2 + k1b + 1 : u + 1;
+      // ---------------- phase 1: D of the unit's shell pairs ----------------
+      for (int slot0 = 0; slot0 < nslots; slot0 += 32) {
+        const int slot = slot0 + lane;
+        int k1 = k1a, k2 = 0;
+        bool valid = false;
+        if (slot <= u) { k2 = slot; valid = true; }
+        else if (two && slot >= off2 && slot - off2 <= k1b) { k1 = k1b; k2 = slot - off2; valid = true; }
+        const int mtop = min(M, l3top);
+        for (int pi = 0; pi < npairs; ++pi) {
+          const FoldRow fr = s_rows[pi];
+          if ((fr.m3a < 0 ? -fr.m3a : fr.m3a) > mtop) continue;
+          const int m3a = fr.m3a, m3b = m3a >= 0 ? m3a + 1 : m3a - 1;
+          const int a = max(fr.c0, s_lo & ~1);  // even: 16-byte aligned 3j column pairs
+          const int b = min(fr.c0 + fr.rs, (s_hi + 1) & ~1);
+          const int ne = b - a;
+          if (ne <= 0) continue;
+          const float2* c1 = C1 + (fr.m1lo + l1) * ps + k1;
+          const float2* c2 = C2 + (-m3a - fr.m1lo + l2 + 1) * ps + k2;
+          const int dps = m3a >= 0 ? -ps : ps;
+          const float* w = W + fr.wofs + 2 * (a - fr.c0);
+#define TP3_FOLD_P1(NE)                                                                                  \
+  case NE:                                                                                               \
+    fold_p1_store<NE>(c1, c2, dps, ps, fr.n1, w, 2 * fr.rs, valid, a, fr.s0a, fr.s0b, s_hi, s_lo, l3min, \
+                      m3a, m3b, sym, Dw, slot);                                                          \
+    break;
+          switch (ne) {
+            TP3_FOLD_P1(2) TP3_FOLD_P1(4) TP3_FOLD_P1(6) TP3_FOLD_P1(8)
+            TP3_FOLD_P1(10) TP3_FOLD_P1(12) TP3_FOLD_P1(14) TP3_FOLD_P1(16)
+            default: break;
+          }
+#undef TP3_FOLD_P1
+        }
+      }
+      __syncwarp();
+      // ---------------- phase 2: T of the unit's shell triples ----------------
+      const int qa = (k1a >> 2) + 1, ta = qa * (qa + 1) / 2;
+      const int qb = (k1b >> 2) + 1, tb = two ? qb * (qb + 1) / 2 : 0;
+      const int nt = ta + tb;
+      const int nitems = (s_hi - s_lo) * nt;
+      const float scale = sym ? 2.f : 1.f;
+      for (int base = 0; base < nitems; base += 32) {
+        const int it = base + lane;
+        if (it >= nitems) break;
+        const int sidx = it / nt;
+        const int tile = it - sidx * nt;
+        const int s = s_hi - 1 - sidx;  // largest l3 first
+        int t = tile, k1 = k1a, pbase = 0;
+        if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; }
+        int q2 = 0;
+        while ((q2 + 1) * (q2 + 2) / 2 <= t) ++q2;
+        const int q3 = t - q2 * (q2 + 1) / 2;
+        const int l3 = l3min + 2 * s;
+        const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
+        const int r0 = fold_drow(s, s_lo, l3min, sym);
+        const float4* dp = reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2);
+        const float4* cp = reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3);
+        const int rstride = ps / 2;  // float4 per row
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 2
+        for (int r = 0; r < cnt; ++r) {
+          const float4 d01 = dp[r * rstride], d23 = dp[r * rstride + 1];
+          const float4 c01 = cp[r * rstride], c23 = cp[r * rstride + 1];
+          const float xr[4] = {d01.x, d01.z, d23.x, d23.z}, xi[4] = {d01.y, d01.w, d23.y, d23.w};
+          const float yr[4] = {c01.x, c01.z, c23.x, c23.z}, yi[4] = {c01.y, c01.w, c23.y, c23.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xr[i], yr[j], fmaf(-xi[i], yi[j], acc[i][j]));
+        }
+        const int lt = fb.lt_base + s;
+        const int t3 = k1 * (k1 + 1) * (k1 + 2) / 6;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int k2 = 4 * q2 + i;
+          if (k2 > k1) continue;
+          const int row0 = t3 + k2 * (k2 + 1) / 2 + 4 * q3;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (4 * q3 + j <= k2) {
+              const float v = scale * acc[i][j];
+              fold_store_split(ThiP, TloP, (size_t)(row0 + j) * KP + lt, v, tf32out);
+              if (T32P) T32P[(size_t)(row0 + j) * ldT32 + lt] = v;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+}  // namespace
+
+// ---- host side ----------------------------------------------------------------
+
+std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std::vector<FoldBlock>& blks,
+                              std::vector<FoldRow>& rows, std::vector<float>& w, std::vector<int2>& chunks,
+                              int& wmax, int& cmax) {
+  blks.clear();
+  rows.clear();
+  w.clear();
+  chunks.clear();
+  wmax = 0;
+  cmax = 0;
+  for (const PairBlock& pb : pbs) {
+    FoldBlock fb{};
+    fb.l1 = pb.l1; fb.l2 = pb.l2; fb.l3min = pb.l3min; fb.nl3 = pb.nl3; fb.M = pb.M; fb.lt_base = pb.lt_base;
+    if (pb.M + 1 > kFoldMaxRows) return "fold tables: more m3 pairs than the kernel stages";
+    fb.row0 = (int)rows.size();
+    fb.w0 = (int)w.size();
+    const int nl3e = (pb.nl3 + 1) & ~1;
+    auto s0_of = [&](int m3) {
+      const int am = m3 < 0 ? -m3 : m3;
+      return am > pb.M ? pb.nl3 : std::max(0, (am - pb.l3min + 1) / 2);
+    };
+    auto m1lo_of = [&](int m3) { return std::max(-pb.l1, -pb.l2 - m3); };
+    auto m1hi_of = [&](int m3) { return std::min(pb.l1, pb.l2 - m3); };
+    int run = 0;
+    // pairs (0,1), (2,3), ... (the real-function prefix), then (-1,-2), (-3,-4), ...
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int m3a = pass == 0 ? 0 : -1; pass == 0 ? m3a <= pb.M : m3a >= -pb.M; m3a += pass == 0 ? 2 : -2) {
+        const int m3b = pass == 0 ? m3a + 1 : m3a - 1;
+        const bool hasb = (m3b < 0 ? -m3b : m3b) <= pb.M;
+        FoldRow fr{};
+        fr.m3a = m3a;
+        int lo = m1lo_of(m3a), hi = m1hi_of(m3a);
+        if (hi < lo) return "fold tables: empty m1 range";
+        if (hasb && m1hi_of(m3b) >= m1lo_of(m3b)) {
+          lo = std::min(lo, m1lo_of(m3b));
+          hi = std::max(hi, m1hi_of(m3b));
+        }
+        fr.m1lo = lo;
+        fr.n1 = hi - lo + 1;
+        fr.s0a = s0_of(m3a);
+        fr.s0b = hasb ? s0_of(m3b) : pb.nl3;
+        if (fr.s0a >= pb.nl3) return "fold tables: no order l3 >= |m3|";
+        fr.c0 = fr.s0a & ~1;
+        fr.rs = nl3e - fr.c0;
+        fr.wofs = run;
+        for (int i = 0; i < fr.n1; ++i) {
+          const int m1 = fr.m1lo + i;
+          for (int c = 0; c < fr.rs; ++c) {
+            const int s = fr.c0 + c;
+            const int l3 = pb.l3min + 2 * s;
+            for (int q = 0; q < 2; ++q) {
+              const int m3 = q == 0 ? m3a : m3b;
+              const int s0 = q == 0 ? fr.s0a : fr.s0b;
+              const bool in = (q == 0 || hasb) && s >= s0 && s < pb.nl3 && m1 >= m1lo_of(m3) && m1 <= m1hi_of(m3);
+              w.push_back(in ? (float)tp3::wigner3j(pb.l1, pb.l2, l3, m1, -m3 - m1, m3) : 0.f);
+            }
+          }
+          run += 2 * fr.rs;
+        }
+        rows.push_back(fr);
+      }
+      if (pass == 0) {
+        while (run % 4) { w.push_back(0.f); ++run; }
+        fb.wsym = run;
+        fb.npair_sym = (int)rows.size() - fb.row0;
+      }
+    }
+    fb.npair_all = (int)rows.size() - fb.row0;
+    while (run % 4) { w.push_back(0.f); ++run; }
+    fb.wall = run;
+    wmax = std::max(wmax, run);
+    cmax = std::max(cmax, std::max(2 * pb.l1 + 1, 2 * pb.l2 + 1));
+    // chunks of l3 whose D rows fit drows (grown one order at a time)
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool sym = pass == 0;
+      (sym ? fb.ch_sym0 : fb.ch_gen0) = (int)chunks.size();
+      int n = 0;
+      for (int s_lo = 0; s_lo < pb.nl3;) {
+        int s_hi = s_lo, r = 0;
+        while (s_hi < pb.nl3) {
+          const int l3 = pb.l3min + 2 * s_hi;
+          const int add = sym ? l3 + 1 : 2 * l3 + 1;
+          if (r + add > drows) break;
+          r += add;
+          ++s_hi;
+        }
+        if (s_hi == s_lo) return "fold tables: one order of D exceeds the per-warp buffer";
+        chunks.push_back(make_int2(s_lo, s_hi));
+        s_lo = s_hi;
+        ++n;
+      }
+      if (n > kFoldMaxChunks) return "fold tables: too many l3 chunks";
+      (sym ? fb.nch_sym : fb.nch_gen) = n;
+    }
+    blks.push_back(fb);
+  }
+  return "";
+}
+
+size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax) {
+  return (size_t)(2 * cmax + 2) * ps * sizeof(float2) + (size_t)wmax * sizeof(float) +
+         (size_t)(1 + nw) * drows * ps * sizeof(float2);
+}
+
+cudaError_t fold_configure() {
+  cudaError_t e;
+  const int cs = kCoupleMaxDynSmem;
+  if ((e = cudaFuncSetAttribute(k_couple_fold<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
+    return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const FoldVariant& fv, int n, const float2* cc,
+                               const int* sym, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s,
+                               const RagInfo* rag) {
+  dim3 grid(tc.n_pb, n);
+#define TP3_FOLD_LAUNCH(NW)                                                                                     \
+  k_couple_fold<NW><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks,    \
+                                                   fv.ps, fv.drows, fv.wmax, fv.cmax, t.klp, tc.KP, sym, Thi, Tlo, \
+                                                   tf32, T32, t.n_ltp, rag)
+  switch (fv.nw) {
+    case 4: TP3_FOLD_LAUNCH(4); break;
+    case 8: TP3_FOLD_LAUNCH(8); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef TP3_FOLD_LAUNCH
+  return cudaGetLastError();
+}
+
+}  // namespace tp3

@@ -844,6 +844,8 @@ cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, con
 
 cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, const float2* cc, const int* sym,
                                void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s, const RagInfo* rag) {
+  if (tc.use_fold >= 0 && tc.fold[tc.use_fold].ok)
+    return launch_couple_fold(t, tc, tc.fold[tc.use_fold], n, cc, sym, Thi, Tlo, tf32, T32, s, rag);
   dim3 grid(tc.n_pb, n);
   const bool w2 = tc.use_warp2 && tc.warp2_ok;
   if ((tc.use_warp && tc.warp_ok) || w2) {
