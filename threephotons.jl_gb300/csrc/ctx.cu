@@ -145,6 +145,19 @@ cudaError_t encode_2d(tp3_ctx* c, CUtensorMap* m, void* ptr, uint64_t inner, uin
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 2-D tensor map over the BF16 T operand in the order-major layout [rows][inner] (inner =
+// shell triples): boxes of 64 shell triples (128 bytes) by 32 orders, 128-byte swizzle.
+cudaError_t encode_2d_mn(tp3_ctx* c, CUtensorMap* m, void* ptr, uint64_t inner, uint64_t rows) {
+  cuuint64_t dims[2] = {inner, rows};
+  cuuint64_t strides[1] = {inner * 2};
+  cuuint32_t box[2] = {64, 32};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 std::string setup_tc(tp3_ctx* c) {
   const Basis& b = c->b;
   DevTables& t = c->t;
@@ -381,7 +394,8 @@ std::string setup_tc(tp3_ctx* c) {
       std::vector<int2> fch;
       int wmx = 0, cmx = 0;
       if (!tp3::build_fold_tables(pbs, rows_gen, fbl, frows, fw, fch, wmx, cmx).empty()) continue;
-      const size_t fixed = tp3::fold_smem_bytes(0, ps, 0, wmx, cmx);
+      const int stage = (1 + b.K * (b.K + 1) / 2 + 3) / 4 * 4;
+      const size_t fixed = tp3::fold_smem_bytes(fvs[v].nw, ps, 0, wmx, cmx, stage);
       const size_t per_row = (size_t)(1 + fvs[v].nw) * ps * sizeof(float2);
       if (fixed + per_row > fvs[v].budget) continue;
       const int drows = (int)std::min<size_t>((size_t)rows_gen, (fvs[v].budget - fixed) / per_row);
@@ -394,7 +408,8 @@ std::string setup_tc(tp3_ctx* c) {
       fv.ps = ps;
       fv.wmax = wmx;
       fv.cmax = cmx;
-      fv.smem = tp3::fold_smem_bytes(fv.nw, ps, drows, wmx, cmx);
+      fv.stage = stage;
+      fv.smem = tp3::fold_smem_bytes(fv.nw, ps, drows, wmx, cmx, stage);
       fv.ok = fv.smem <= fvs[v].budget;
     }
   }
@@ -470,6 +485,8 @@ int ensure_cap(tp3_ctx* c, int n) {
       return cuda_fail(c, e, "cudaMemset T hi/lo");
     if ((e = encode_2d(c, &c->maps.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 128, false)) != cudaSuccess ||
         (e = encode_2d(c, &c->maps.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 128, false)) != cudaSuccess ||
+        (e = encode_2d_mn(c, &c->maps.a_hi_mn, c->d_Thi, t.klp, (uint64_t)n * c->tc.KP)) != cudaSuccess ||
+        (e = encode_2d_mn(c, &c->maps.a_lo_mn, c->d_Tlo, t.klp, (uint64_t)n * c->tc.KP)) != cudaSuccess ||
         (elem == 4 &&
          ((e = encode_2d(c, &c->maps32.a_hi, c->d_Thi, c->tc.KP, (uint64_t)n * t.klp, 128, true)) != cudaSuccess ||
           (e = encode_2d(c, &c->maps32.a_lo, c->d_Tlo, c->tc.KP, (uint64_t)n * t.klp, 128, true)) != cudaSuccess)))

@@ -94,6 +94,7 @@ struct FoldRow {
 struct FoldVariant {
   bool ok = false;
   int nw = 0, drows = 0, ps = 0, wmax = 0, cmax = 0;
+  int stage = 0;  // floats of a warp's staging row (1 + K(K+1)/2 shell triples, rounded to 4)
   size_t smem = 0;
   const FoldBlock* blks = nullptr;
   const FoldRow* rows = nullptr;
@@ -168,6 +169,7 @@ struct RagInfo {
 
 struct TcMaps {
   CUtensorMap a_hi, a_lo, b_hi, b_lo;
+  CUtensorMap a_hi_mn, a_lo_mn;  // BF16 T operand in the order-major layout [lt][ki]
 };
 
 size_t tc_smem_bytes();
@@ -193,7 +195,13 @@ cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);
 std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std::vector<FoldBlock>& blks,
                               std::vector<FoldRow>& rows, std::vector<float>& w, std::vector<int2>& chunks,
                               int& wmax, int& cmax);
-size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax);
+size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage);
+// Layout of the T operand: the folded-row coupling in BF16 mode writes it order-major,
+// [lt][ki] (shell triples contiguous), read by the angular kernel as an MN-major operand;
+// every other coupling form and the TF32 mode use [ki][lt].
+inline bool t_order_major(const TcTables& tc, bool tf32) {
+  return !tf32 && tc.use_fold >= 0 && tc.fold[tc.use_fold].ok;
+}
 cudaError_t fold_configure();
 cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const FoldVariant& fv, int n, const float2* cc,
                                const int* sym, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s,

@@ -107,13 +107,45 @@ __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2
   }
 }
 
+// Phase-2 tile: acc[i][j] = Re sum_r D[row r][pair slot + i] cT[row r][shell + j] over the
+// cnt rows of one order (dp, cp at the order's first row; rows are rstride float4 apart).
+__device__ __forceinline__ void fold_tile(const float4* __restrict__ dp, const float4* __restrict__ cp, int rstride,
+                                          int cnt, float (&acc)[4][4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 2
+  for (int r = 0; r < cnt; ++r) {
+    const float4 d01 = dp[r * rstride], d23 = dp[r * rstride + 1];
+    const float4 c01 = cp[r * rstride], c23 = cp[r * rstride + 1];
+    const float xr[4] = {d01.x, d01.z, d23.x, d23.z}, xi[4] = {d01.y, d01.w, d23.y, d23.w};
+    const float yr[4] = {c01.x, c01.z, c23.x, c23.z}, yi[4] = {c01.y, c01.w, c23.y, c23.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xr[i], yr[j], fmaf(-xi[i], yi[j], acc[i][j]));
+  }
+}
+
+// Tile (q2, q3) of a unit's tile index t (tiles of one k1 row: q2 = 0.., q3 <= q2).
+__device__ __forceinline__ void fold_tile_of(int t, int& q2, int& q3) {
+  q2 = 0;
+  while ((q2 + 1) * (q2 + 2) / 2 <= t) ++q2;
+  q3 = t - q2 * (q2 + 1) / 2;
+}
+
 // grid: (n_pb, n); block NW * 32; dynamic shared memory FoldVariant::smem.
+// T layout: ltmaj = false: [prop][ki][lt] (row stride KP); ltmaj = true (BF16 only):
+// [prop][lt][ki] (row stride klp), written through a per-warp staging row of `stage`
+// floats so that each order's values of the unit's shell triples leave as contiguous runs.
 template <int NW>
 __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff, const FoldBlock* __restrict__ blks,
     const FoldRow* __restrict__ rows, const float* __restrict__ wtab, const int2* __restrict__ chunks, int ps,
-    int drows, int wmax, int cmax, int klp, int KP, const int* __restrict__ symflags, void* __restrict__ Thi,
-    void* __restrict__ Tlo, bool tf32out, float* __restrict__ T32, int ldT32, const RagInfo* __restrict__ rag) {
+    int drows, int wmax, int cmax, int stage, int klp, int KP, const int* __restrict__ symflags,
+    void* __restrict__ Thi, void* __restrict__ Tlo, bool tf32out, bool ltmaj, float* __restrict__ T32, int ldT32,
+    const RagInfo* __restrict__ rag) {
   extern __shared__ __align__(16) float smf[];
   __shared__ int s_next[kFoldMaxChunks];
   __shared__ FoldRow s_rows[kFoldMaxRows];
@@ -149,7 +181,12 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const int klen = s_misc[3];
     for (int i = threadIdx.x; i < klen * fb.nl3; i += blockDim.x) {
       const int ki = i / fb.nl3, sj = i - ki * fb.nl3;
-      fold_store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + fb.lt_base + sj, 0.f, tf32out);
+      if (ltmaj) {
+        const int li = i % klen, lj = i / klen;  // consecutive threads: consecutive shell triples
+        fold_store_split(Thi, Tlo, ((size_t)prop * KP + fb.lt_base + lj) * klp + li, 0.f, false);
+      } else {
+        fold_store_split(Thi, Tlo, ((size_t)prop * klp + ki) * KP + fb.lt_base + sj, 0.f, tf32out);
+      }
       if (T32) T32[((size_t)prop * klp + ki) * ldT32 + fb.lt_base + sj] = 0.f;
     }
     return;
@@ -164,6 +201,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
   float* W = reinterpret_cast<float*>(C2 + (size_t)(cmax + 2) * ps);
   float2* cT = reinterpret_cast<float2*>(W + wmax);
   float2* Dall = cT + (size_t)drows * ps;
+  float* Stage = reinterpret_cast<float*>(Dall + (size_t)NW * drows * ps);  // [NW][stage]
   const float2* src = cc + (size_t)prop * K * nc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   {
@@ -200,6 +238,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
   if (threadIdx.x < kFoldMaxChunks) s_next[threadIdx.x] = 0;
 
   float2* Dw = Dall + (size_t)warp * drows * ps;
+  float* Ts = Stage + (size_t)warp * stage;
   const size_t tbase = (size_t)prop * klp * KP;
   void* ThiP = tf32out ? (void*)((float*)Thi + tbase) : (void*)((__nv_bfloat16*)Thi + tbase);
   void* TloP = tf32out ? (void*)((float*)Tlo + tbase) : (void*)((__nv_bfloat16*)Tlo + tbase);
@@ -284,52 +323,84 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
       const int nt = ta + tb;
       const int nitems = (s_hi - s_lo) * nt;
       const float scale = sym ? 2.f : 1.f;
-      for (int base = 0; base < nitems; base += 32) {
-        const int it = base + lane;
-        if (it >= nitems) break;
-        const int sidx = it / nt;
-        const int tile = it - sidx * nt;
-        const int s = s_hi - 1 - sidx;  // largest l3 first
-        int t = tile, k1 = k1a, pbase = 0;
-        if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; }
-        int q2 = 0;
-        while ((q2 + 1) * (q2 + 2) / 2 <= t) ++q2;
-        const int q3 = t - q2 * (q2 + 1) / 2;
-        const int l3 = l3min + 2 * s;
-        const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
-        const int r0 = fold_drow(s, s_lo, l3min, sym);
-        const float4* dp = reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2);
-        const float4* cp = reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3);
-        const int rstride = ps / 2;  // float4 per row
-        float acc[4][4];
+      const int rstride = ps / 2;  // float4 per row
+      if (ltmaj) {
+        // order by order: tiles -> staging row (the unit's shell triples, k1a's then
+        // k1b's) -> contiguous runs of T[lt][ki]
+        const int na = (k1a + 1) * (k1a + 2) / 2, nb = two ? (k1b + 1) * (k1b + 2) / 2 : 0;
+        const int t3a = k1a * (k1a + 1) * (k1a + 2) / 6, t3b = k1b * (k1b + 1) * (k1b + 2) / 6;
+        for (int s = s_hi - 1; s >= s_lo; --s) {
+          const int l3 = l3min + 2 * s;
+          const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
+          const int r0 = fold_drow(s, s_lo, l3min, sym);
+          const int lt = fb.lt_base + s;
+          for (int tile = lane; tile < nt; tile += 32) {
+            int t = tile, k1 = k1a, pbase = 0, lbase = 0;
+            if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; lbase = na; }
+            int q2, q3;
+            fold_tile_of(t, q2, q3);
+            float acc[4][4];
+            fold_tile(reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2),
+                      reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3), rstride, cnt, acc);
+            const int t3 = k1 * (k1 + 1) * (k1 + 2) / 6;
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i) {
+              const int k2 = 4 * q2 + i;
+              if (k2 > k1) continue;
+              const int loc0 = k2 * (k2 + 1) / 2 + 4 * q3;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-#pragma unroll 2
-        for (int r = 0; r < cnt; ++r) {
-          const float4 d01 = dp[r * rstride], d23 = dp[r * rstride + 1];
-          const float4 c01 = cp[r * rstride], c23 = cp[r * rstride + 1];
-          const float xr[4] = {d01.x, d01.z, d23.x, d23.z}, xi[4] = {d01.y, d01.w, d23.y, d23.w};
-          const float yr[4] = {c01.x, c01.z, c23.x, c23.z}, yi[4] = {c01.y, c01.w, c23.y, c23.w};
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xr[i], yr[j], fmaf(-xi[i], yi[j], acc[i][j]));
+              for (int j = 0; j < 4; ++j) {
+                if (4 * q3 + j <= k2) {
+                  const float v = scale * acc[i][j];
+                  Ts[lbase + loc0 + j] = v;
+                  if (T32P) T32P[(size_t)(t3 + loc0 + j) * ldT32 + lt] = v;
+                }
+              }
+            }
+          }
+          __syncwarp();
+          __nv_bfloat16* hrow = reinterpret_cast<__nv_bfloat16*>(Thi) + ((size_t)prop * KP + lt) * klp;
+          __nv_bfloat16* lrow = reinterpret_cast<__nv_bfloat16*>(Tlo) + ((size_t)prop * KP + lt) * klp;
+          for (int idx = lane; idx < na + nb; idx += 32) {
+            const int ki = idx < na ? t3a + idx : t3b + (idx - na);
+            const float v = Ts[idx];
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            hrow[ki] = h;
+            lrow[ki] = __float2bfloat16_rn(v - __bfloat162float(h));
+          }
+          __syncwarp();
         }
-        const int lt = fb.lt_base + s;
-        const int t3 = k1 * (k1 + 1) * (k1 + 2) / 6;
+      } else {
+        for (int base = 0; base < nitems; base += 32) {
+          const int it = base + lane;
+          if (it >= nitems) break;
+          const int sidx = it / nt;
+          const int tile = it - sidx * nt;
+          const int s = s_hi - 1 - sidx;  // largest l3 first
+          int t = tile, k1 = k1a, pbase = 0;
+          if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; }
+          int q2, q3;
+          fold_tile_of(t, q2, q3);
+          const int l3 = l3min + 2 * s;
+          const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
+          const int r0 = fold_drow(s, s_lo, l3min, sym);
+          float acc[4][4];
+          fold_tile(reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2),
+                    reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3), rstride, cnt, acc);
+          const int lt = fb.lt_base + s;
+          const int t3 = k1 * (k1 + 1) * (k1 + 2) / 6;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int k2 = 4 * q2 + i;
-          if (k2 > k1) continue;
-          const int row0 = t3 + k2 * (k2 + 1) / 2 + 4 * q3;
+          for (int i = 0; i < 4; ++i) {
+            const int k2 = 4 * q2 + i;
+            if (k2 > k1) continue;
+            const int row0 = t3 + k2 * (k2 + 1) / 2 + 4 * q3;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            if (4 * q3 + j <= k2) {
-              const float v = scale * acc[i][j];
-              fold_store_split(ThiP, TloP, (size_t)(row0 + j) * KP + lt, v, tf32out);
-              if (T32P) T32P[(size_t)(row0 + j) * ldT32 + lt] = v;
+            for (int j = 0; j < 4; ++j) {
+              if (4 * q3 + j <= k2) {
+                const float v = scale * acc[i][j];
+                fold_store_split(ThiP, TloP, (size_t)(row0 + j) * KP + lt, v, tf32out);
+                if (T32P) T32P[(size_t)(row0 + j) * ldT32 + lt] = v;
+              }
             }
           }
         }
@@ -441,9 +512,9 @@ std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std:
   return "";
 }
 
-size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax) {
+size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage) {
   return (size_t)(2 * cmax + 2) * ps * sizeof(float2) + (size_t)wmax * sizeof(float) +
-         (size_t)(1 + nw) * drows * ps * sizeof(float2);
+         (size_t)(1 + nw) * drows * ps * sizeof(float2) + (size_t)nw * stage * sizeof(float);
 }
 
 cudaError_t fold_configure() {
@@ -459,10 +530,11 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
                                const int* sym, void* Thi, void* Tlo, bool tf32, float* T32, cudaStream_t s,
                                const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
-#define TP3_FOLD_LAUNCH(NW)                                                                                     \
-  k_couple_fold<NW><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks,    \
-                                                   fv.ps, fv.drows, fv.wmax, fv.cmax, t.klp, tc.KP, sym, Thi, Tlo, \
-                                                   tf32, T32, t.n_ltp, rag)
+  const bool ltmaj = t_order_major(tc, tf32);
+#define TP3_FOLD_LAUNCH(NW)                                                                                      \
+  k_couple_fold<NW><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks,     \
+                                                   fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP, sym, \
+                                                   Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag)
   switch (fv.nw) {
     case 4: TP3_FOLD_LAUNCH(4); break;
     case 8: TP3_FOLD_LAUNCH(8); break;

@@ -574,7 +574,9 @@ struct TcSmemHeader {
 
 // grid: (klp / 128, n); block kThreads; dyn smem = 1 KB alignment slack + stages + header.
 // STORE: write c3 (all four images of every unique point) instead of the Bayes terms.
-template <bool STORE, bool TF32>
+// AMN (BF16 only): T is order-major, [prop][lt][ki]; each stage's A tile arrives as two
+// 64-shell-triple boxes (128-byte swizzle) and is read as an MN-major operand.
+template <bool STORE, bool TF32, bool AMN>
 __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
     const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
     const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
@@ -638,8 +640,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
           last[s] = it;
           uint8_t* st = stages + s * kStageBytes;
           mbar_expect_tx(&hd->full[s], kStageBytes);
-          tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kbk, row0);
-          tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kbk, row0);
+          if (AMN) {
+            const int y = prop * KP + kc * kbk;  // order row of T[lt][ki]
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+              tma_load_2d(st + g * (kABytes / 2), &tmA_hi, &hd->full[s], mtile * kBM + g * 64, y);
+              tma_load_2d(st + kABytes + g * (kABytes / 2), &tmA_lo, &hd->full[s], mtile * kBM + g * 64, y);
+            }
+          } else {
+            tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kbk, row0);
+            tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kbk, row0);
+          }
           tma_load_2d(st + 2 * kABytes, &tmB_hi, &hd->full[s], kc * kbk, h * kBN);
           tma_load_2d(st + 2 * kABytes + kBBytes, &tmB_lo, &hd->full[s], kc * kbk, h * kBN);
         }
@@ -658,7 +669,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = idesc_m128_n256(TF32 ? 2u : 1u);
+      const uint32_t idesc = idesc_m128_n256(TF32 ? 2u : 1u) | (AMN ? (1u << 15) : 0u);  // bit 15: A MN-major
       int it = 0;
       for (int h = 0; h < nhalf && !*abort_flag; ++h) {
         const uint32_t dt = tmem + (uint32_t)(h * kBN);
@@ -668,15 +679,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
           if (!mbar_wait(&hd->full[s], ph, abort_flag, err)) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t st = smem_u32(stages + s * kStageBytes);
-          const uint64_t ahi = smem_desc_sw64(st), alo = smem_desc_sw64(st + kABytes);
+          const uint64_t ahi = AMN ? smem_desc_mn_sw128(st, kABytes / 2) : smem_desc_sw64(st);
+          const uint64_t alo = AMN ? smem_desc_mn_sw128(st + kABytes, kABytes / 2) : smem_desc_sw64(st + kABytes);
           const uint64_t bhi = smem_desc_sw64(st + 2 * kABytes), blo = smem_desc_sw64(st + 2 * kABytes + kBBytes);
-          // two MMA K-steps of 32 bytes per 64-byte row (K = 16 bf16 or K = 8 tf32 each)
+          // two MMA K-steps per stage (K = 16 bf16 or K = 8 tf32 each): 32 bytes along a
+          // K-major row, or 16 rows of 128 bytes (2 KB) of an MN-major tile
 #pragma unroll
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t dk = (uint64_t)(ks * 2);  // +32 bytes, in 16-byte descriptor units
-            mma_issue<TF32>(dt, ahi + dk, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
-            mma_issue<TF32>(dt, ahi + dk, blo + dk, idesc, 1u);
-            mma_issue<TF32>(dt, alo + dk, bhi + dk, idesc, 1u);
+            const uint64_t da = AMN ? (uint64_t)(ks * 128) : dk;  // +2048 bytes for MN-major A
+            mma_issue<TF32>(dt, ahi + da, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+            mma_issue<TF32>(dt, ahi + da, blo + dk, idesc, 1u);
+            mma_issue<TF32>(dt, alo + da, bhi + dk, idesc, 1u);
           }
           mma_commit(&hd->empty[s]);
         }
@@ -803,14 +817,13 @@ size_t tc_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(Tc
 cudaError_t tc_configure() {
   cudaError_t e;
   const int smem = (int)tc_smem_bytes();
-  if ((e = cudaFuncSetAttribute(k_angular_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
-          cudaSuccess)
+  const cudaFuncAttribute ds = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if ((e = cudaFuncSetAttribute(k_angular_tc<false, false, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<true, false, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<false, true, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<true, true, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<false, false, true>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tc<true, false, true>, ds, smem)) != cudaSuccess)
     return e;
   const int cs = kCoupleMaxDynSmem, css = kCoupleSmallSmem;
 #define TP3_CP_ATTR(S, W)                                                                                    \
@@ -916,14 +929,19 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
                               const RagInfo* rag) {
   dim3 grid(t.klp / kBM, n);
   const size_t smem = tc_smem_bytes();
-#define TP3_ANG(ST, TF)                                                                                        \
-  k_angular_tc<ST, TF><<<grid, kThreads, smem, s>>>(maps.a_hi, maps.a_lo, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, \
-                                                     tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out,      \
-                                                     t.u_to_g, t.N, err, rag)
+  const bool amn = t_order_major(tc, tf32);
+#define TP3_ANG(ST, TF, MN, AH, AL)                                                                            \
+  k_angular_tc<ST, TF, MN><<<grid, kThreads, smem, s>>>(AH, AL, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu,        \
+                                                         tc.nhalf, t.klength, qt, Qs, t.tf, t.mult, Eslab, c3out, \
+                                                         t.u_to_g, t.N, err, rag)
   if (c3out) {
-    if (tf32) TP3_ANG(true, true); else TP3_ANG(true, false);
+    if (tf32) TP3_ANG(true, true, false, maps.a_hi, maps.a_lo);
+    else if (amn) TP3_ANG(true, false, true, maps.a_hi_mn, maps.a_lo_mn);
+    else TP3_ANG(true, false, false, maps.a_hi, maps.a_lo);
   } else {
-    if (tf32) TP3_ANG(false, true); else TP3_ANG(false, false);
+    if (tf32) TP3_ANG(false, true, false, maps.a_hi, maps.a_lo);
+    else if (amn) TP3_ANG(false, false, true, maps.a_hi_mn, maps.a_lo_mn);
+    else TP3_ANG(false, false, false, maps.a_hi, maps.a_lo);
   }
 #undef TP3_ANG
   return cudaGetLastError();

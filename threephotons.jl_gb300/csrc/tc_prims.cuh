@@ -85,6 +85,18 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
   return d;
 }
 
+// MN-major operand, 128-byte swizzle: rows of 128 bytes along M (64 bf16), 8-row atoms
+// of 1 KB along K (SBO = 1024 B), 64-element M groups lbo bytes apart (LBO).
+__device__ __forceinline__ uint64_t smem_desc_mn_sw128(uint32_t addr, uint32_t lbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;  // LBO: next 64 elements along M
+  d |= (uint64_t)(1024u >> 4) << 32;            // SBO: next 8 rows along K
+  d |= (uint64_t)1u << 46;                      // descriptor version (sm_100 family)
+  d |= (uint64_t)2u << 61;                      // SWIZZLE_128B
+  return d;
+}
+
 template <bool TF32>
 __device__ __forceinline__ void mma_issue(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
