@@ -51,7 +51,7 @@ METRIC = "c3+Bayes proposal evals/s at L18 K26 N32"
 UNIT = "proposals/s"
 MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
 COUPLING_NAMES = {0: "fused_512", 1: "split", 2: "fused_256x2", 3: "warp_local", 4: "warp_local_256x2",
-                  5: "folded_8w", 6: "folded_4w_x2"}
+                  5: "folded_8w", 6: "folded_7w"}
 DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
 
 

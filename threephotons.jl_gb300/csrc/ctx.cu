@@ -373,8 +373,9 @@ std::string setup_tc(tp3_ctx* c) {
       (e = upload(c, Fhi32, &tc.Fhi32)) != cudaSuccess || (e = upload(c, Flo32, &tc.Flo32)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
-  // folded-row coupling: two tilings (8 warps in up to 225 KB, one CTA per SM; 4 warps in
-  // up to 110 KB, two CTAs per SM), each with the largest per-warp D buffer that fits
+  // folded-row coupling: two tilings (8 warps and 7 warps in up to 225 KB, one CTA per SM;
+  // 7 warps take a K = 26 proposal's 13 folded units in two rounds with one warp idle),
+  // each with the largest per-warp D buffer that fits
   if ((e = tp3::fold_configure()) != cudaSuccess) return std::string("fold coupling: ") + cudaGetErrorString(e);
   {
     int rows_gen = 0;  // D rows of the largest block, general path (all l3 in one chunk)
@@ -385,7 +386,7 @@ std::string setup_tc(tp3_ctx* c) {
     }
     const int ps = (b.K + 5 + 31) / 32 * 32;
     const struct { int nw; size_t budget; } fvs[2] = {{8, (size_t)tp3::kCoupleMaxDynSmem},
-                                                      {4, (size_t)tp3::kCoupleSmallSmem}};
+                                                      {7, (size_t)tp3::kCoupleMaxDynSmem}};
     for (int v = 0; v < 2; ++v) {
       tp3::FoldVariant& fv = tc.fold[v];
       std::vector<tp3::FoldBlock> fbl;

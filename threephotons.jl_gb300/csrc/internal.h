@@ -104,7 +104,7 @@ struct FoldVariant {
 
 // Device tables of the tensor-core path.
 struct TcTables {
-  // folded-row coupling: [0] 8 warps, one CTA per SM; [1] 4 warps, two CTAs per SM
+  // folded-row coupling: [0] 8 warps, [1] 7 warps, one CTA per SM
   FoldVariant fold[2];
   int use_fold = -1;
   int n_pb = 0, maxs = 0, SDmax = 0;

@@ -520,7 +520,7 @@ size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage)
 cudaError_t fold_configure() {
   cudaError_t e;
   const int cs = kCoupleMaxDynSmem;
-  if ((e = cudaFuncSetAttribute(k_couple_fold<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+  if ((e = cudaFuncSetAttribute(k_couple_fold<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
       (e = cudaFuncSetAttribute(k_couple_fold<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
     return e;
   return cudaSuccess;
@@ -536,7 +536,7 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
                                                    fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP, sym, \
                                                    Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag)
   switch (fv.nw) {
-    case 4: TP3_FOLD_LAUNCH(4); break;
+    case 7: TP3_FOLD_LAUNCH(7); break;
     case 8: TP3_FOLD_LAUNCH(8); break;
     default: return cudaErrorInvalidValue;
   }
