@@ -4,6 +4,7 @@
     python bench.py --impl reference [--steps K] [--warmup W]
     python bench.py --workload ragged      # 64 chains x 16 candidates, K in 16..26, L in 12..18, own histograms
     python bench.py --workload learned     # learned vs plain annealer: time to the plain final energy
+    python bench.py --no-ragged --no-learned   # the proposal line without the two extra legs
 
 --mode tuned (and auto) runs the evaluation-variant autotuner first and benchmarks its
 choice; plain / tc / tf32 force the plain FP32, BF16 hi/lo x3 or TF32 hi/lo x3 path.
@@ -21,6 +22,10 @@ Synthetic data stands in for the reference's PDB / measured histograms (none are
 benchmark datasets).  The L2 cache (129 MB) is flushed by a 512 MB write between
 timed steps, outside the per-step event window.
 
+The line also carries `ragged` (64 chains of mixed L and K, one ragged launch per graph
+replay, with a spot check of three chains against contexts of their own shape) and
+`learned` (the learned-proposal experiment with its network-free drift ablation).
+
 Rank 0 prints one JSON line.  --gpus N > 1 runs N independent replicas (one per
 GPU, launched by torchrun); the path has no collective (annealing chains and
 proposals are independent), so scaling is weak.
@@ -33,6 +38,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -53,6 +59,16 @@ MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
 COUPLING_NAMES = {0: "fused_512", 1: "split", 2: "fused_256x2", 3: "warp_local", 4: "warp_local_256x2",
                   5: "folded_8w", 6: "folded_7w"}
 DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each stage's kernel, measured
+# with ncu on one 32-proposal launch of this workload and written as bytes per proposal plus
+# a per-launch constant (each proposal's T is written and read once; the histogram and the
+# tables are read once per launch), by (mode, coupling form).
+STAGE_TRAFFIC = {
+    ("tc_bf16x3", "folded_7w"): {"coupling": (154.2e6 / 32, 0.0), "angular": (230.2e6 / 32, 0.0),
+                                 "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal "
+                                           "launch, scaled in proportion to the proposals "
+                                           "(profiles/traffic_L18K26N32_b32_folded7w.md)"},
+}
 
 
 def dist_env():
@@ -162,7 +178,7 @@ def sample_clocks_stop(p, f, path, gpu_index):
             "samples": len(sm)}
 
 
-def cpu_baseline_sample(base, hist, n_props=1):
+def cpu_baseline_sample(base, hist, n_props=3):
     """Reference-form CPU path (oracle port) on this host: bounded sample."""
     from oracle.refcpu import RefCPU, threads
     t0 = time.time()
@@ -251,18 +267,18 @@ def _molecule_job(args):
     return intensity_coefficients(synthetic_molecule(n_atoms, seed=seed), LMAX, KMAX, RMAX, kcount=kcount)
 
 
-def run_ragged(args):
+def ragged_measure(reps: int, warmup: int, rank: int = 0) -> dict:
     """64 chains x 16 speculative candidates per launch; chain c has its own K (16..26), L
     (12..18), molecule (200-400 atoms) and 1e9-triplet histogram; all candidates of a
     launch go through one ragged tensor-core launch on the L18 K26 N32 shape, replayed
-    from a CUDA graph."""
+    from a CUDA graph.  A spot check scores three chains' current states through the
+    ragged launch and through contexts of their own (L, K) and reports the largest
+    relative energy difference."""
     import multiprocessing as mp
     import torch
     import tp3
     from tp3.chains import Chains
-    from tp3.structure import poisson_histogram, loadHistograms
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
+    from tp3.structure import poisson_histogram, loadHistograms, seanindex0
     nch, ncand = 64, 16
     rng = np.random.default_rng(20250301 + rank)
     Ks = rng.integers(16, K + 1, nch)
@@ -272,7 +288,6 @@ def run_ragged(args):
         coeffs = pool.map(_molecule_job, [(int(a), 5000 + 97 * c + rank, K) for c, a in enumerate(atoms)])
     coeffs = np.stack([c[:K] for c in coeffs])
     basis = tp3.calculate_basis(L, LMAX, N, K)
-    from tp3.structure import seanindex0
     hists = []
     for c in range(nch):
         x = coeffs[c].copy()
@@ -292,12 +307,11 @@ def run_ragged(args):
         basis.set_mode(tp3.TP3_MODE_TC_BF16X3)  # ragged launches are tensor-core only
     shapes = [(int(Ls[c]), int(Ks[c]), c) for c in range(nch)]
     ch = Chains(basis, coeffs, 0.1, math.pi / 4, 1.02, 0.99998, 4242 + rank, ncand=ncand, shapes=shapes)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ch.run(1)
     s0 = ch.state()
     stream = torch.cuda.Stream()  # a real stream: the library treats handle 0 as "its own stream"
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = max(3, args.steps)
     torch.cuda.synchronize()
     basis.set_stream(stream.cuda_stream)
     ev0.record(stream)
@@ -307,58 +321,114 @@ def run_ragged(args):
     ms = ev0.elapsed_time(ev1)
     s1 = ch.state()
     basis.set_stream(None)
+    final = ch.coeff()
     ch.close()
-    ms = max_over_ranks(ms)
-    value = whole_job_rate(ws, nch * ncand, reps, ms)
-    line = {"metric": "ragged c3+Bayes proposal evals/s, 64 chains x 16 candidates, K 16..26, L 12..18, N32",
-            "value": value, "unit": UNIT, "n_gpus": ws, "steps": reps, "warmup": args.warmup,
-            "ms_per_step": ms / reps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": DTYPES.get(basis.mode, "fp32"), "data": "synthetic",
-            "config": {"workload": "64 chains (own molecule of 200-400 atoms, own 1e9-triplet histogram, K in "
-                                   "16..26, L in 12..18, N32, LMAX25) x 16 speculative candidates per CUDA-graph "
-                                   "replay; one ragged tensor-core launch per step on the L18 K26 shape",
-                       "Ks": Ks.tolist(), "Ls": Ls.tolist(), "mode": MODE_NAMES.get(basis.mode),
-                       "autotune": [{"mode": MODE_NAMES.get(m), "coupling": COUPLING_NAMES.get(sp) if m else None,
-                                     "ms_per_proposal": t} for m, sp, t in tuning]},
+    # spot check: three chains of distinct shapes, ragged launch vs contexts of their own shape
+    picks, seen = [], set()
+    for c in range(nch):
+        if (int(Ls[c]), int(Ks[c])) not in seen and len(picks) < 3:
+            seen.add((int(Ls[c]), int(Ks[c])))
+            picks.append(c)
+    dev = torch.device("cuda")
+    states = np.stack([final[c] for c in picks])
+    d_c = torch.from_numpy(np.ascontiguousarray(states).view(np.float64).copy()).to(dev)
+    d_l = torch.tensor([(int(Ls[c]), int(Ks[c]), c) for c in picks], dtype=torch.int32, device=dev)
+    d_E = torch.empty(len(picks), dtype=torch.float64, device=dev)
+    basis.energy_batch_ragged_device(len(picks), d_c.data_ptr(), d_l.data_ptr(), d_E.data_ptr())
+    basis.sync()
+    E_rag = d_E.cpu().numpy()
+    rel = []
+    for j, c in enumerate(picks):
+        own = tp3.calculate_basis(int(Ls[c]), LMAX, N, int(Ks[c]))
+        own.set_mode(basis.mode)
+        own.set_histogram(hists[c])
+        E_own = float(own.energy_batch(states[j][None, :int(Ks[c])])[0])
+        own.close()
+        rel.append(abs(E_rag[j] - E_own) / abs(E_own))
+    mode = basis.mode
+    basis.close()
+    return {"value": nch * ncand * reps / (ms / 1e3), "unit": UNIT, "ms_per_launch": ms / reps, "launches": reps,
             "chain_steps_per_s": float((s1["steps"] - s0["steps"]).sum()) / (ms / 1e3),
-            # per replay: propose, gather, couple, angular + Bayes, finalize, select, commit
-            "gpu_launches": 7 * reps}
+            "Ks": Ks.tolist(), "Ls": Ls.tolist(), "mode": MODE_NAMES.get(mode),
+            "autotune": [{"mode": MODE_NAMES.get(m), "coupling": COUPLING_NAMES.get(sp) if m else None,
+                          "ms_per_proposal": t} for m, sp, t in tuning],
+            "spot_check": {"chains": [(int(Ls[c]), int(Ks[c])) for c in picks],
+                           "max_rel_energy_diff_vs_own_shape_context": float(max(rel))},
+            "gpu_launches_per_replay": 7,
+            "workload": "64 chains (own molecule of 200-400 atoms, own 1e9-triplet histogram, K in 16..26, "
+                        "L in 12..18, N32, LMAX25) x 16 speculative candidates per CUDA-graph replay; one ragged "
+                        "tensor-core launch per step on the L18 K26 shape"}
+
+
+def run_ragged(args):
+    """--workload ragged: the ragged measurement as its own JSON line."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    r = ragged_measure(max(3, args.steps), args.warmup, rank)
+    ms = max_over_ranks(r["ms_per_launch"] * r["launches"])
+    value = whole_job_rate(ws, 64 * 16, r["launches"], ms)
+    line = {"metric": "ragged c3+Bayes proposal evals/s, 64 chains x 16 candidates, K 16..26, L 12..18, N32",
+            "value": value, "unit": UNIT, "n_gpus": ws, "steps": r["launches"], "warmup": args.warmup,
+            "ms_per_step": ms / r["launches"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES.get(tp3_mode_id(r["mode"]), "fp32"), "data": "synthetic",
+            "config": {"workload": r["workload"], "Ks": r["Ks"], "Ls": r["Ls"], "mode": r["mode"],
+                       "autotune": r["autotune"]},
+            "chain_steps_per_s": r["chain_steps_per_s"], "spot_check": r["spot_check"],
+            "gpu_launches": r["gpu_launches_per_replay"] * r["launches"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    basis.close()
     return 0
 
 
-def run_learned(args):
+def tp3_mode_id(name):
+    return {v: k for k, v in MODE_NAMES.items()}.get(name, 0)
+
+
+def learned_measure(rank: int = 0, **kw) -> dict:
     """The learned-proposal experiment at L18 K26 N32 (64 chains x 16 candidates): the
     isotropic per-shell annealer logs >= 1e6 moves, the network is trained on the device,
     and the learned annealer's wall-clock to the plain annealer's final median energy is
-    measured from fresh starts (each shell of the molecule turned by a Haar rotation)."""
-    import torch
+    measured from fresh starts (each shell of the molecule turned by a Haar rotation),
+    beside the network-free drift annealer (the ablation)."""
     import tp3
     from tp3.learned import learned_vs_plain
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
     base = molecule_coefficients()
     basis = tp3.calculate_basis(L, LMAX, N, K)
     basis.set_histogram(build_histogram(basis, base))
     basis.autotune(64)
-    res = learned_vs_plain(basis, base, seed=2024 + rank)
+    res = learned_vs_plain(basis, base, seed=2024 + rank, **kw)
     basis.close()
-    plain_s = res["plain"]["seconds"]
-    lrn_s = res["learned"]["seconds_to_target"] if res["learned"]["reached"] else None
+    d = res.get("drift", {})
+    return {"plain_seconds": res["plain"]["seconds"], "plain_launches": res["plain"]["launches"],
+            "plain_final_median_E": res["plain"]["final_median_E"],
+            "learned_seconds_to_target": res["learned"]["seconds_to_target"] if res["learned"]["reached"] else None,
+            "learned_launches": res["learned"]["launches"], "learned_median_E": res["learned"]["median_E"],
+            "time_ratio": res["time_ratio"],
+            "drift_seconds_to_target": d.get("seconds_to_target") if d.get("reached") else None,
+            "drift_launches": d.get("launches"), "drift_median_E": d.get("median_E"),
+            "time_ratio_drift": res.get("time_ratio_drift"),
+            "accept_rate": {"plain": res["plain"]["accept_rate"], "learned": res["learned"]["accept_rate"],
+                            "drift": d.get("accept_rate")},
+            "collect_moves": res["collect"]["moves"],
+            "train": {k: res["train"][k] for k in ("steps", "heldout_nll_before", "heldout_nll_after", "seconds")},
+            "workload": "64 chains x 16 candidates, per-shell SO(3) moves, 327-atom molecule, 1e9-triplet "
+                        "histogram; plain = isotropic steps, learned = 0.8 network / 0.2 isotropic mixture with "
+                        "Metropolis-Hastings correction, drift = the same mixture with the drift along the newest "
+                        "gradient estimate and no network"}
+
+
+def run_learned(args):
+    """--workload learned: the learned-proposal measurement as its own JSON line."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    r = learned_measure(rank)
     line = {"metric": "time to the plain annealer's final median energy (learned proposal), L18 K26 N32",
-            "value": lrn_s, "unit": "s", "n_gpus": ws, "steps": res["plain"]["launches"], "warmup": 1,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, fp64 moves",
-            "data": "synthetic",
-            "config": {"workload": "64 chains x 16 candidates, per-shell SO(3) moves, 327-atom molecule, "
-                                   "1e9-triplet histogram; plain = isotropic steps, learned = 0.8 network / 0.2 "
-                                   "isotropic mixture with Metropolis-Hastings correction",
-                       "collect_moves": res["collect"]["moves"]},
-            "plain_seconds": plain_s, "time_ratio": res["time_ratio"],
-            "plain_final_median_E": res["plain"]["final_median_E"], "learned_median_E": res["learned"]["median_E"],
-            "accept_rate": {"plain": res["plain"]["accept_rate"], "learned": res["learned"]["accept_rate"]},
-            "train": {k: res["train"][k] for k in ("steps", "heldout_nll_before", "heldout_nll_after", "seconds")}}
+            "value": r["learned_seconds_to_target"], "unit": "s", "n_gpus": ws, "steps": r["plain_launches"],
+            "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network, fp64 moves", "data": "synthetic",
+            "config": {"workload": r["workload"], "collect_moves": r["collect_moves"]}, **r}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -377,6 +447,8 @@ def main():
                     help="force a tensor-core coupling form (with --mode tc/tf32)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chains", action="store_true")
+    ap.add_argument("--no-ragged", action="store_true", help="leave the ragged-chain key out of the line")
+    ap.add_argument("--no-learned", action="store_true", help="leave the learned-proposal key out of the line")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -429,8 +501,8 @@ def main():
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    clk_path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
-    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    clk_dir = tempfile.mkdtemp(prefix="tp3_clocks_")
+    clk_path = os.path.join(clk_dir, f"clocks_rank{rank}.csv")
     cp, cf = sample_clocks_start(clk_path)
     time.sleep(0.3)
     if ws > 1:
@@ -469,7 +541,9 @@ def main():
     if not np.allclose(E_host, E_dev, rtol=0, atol=0):
         raise SystemExit("device-resident and host-API energies differ")
 
-    # roofline of the dominant kernel (angular contraction + fused Bayes)
+    # per-stage rooflines: the coupling (SIMT FP32, the longest-running kernel) against the
+    # FP32 FMA peak measured in this run, the angular contraction + fused Bayes against the
+    # BF16 tensor peak of MEASURED_PEAKS.json
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 1900.0, "fallback"
     if os.path.exists(peaks_path):
@@ -484,22 +558,20 @@ def main():
     W_b = min(2.0 * G * n_lt * klength, 2.0 * nnz * klength + klength * (4 * N * M * M * 2 + 4 * N * N * M * 2))
     per_launch_ms = ms_prof / max(1, n_prof)
     achieved = W_b * B / (per_launch_ms / 1e3) / 1e12
-    # DRAM traffic of the angular kernel, measured with ncu (dram__bytes_read + write) on a
-    # 32-proposal launch of this workload: 230.7 MB, i.e. 7.09 MB per proposal plus the folded
-    # histogram and F read once per launch; scaled here to this launch's proposals
-    traffic = None
-    if mode_used == 1:
-        traffic = 7.09e6 * B + 7.7e6
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch", "peak_source": f"{peak_src} bf16 dense burst",
-                "kernel": "angular contraction + fused Bayes", "kernel_ms_per_launch": per_launch_ms,
-                "algorithmic_flop_per_proposal": W_b,
-                "note": "the tensor-core stage; the longest-running kernel is the SIMT FP32 coupling, whose "
-                        "roofline against the measured FP32 FMA peak is stages.coupling"}
-
-    # per-stage rooflines: the coupling (SIMT FP32) against the measured FFMA peak, the
-    # angular contraction against the BF16 tensor peak
+    cform = None
+    if tuning:
+        best = min((t for t in tuning if t["mode"] == MODE_NAMES.get(mode_used)), key=lambda t: t["ms_per_proposal"],
+                   default=None)
+        cform = best["coupling"] if best else None
+    elif args.coupling >= 0:
+        cform = COUPLING_NAMES.get(args.coupling)
+    traffic_c = traffic_a = None
+    tsrc = STAGE_TRAFFIC.get((MODE_NAMES.get(mode_used), cform))
+    if tsrc is not None:
+        traffic_c = tsrc["coupling"][0] * B + tsrc["coupling"][1]
+        traffic_a = tsrc["angular"][0] * B + tsrc["angular"][1]
     stages = None
+    roofline = None
     if n_prof_c > 0:
         # W_a = 10 P2 basislen + 4 S klength (pair-factorised coupling), S = sum over the
         # l-triples (even l <= L, triangle) of 2 l3 + 1
@@ -512,20 +584,26 @@ def main():
         ms_c = ms_prof_c / n_prof_c
         fp32_peak = basis.measure_fp32_peak()
         ach_c = W_a * B / (ms_c / 1e3) / 1e12
-        cform = None
-        if tuning:
-            best = min((t for t in tuning if t["mode"] == MODE_NAMES.get(mode_used)), key=lambda t: t["ms_per_proposal"],
-                       default=None)
-            cform = best["coupling"] if best else None
-        elif args.coupling >= 0:
-            cform = COUPLING_NAMES.get(args.coupling)
         stages = {"coupling": {"bound": "fp32", "kernel": f"coupling ({cform or 'default form'})",
                                "ms_per_launch": ms_c, "algorithmic_flop_per_proposal": W_a, "achieved": ach_c,
                                "peak": fp32_peak, "frac": ach_c / fp32_peak, "unit": "TFLOP/s",
-                               "peak_source": "measured FFMA (tp3_measure_fp32_peak, this run)"},
-                  "angular": {"bound": "tensor", "ms_per_launch": per_launch_ms, "algorithmic_flop_per_proposal": W_b,
+                               "peak_source": "measured FFMA (tp3_measure_fp32_peak, this run)",
+                               "traffic": traffic_c},
+                  "angular": {"bound": "tensor", "kernel": "angular contraction + fused Bayes (tcgen05)",
+                              "ms_per_launch": per_launch_ms, "algorithmic_flop_per_proposal": W_b,
                               "achieved": achieved, "peak": peak, "frac": achieved / peak, "unit": "TFLOP/s",
-                              "peak_source": f"{peak_src} bf16 dense burst"}}
+                              "peak_source": f"{peak_src} bf16 dense burst", "traffic": traffic_a}}
+        # headline: the dominant (longest-running) kernel of the step
+        dom = "coupling" if ms_c >= per_launch_ms else "angular"
+        st = stages[dom]
+        roofline = {"bound": st["bound"], "achieved": st["achieved"], "peak": st["peak"], "unit": "TFLOP/s",
+                    "frac": st["frac"], "traffic": st["traffic"], "traffic_unit": "bytes per launch",
+                    "traffic_source": tsrc["source"] if tsrc else None, "peak_source": st["peak_source"],
+                    "kernel": st["kernel"], "kernel_ms_per_launch": st["ms_per_launch"],
+                    "algorithmic_flop_per_proposal": st["algorithmic_flop_per_proposal"],
+                    "share_of_step": st["ms_per_launch"] / ms_per_step,
+                    "note": "the coupling runs on the FP32 FMA pipes (MEASURED_PEAKS.json has no FP32 figure, so "
+                            "its peak is measured in this run); the tensor-core stage is stages.angular"}
 
     # device-resident annealing chains: 64 chains x 16 speculative candidates per graph replay
     chains_info = None
@@ -563,7 +641,7 @@ def main():
             chp.run(1)
             q0 = chp.state()
             t0 = time.perf_counter()
-            chp.run(2)
+            chp.run(10)
             q1 = chp.state()
             dtp = time.perf_counter() - t0
             chp.close()
@@ -586,9 +664,21 @@ def main():
             "gpu_launches": kernels_per_step * args.steps}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(base, hist)
+    basis.close()
+    # the batched ragged workload (64 chains of mixed L and K) and the learned-proposal
+    # experiment with its drift-only ablation, measured in the same run (rank 0)
+    if rank == 0 and not args.no_ragged:
+        try:
+            line["ragged"] = ragged_measure(10, 2, rank)
+        except Exception as exc:  # informational keys: report why they are missing
+            line["ragged"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+    if rank == 0 and not args.no_learned:
+        try:
+            line["learned"] = learned_measure(rank)
+        except Exception as exc:
+            line["learned"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    basis.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0

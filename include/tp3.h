@@ -231,10 +231,15 @@ int tp3_chains_restore(tp3_chains* chains, const void* buf, size_t bytes);
  * density (the network part a two-component mixture over a, evaluated at x' for the
  * reverse step with the network re-run there) corrects the acceptance.  The network
  * must have n_in = (L+1)^2 + 33 and max_rows >= chains x candidates x K.
- * No reference counterpart for the two per-shell kinds. */
+ * TP3_MOVE_DRIFT: the same mixture with probability p_net and no network: u_k = the
+ * chain's newest gradient estimate e_k, all s_k = 0.  The drift is a fixed parameter of
+ * the step, so the proposal is symmetric and plain Metropolis acceptance is exact (net
+ * is ignored).  It measures what a trained network adds over its own strongest input.
+ * No reference counterpart for the three per-shell kinds. */
 #define TP3_MOVE_REFERENCE 0
 #define TP3_MOVE_SHELL_SO3 1
 #define TP3_MOVE_LEARNED 2
+#define TP3_MOVE_DRIFT 3
 int tp3_chains_set_move(tp3_chains* chains, int kind, double sigma0, double p_net, tp3_mlp* net);
 
 /* Move log for training the network: a ring of `launches` launches of per-shell

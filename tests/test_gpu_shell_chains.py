@@ -233,6 +233,51 @@ def test_learned_moves_match_oracle(setup):
     net.close()
 
 
+def test_drift_moves_match_oracle(setup):
+    """The network-free drift move: with a planted gradient history, every logged step is
+    v = a sigma f(u) u + sigma z (drift-drawn) or sigma z (isotropic) with u the chain's
+    newest gradient estimate and isotropic scales; the proposal is symmetric, so the
+    logged Metropolis-Hastings log ratio is exactly 0; energy changes match the FP64
+    oracle."""
+    basis, e64, start, p = setup
+    nch, B = 2, 8
+    L, LMAX, K = p["L"], p["LMAX"], p["K"]
+    T0, sigma0, decay, p_net = 2.0, 0.3, 0.995, 0.8
+    ch = Chains(basis, np.repeat(start[None], nch, axis=0), T0, 0.1, 1.05, decay, SEED, ncand=B)
+    ch.set_move(tp3.TP3_MOVE_DRIFT, sigma0, p_net)
+    ch.enable_move_log(4)
+    blob = bytearray(ch.snapshot())
+    ng = nch * 8 * K * 3
+    ghist = np.random.default_rng(9).normal(size=(nch, 8, K, 3)).astype(np.float32)
+    blob[len(blob) - 4 * ng:] = ghist.tobytes()
+    ch.restore(bytes(blob))
+    ch.run(1)
+    n = ch.move_log_count()
+    assert n == nch * B
+    stride = (n_in_for(L) + 31) // 32 * 32
+    _, V, M = _gather(ch, list(range(n)), K, stride)
+    E0 = e64(start)
+    n_drift = 0
+    for c in range(nch):
+        u = ghist[c, 0].astype(np.float64)
+        for i in range(B):
+            j = c * B + i
+            comp = 1.0 if oc.component_uniform(SEED, i, c) < p_net else 0.0
+            assert M[j, 3] == comp
+            n_drift += int(comp)
+            z, a = oc.shell_noise(SEED, 0, c, i, K)
+            sig_i = sigma0 / 1.05 ** i
+            v = V[j * K:(j + 1) * K] * M[j, 5]
+            m, s = oc.shell_params(u, np.zeros((K, 3)), sig_i)
+            vref = a * m + np.exp(s) * z if comp else sig_i * z
+            np.testing.assert_allclose(v, vref, rtol=1e-5, atol=1e-6)
+            assert M[j, 4] == 0.0
+            x2 = oc.rotate_shells(start, v, L, LMAX)
+            assert M[j, 0] == pytest.approx(e64(x2) - E0, abs=5e-7 * abs(E0))
+    assert 0 < n_drift < nch * B
+    ch.close()
+
+
 def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
     """The full learned-proposal protocol at the small configuration: the plain
     annealer's logged moves train the network on the device (held-out loss falls), and
@@ -262,8 +307,10 @@ def test_learned_proposal_gain_is_measured(config1, config1_hist, capsys):
 def test_learned_proposal_gain_at_production_shape(capsys):
     """A shortened run of the benchmark's protocol at L18 K26 N32 (64 chains x 16
     candidates: 300 logged launches, 600 Adam steps, 150 evaluation launches): the
-    learned annealer reaches the plain annealer's final median energy in well under its
-    wall-clock (the full protocol, bench.py --workload learned, measures about 0.25)."""
+    learned annealer reaches the plain annealer's final median energy in at most half its
+    wall-clock (the spec bar).  The network-free drift annealer (drift along the
+    newest gradient estimate, same mixture) runs the same protocol beside it; its ratio
+    is reported so the network's own contribution is measured, not assumed."""
     import os
     import sys
     from tp3.learned import learned_vs_plain
@@ -278,8 +325,12 @@ def test_learned_proposal_gain_at_production_shape(capsys):
     finally:
         basis.close()
     assert res["learned"]["reached"]
-    assert res["time_ratio"] < 0.75, res["time_ratio"]
+    assert res["time_ratio"] <= 0.5, res["time_ratio"]
+    assert "drift" in res and math.isfinite(res["drift"]["median_E"])
     with capsys.disabled():
+        d = res["drift"]
         print(f"\n[learned proposal, L18 K26 N32, shortened] plain {res['plain']['seconds']:.2f} s -> "
               f"{res['plain']['final_median_E']:.3f}; learned {res['learned']['seconds_to_target']:.2f} s "
-              f"({res['learned']['launches']} launches), time ratio {res['time_ratio']:.3f}")
+              f"({res['learned']['launches']} launches), time ratio {res['time_ratio']:.3f}; drift-only "
+              f"{d['seconds_to_target']:.2f} s ({d['launches']} launches, reached={d['reached']}), "
+              f"time ratio {res['time_ratio_drift']}")

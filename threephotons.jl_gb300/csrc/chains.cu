@@ -44,6 +44,11 @@
 // The network's history inputs (the chain's recent dE/T and gradient estimates) and
 // the candidate's temperature are fixed parameters of the step, so every step is an
 // exact MH step for exp(-E/T).
+// TP3_MOVE_DRIFT is the same mixture without a network: the drift direction u_k is the
+// chain's newest gradient estimate e_k and the scales are isotropic (s_k = 0).  The
+// drift is a fixed parameter of the step, so the proposal is symmetric and the plain
+// Metropolis rule is exact.  It isolates what the trained network adds over its own
+// strongest input.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -455,7 +460,8 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
                                                        const ChainState* __restrict__ cs,
                                                        const double* __restrict__ sigma, int nl, int B, int K, int LMAX,
                                                        int L, double f, uint64_t seed, const float* __restrict__ O,
-                                                       double p_net, double* __restrict__ vout,
+                                                       const float* __restrict__ G, double p_net,
+                                                       double* __restrict__ vout,
                                                        float* __restrict__ wout, int* __restrict__ comp,
                                                        double* __restrict__ lq, const double* __restrict__ delta,
                                                        const int* __restrict__ doff, float* __restrict__ vlog,
@@ -475,7 +481,8 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   for (int t = 0; t < i; ++t) sg /= f;
   uint32_t pc[4] = {(uint32_t)step, (uint32_t)cid, (uint32_t)kPurposeComponent, 0u};
   philox4x32_10(pc, (uint32_t)seed, (uint32_t)(seed >> 32));
-  const bool use_net = O != nullptr && u01(pc[0]) < p_net;
+  const bool drift = O != nullptr || G != nullptr;  // network or gradient-history drift
+  const bool use_net = drift && u01(pc[0]) < p_net;
   // Per-shell steps draw their noise (and a network step its side) from a stream keyed
   // by the launch, not the step: the speculative candidates of one launch are
   // re-proposed at the same step numbers by the next, and the gradient-history inputs
@@ -489,9 +496,19 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
   const double a = u01(pa[0]) < 0.5 ? -1.0 : 1.0;  // side of the network's two-sided drift
   const double ls = log(sg);
   double smean[3] = {0, 0, 0}, df = 0.0;
-  if (O) {
-    for (int k = threadIdx.x; k < K; k += blockDim.x)
-      mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hu[k], hs[k]);
+  if (drift) {
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      if (O) {
+        mlp_head(O + ((size_t)blockIdx.x * K + k) * kMlpOutPad, hu[k], hs[k]);
+      } else {
+        // newest gradient estimate of shell k (history slot 0), isotropic scales
+        const float* g = G + ((size_t)cid * kMlpGHist * K + k) * 3;
+        for (int d = 0; d < 3; ++d) {
+          hu[k][d] = isfinite(g[d]) ? (double)g[d] : 0.0;
+          hs[k][d] = 0.0;
+        }
+      }
+    }
     __syncthreads();
     shell_scale_mean(hs, K, smean);
     df = shell_drift_factor(hu, K);
@@ -501,14 +518,14 @@ __global__ void __launch_bounds__(128) k_propose_shell(const double2* __restrict
     double z[4];
     normals4(seed, launch, cid, pnet_i, k, z);
     double mu[3] = {0, 0, 0}, s[3] = {ls, ls, ls}, v[3], w[3];
-    if (O) shell_params(hu[k], hs[k], smean, sg, df, ls, mu, s);
+    if (drift) shell_params(hu[k], hs[k], smean, sg, df, ls, mu, s);
     for (int d = 0; d < 3; ++d) {
       v[d] = use_net ? a * mu[d] + exp(s[d]) * z[d] : sg * z[d];
       w[d] = use_net ? z[d] * exp(ls - s[d]) : z[d];
     }
     const double si[3] = {ls, ls, ls}, zero[3] = {0, 0, 0};
     liso += rot_logdens(v, zero, si);
-    if (O) {
+    if (drift) {
       const double mneg[3] = {-mu[0], -mu[1], -mu[2]};
       lp += rot_logdens(v, mu, s);
       lm += rot_logdens(v, mneg, s);
@@ -738,7 +755,9 @@ int chains_enqueue(tp3_chains* h) {
       if (int r = tp3::mlp_forward_raw(h->net, n * h->K, &O)) return r;
     }
     k_propose_shell<<<n, 128, 0, c->stream>>>(h->d_state, h->d_cand, h->d_cs, h->d_sigma, h->nl, h->B, h->K, h->LMAX,
-                                              h->L, h->f, h->seed, O, h->p_net, h->d_v, h->d_w, h->d_comp, h->d_lq,
+                                              h->L, h->f, h->seed, O,
+                                              h->kind == TP3_MOVE_DRIFT ? h->d_ghist : nullptr, h->p_net, h->d_v,
+                                              h->d_w, h->d_comp, h->d_lq,
                                               c->d_delta,
                                               c->d_doff, mlog ? h->d_lv : nullptr, lctr, h->mlog_cap, h->nch,
                                               h->d_rag);
@@ -1056,7 +1075,8 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
   if (!h) return TP3_ERR_ARG;
   tp3_ctx* c = h->ctx;
   if (int r = tp3::ctx_check(c)) return r;
-  if (kind != TP3_MOVE_REFERENCE && kind != TP3_MOVE_SHELL_SO3 && kind != TP3_MOVE_LEARNED)
+  if (kind != TP3_MOVE_REFERENCE && kind != TP3_MOVE_SHELL_SO3 && kind != TP3_MOVE_LEARNED &&
+      kind != TP3_MOVE_DRIFT)
     return tp3::ctx_fail(c, TP3_ERR_ARG, "unknown move kind");
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "set move sync");
@@ -1084,8 +1104,10 @@ int tp3_chains_set_move(tp3_chains* h, int kind, double sigma0, double p_net, tp
     if (tp3::mlp_max_rows(net) < h->nch * h->B * h->K)
       return tp3::ctx_fail(c, TP3_ERR_ARG, "network max_rows < chains x candidates x shells");
   }
+  if (kind == TP3_MOVE_DRIFT && !(p_net > 0.0 && p_net <= 1.0))
+    return tp3::ctx_fail(c, TP3_ERR_ARG, "p_net must be in (0, 1]");
   h->kind = kind;
-  h->p_net = kind == TP3_MOVE_LEARNED ? p_net : 0.0;
+  h->p_net = (kind == TP3_MOVE_LEARNED || kind == TP3_MOVE_DRIFT) ? p_net : 0.0;
   h->net = kind == TP3_MOVE_LEARNED ? net : nullptr;
   h->xs = tp3::mlp_n_in_pad(h->L);
   h->dirty = true;

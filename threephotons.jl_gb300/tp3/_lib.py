@@ -34,6 +34,7 @@ TP3_MODE_AUTO = -1
 TP3_MOVE_REFERENCE = 0
 TP3_MOVE_SHELL_SO3 = 1
 TP3_MOVE_LEARNED = 2
+TP3_MOVE_DRIFT = 3
 
 # name -> (restype, argtypes); every symbol include/tp3.h declares
 SIGNATURES = {

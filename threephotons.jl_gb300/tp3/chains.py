@@ -118,7 +118,8 @@ class Chains:
     def set_move(self, kind: int, sigma0: float = 0.1, p_net: float = 0.0, net=None) -> None:
         """Move kind: 0 reference get_MC_step, 1 per-shell isotropic SO(3) step with
         sigma0 (radians), 2 mixture of the network's step (probability p_net) and the
-        isotropic one, Metropolis-Hastings corrected."""
+        isotropic one, Metropolis-Hastings corrected, 3 the same mixture with the drift
+        along the newest gradient estimate instead of a network (symmetric proposal)."""
         check(self._lib.tp3_chains_set_move(self._h, kind, float(sigma0), float(p_net),
                                             net.handle if net is not None else None), self.basis.ctx)
 

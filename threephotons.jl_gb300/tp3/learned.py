@@ -242,7 +242,7 @@ def learned_vs_plain(basis, base: np.ndarray, nchains: int = 64, ncand: int = 16
                      train_steps: int = 1500, batch_candidates: int = 1024, eval_launches: int = 300,
                      sigma0: float = 0.2, stepsizefactor: float = 1.02, temperature_decay: float = 0.9995,
                      temperature_factor: float = 0.1, p_net: float = 0.8, hidden: int = 512, lr: float = 1e-3,
-                     seed: int = 2024, chunk: int = 10) -> dict:
+                     seed: int = 2024, chunk: int = 10, drift: bool = True) -> dict:
     """The learned-proposal experiment on the basis's histogram (set beforehand):
     1. the plain annealer (isotropic per-shell steps) logs its moves from Haar-rotated
        starts (collect_launches x nchains x ncand candidates);
@@ -251,7 +251,10 @@ def learned_vs_plain(basis, base: np.ndarray, nchains: int = 64, ncand: int = 16
     3. from fresh starts (another seed), the plain annealer runs eval_launches launches;
        its final median energy is the target;
     4. the learned annealer (mixture p_net network / isotropic, MH-corrected) runs from
-       the same starts with the same schedule until its median energy reaches the target.
+       the same starts with the same schedule until its median energy reaches the target;
+    5. (drift=True) the network-free drift annealer (the same mixture with the drift along
+       the newest gradient estimate, TP3_MOVE_DRIFT) does the same: the ablation that
+       shows what the trained network adds over its strongest input.
     Times are wall clock around graph replays (chunks of `chunk` launches)."""
     import time
     from .chains import Chains
@@ -299,6 +302,18 @@ def learned_vs_plain(basis, base: np.ndarray, nchains: int = 64, ncand: int = 16
     stl = lrn.state()
     lrn.close()
     net.close()
+    if drift:
+        # 5. drift-only ablation: same starts, schedule, seed and mixture weight
+        dr = Chains(basis, ev_starts, T0, 0.1, stepsizefactor, temperature_decay, seed + 11, ncand=ncand)
+        dr.set_move(3, sigma0, p_net)
+        dr.run(1)
+        sec_d, n_d, med_d, trace_d = time_to_energy(dr, target, eval_launches - 1, chunk)
+        std = dr.state()
+        dr.close()
+        out["drift"] = {"seconds_to_target": sec_d, "launches": n_d + 1, "median_E": med_d,
+                        "reached": bool(med_d <= target),
+                        "accept_rate": float(std["accepted"].sum() / max(std["steps"].sum(), 1)), "trace": trace_d}
+        out["time_ratio_drift"] = sec_d / sec_p if med_d <= target else None
     out["plain"] = {"seconds": sec_p, "launches": n_p + 1, "final_median_E": med_p,
                     "accept_rate": float(stp["accepted"].sum() / max(stp["steps"].sum(), 1)), "trace": trace_p}
     out["learned"] = {"seconds_to_target": sec_l, "launches": n_l + 1, "median_E": med_l,
