@@ -314,6 +314,20 @@ int tp3_histogram_pictures(tp3_ctx* ctx, int n_pictures, const void* d_photons, 
 int tp3_sample_pictures(tp3_ctx* ctx, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX, int LMAX,
                         double dq, double qcut, double envelope_sigma, int incident_photons, double lambda,
                         double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts);
+/* pointsPerOrientation with the rest of generateHistogram's picture model
+ * (src/datagen.jl:88-113, 397-405): as tp3_sample_pictures, plus
+ *   incident_photon_variance > 0: the picture's incident photons are
+ *     round(N(incident_photons, incident_photon_variance)) (the reference passes it as
+ *     the standard deviation of its Normal), clamped to 0 .. 2^24;
+ *   beamstop_width > 0: incident photons with |x| <= beamstop_width or
+ *     |y| <= beamstop_width are dropped before the qcut test;
+ *   stream (0..15): independent photon draws for the same pictures and orientations
+ *     (0 molecule; GaussianNoise photons are a second call with stream 1, the noise
+ *     intensity and the envelope width noise.sigma * 1.05). */
+int tp3_sample_pictures_ex(tp3_ctx* ctx, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX,
+                           int LMAX, double dq, double qcut, double envelope_sigma, int incident_photons,
+                           int incident_photon_variance, double beamstop_width, int stream, double lambda,
+                           double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts);
 /* Largest intensity on the shells x (n_theta x n_phi) grid (the maximum the
  * rejection sampling is normalised by).  Synchronises. */
 int tp3_intensity_max(tp3_ctx* ctx, const void* d_coeff, int KMAX, int LMAX, double dq, int n_theta, int n_phi,

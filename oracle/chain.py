@@ -88,6 +88,54 @@ def propose(coeff: np.ndarray, L: int, LMAX: int, sigma: dict, seed: int, step: 
     return out
 
 
+class SequentialChain:
+    """The chain of run_chain advanced one step at a time (rotate_all_at_once /
+    evaluate_step, src/determination.jl:281-338, 491-515): peek() proposes the next
+    candidate and evaluates its energy change and natural Metropolis decision; commit(acc)
+    takes a decision, so a comparison can make the oracle follow a device chain through a
+    decision that lies within the energy tolerance of its boundary."""
+
+    def __init__(self, energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, initial_stepsize: float,
+                 stepsizefactor: float, temperature_decay: float, seed: int, chain: int):
+        self.energy_fn, self.L, self.LMAX = energy_fn, L, LMAX
+        self.f, self.decay, self.seed, self.chain = stepsizefactor, temperature_decay, seed, chain
+        self.state = coeff0.copy()
+        self.E = energy_fn(self.state)
+        self.T = T0
+        self.sigma = {l: initial_stepsize * (l - 1) for l in range(2, L + 1, 2)}
+        self.s = 0
+        self._pending = None
+
+    def peek(self) -> dict:
+        T = self.T * self.decay
+        cand = propose(self.state, self.L, self.LMAX, self.sigma, self.seed, self.s, self.chain)
+        En = self.energy_fn(cand)
+        dE = En - self.E
+        ap = math.exp(-dE / T) if -dE / T < 700 else float("inf")
+        u = u01(philox4x32_10((self.s & M32, self.chain, 2, 0), _key(self.seed))[0])
+        acc = dE < 0.0 or (dE > 0.0 and u < ap)
+        self._pending = dict(cand=cand, En=En, dE=dE, T=T, ap=ap, u=u, acc=acc)
+        return self._pending
+
+    def commit(self, acc: bool) -> list:
+        p = self._pending
+        self._pending = None
+        self.T = p["T"]
+        sign = 0.0
+        if acc:
+            sign = 1.0 if p["dE"] < 0.0 else -1.0
+            for l in self.sigma:
+                self.sigma[l] *= self.f
+            self.E = p["En"]
+            self.state = p["cand"]
+        else:
+            for l in self.sigma:
+                self.sigma[l] /= self.f
+        self.s += 1
+        return [self.s, sign, p["En"], self.E, p["dE"], p["T"], p["ap"],
+                self.sigma[max(self.sigma)] if self.sigma else 0.0]
+
+
 def run_chain(energy_fn, coeff0: np.ndarray, L: int, LMAX: int, T0: float, initial_stepsize: float,
               stepsizefactor: float, temperature_decay: float, seed: int, chain: int, nsteps: int):
     """Sequential chain; returns (final coeff, E, T, sigma, log rows [step, sign, E_new, E, dE, T, ap, sigma_L])."""

@@ -37,6 +37,7 @@ namespace {
 
 constexpr int kMaxPhotons = 1536;  // photons per picture after the k filter (43 KB of shared memory)
 constexpr int kBinThreads = 256;
+constexpr int kMaxIncident = 1 << 24;  // incident photons of one picture
 
 __device__ inline double angle_between(double x1, double y1, double x2, double y2, double n1, double n2) {
   const double dot = __dadd_rn(__dmul_rn(x1, x2), __dmul_rn(y1, y2));
@@ -197,14 +198,22 @@ __device__ inline double intensity_at(const double2* __restrict__ coeff, int KMA
 }
 
 // grid: pictures; block 256.  Accepted photons go to out[pic][0 .. counts[pic]) ((x, y)).
+// incident_var > 0: the picture's incident photons are round(N(incident, incident_var))
+// (>= 0, <= kMaxIncident) instead of `incident` (src/datagen.jl:93-97).  beamstop > 0:
+// incident photons with |x| <= beamstop or |y| <= beamstop are dropped
+// (src/datagen.jl:111-113).  stream selects independent photon draws for the same
+// pictures (the same orientation R): 0 for the molecule, 1 for noise photons
+// (src/datagen.jl:403-405 samples the noise with the molecule's rotation).
 __global__ void __launch_bounds__(256) k_sample_pictures(const double2* __restrict__ coeff, int KMAX, int LMAX,
                                                          double dq, double qcut, double sigma, int incident,
+                                                         int incident_var, double beamstop, int stream,
                                                          double lambda, double Imax, uint64_t seed, int max_out,
                                                          double2* __restrict__ out, int* __restrict__ counts,
                                                          long long pic0) {
   __shared__ double R[9];
-  __shared__ int s_n;
+  __shared__ int s_n, s_incident;
   const long long pic = pic0 + blockIdx.x;
+  const uint32_t pur = 16u * (uint32_t)stream;  // purposes of this stream's photon draws
   if (threadIdx.x == 0) {
     // Haar rotation from a uniform unit quaternion
     double z[4];
@@ -215,13 +224,23 @@ __global__ void __launch_bounds__(256) k_sample_pictures(const double2* __restri
     R[3] = 2 * (b * c + a * d);         R[4] = a * a - b * b + c * c - d * d; R[5] = 2 * (c * d - a * b);
     R[6] = 2 * (b * d - a * c);         R[7] = 2 * (c * d + a * b);         R[8] = a * a - b * b - c * c + d * d;
     s_n = 0;
+    int n = incident;
+    if (incident_var > 0) {
+      double zc[4];
+      normal4(seed, (uint32_t)pic, 0xFFFFFFFEu, 10u + pur, zc);
+      const double v = rint((double)incident + (double)incident_var * zc[0]);
+      n = v < 0.0 ? 0 : (v > (double)kMaxIncident ? kMaxIncident : (int)v);
+    }
+    s_incident = n;
   }
   __syncthreads();
   const double inv2s2 = 0.5 / (sigma * sigma);
-  for (int i = threadIdx.x; i < incident; i += blockDim.x) {
+  const int n_inc = s_incident;
+  for (int i = threadIdx.x; i < n_inc; i += blockDim.x) {
     double z[4];
-    normal4(seed, (uint32_t)pic, (uint32_t)i, 8u, z);
+    normal4(seed, (uint32_t)pic, (uint32_t)i, 8u + pur, z);
     const double px = sigma * z[0], py = sigma * z[1];
+    if (beamstop > 0.0 && !(fabs(px) > beamstop && fabs(py) > beamstop)) continue;
     const double qn = sqrt(px * px + py * py);
     if (qn > qcut) continue;
     // detector_to_Ewald_sphere: theta = acos(q lambda / 4 pi), (sin(theta) p, cos(theta) q)
@@ -233,7 +252,7 @@ __global__ void __launch_bounds__(256) k_sample_pictures(const double2* __restri
     const double I = intensity_at(coeff, KMAX, LMAX, dq, rx, ry, rz);
     const double r2 = rx * rx + ry * ry + rz * rz;
     const double ratio = I / Imax * exp(r2 * inv2s2);
-    uint32_t c[4] = {(uint32_t)pic, (uint32_t)i, 9u, 0u};
+    uint32_t c[4] = {(uint32_t)pic, (uint32_t)i, 9u + pur, 0u};
     philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
     if (u01(c[0]) < ratio) {
       const int slot = atomicAdd(&s_n, 1);
@@ -287,20 +306,31 @@ int tp3_histogram_pictures(tp3_ctx* c, int n_pictures, const void* d_photons, in
   return TP3_OK;
 }
 
-int tp3_sample_pictures(tp3_ctx* c, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX, int LMAX,
-                        double dq, double qcut, double envelope_sigma, int incident_photons, double lambda,
-                        double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts) {
+int tp3_sample_pictures_ex(tp3_ctx* c, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX,
+                           int LMAX, double dq, double qcut, double envelope_sigma, int incident_photons,
+                           int incident_photon_variance, double beamstop_width, int stream, double lambda,
+                           double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts) {
   if (int r = tp3::ctx_check(c)) return r;
   if (n_pictures < 1 || !d_coeff || !d_photons || !d_counts || KMAX < 1 || LMAX < 1 || !(dq > 0.0) ||
-      !(qcut > 0.0) || !(envelope_sigma > 0.0) || incident_photons < 0 || !(max_intensity > 0.0) || max_out < 1 ||
-      !(lambda >= 0.0) || qcut * lambda > 4.0 * 3.141592653589793)
+      !(qcut > 0.0) || !(envelope_sigma > 0.0) || incident_photons < 0 || incident_photons > kMaxIncident ||
+      incident_photon_variance < 0 || !(beamstop_width >= 0.0) || stream < 0 || stream > 15 ||
+      !(max_intensity > 0.0) || max_out < 1 || !(lambda >= 0.0) || qcut * lambda > 4.0 * 3.141592653589793)
     return tp3::ctx_fail(c, TP3_ERR_ARG, "bad sampling arguments");
   k_sample_pictures<<<n_pictures, 256, 0, c->stream>>>((const double2*)d_coeff, KMAX, LMAX, dq, qcut, envelope_sigma,
-                                                       incident_photons, lambda, max_intensity, seed, max_out,
+                                                       incident_photons, incident_photon_variance, beamstop_width,
+                                                       stream, lambda, max_intensity, seed, max_out,
                                                        (double2*)d_photons, d_counts, (long long)first_picture);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "sample pictures");
   return TP3_OK;
+}
+
+int tp3_sample_pictures(tp3_ctx* c, int n_pictures, int64_t first_picture, const void* d_coeff, int KMAX, int LMAX,
+                        double dq, double qcut, double envelope_sigma, int incident_photons, double lambda,
+                        double max_intensity, uint64_t seed, int max_out, void* d_photons, int* d_counts) {
+  return tp3_sample_pictures_ex(c, n_pictures, first_picture, d_coeff, KMAX, LMAX, dq, qcut, envelope_sigma,
+                                incident_photons, 0, 0.0, 0, lambda, max_intensity, seed, max_out, d_photons,
+                                d_counts);
 }
 
 int tp3_intensity_max(tp3_ctx* c, const void* d_coeff, int KMAX, int LMAX, double dq, int n_theta, int n_phi,

@@ -84,6 +84,9 @@ SIGNATURES = {
                                        c_void_p, c_void_p, c_void_p]),
     "tp3_sample_pictures": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_int, c_int, c_double, c_double, c_double,
                                     c_int, c_double, c_double, ctypes.c_uint64, c_int, c_void_p, c_void_p]),
+    "tp3_sample_pictures_ex": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_int, c_int, c_double, c_double,
+                                       c_double, c_int, c_int, c_double, c_int, c_double, c_double, ctypes.c_uint64,
+                                       c_int, c_void_p, c_void_p]),
     "tp3_intensity_max": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_int, c_int, P(c_double)]),
     "tp3_wigner_D": (c_int, [c_int, c_double, c_double, c_double, c_void_p]),
     "tp3_rotate_shells_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
