@@ -48,6 +48,22 @@ __device__ __forceinline__ void fold_store_split(void* hi, void* lo, size_t i, f
   }
 }
 
+// Asynchronous global -> shared copies (cp.async): every copy of a staging step is in
+// flight at once and one wait covers them.  live = false writes zeros (no bytes read).
+__device__ __forceinline__ void fold_cp8(void* dst, const void* src, bool live) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src)), "r"(live ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void fold_cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void fold_cp_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // D row of order s inside a chunk starting at s_lo: rows of the orders before s,
 // (l3 + 1) per order for real functions (m3 = 0..l3), (2 l3 + 1) otherwise.
 __device__ __forceinline__ int fold_drow(int s, int s_lo, int l3min, bool sym) {
@@ -101,7 +117,9 @@ __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2
     if (s >= s_lo && s < s_hi) {
       const int l3 = l3min + 2 * s;
       const int r = fold_drow(s, s_lo, l3min, sym);
-      if (s >= s0a) Dw[(r + (sym ? m3a : m3a + l3)) * ps + slot] = make_float2(ar0[j], ai0[j]);
+      // real functions: T = 2 sum_{m3 >= 0} Re(D c) with the m3 = 0 term halved here
+      const float h = (sym && m3a == 0) ? 0.5f : 1.f;
+      if (s >= s0a) Dw[(r + (sym ? m3a : m3a + l3)) * ps + slot] = make_float2(h * ar0[j], h * ai0[j]);
       if (s >= s0b) Dw[(r + (sym ? m3b : m3b + l3)) * ps + slot] = make_float2(ar1[j], ai1[j]);
     }
   }
@@ -218,21 +236,19 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
       const int k = k0 + lane;
       const bool live = k < Kp;
       const float2* sk = src + (size_t)(live ? k : 0) * nc;
-#pragma unroll 4
-      for (int m = warp; m < n1r; m += NW) C1[m * ps + k] = live ? sk[o1 + m] : make_float2(0.f, 0.f);
+      for (int m = warp; m < n1r; m += NW) fold_cp8(&C1[m * ps + k], sk + o1 + m, live);
       // C2 has a zero row at each end: the union m1 range of an m3 pair reaches one row
       // past either end, where the pair's 3j value is zero
-#pragma unroll 4
       for (int m = warp; m < n2r + 2; m += NW)
-        C2[m * ps + k] = (live && m >= 1 && m <= n2r) ? sk[o2 + m - 1] : make_float2(0.f, 0.f);
+        fold_cp8(&C2[m * ps + k], sk + o2 + (m >= 1 && m <= n2r ? m - 1 : 0), live && m >= 1 && m <= n2r);
     }
     const int wn = (sym ? fb.wsym : fb.wall) / 4;
     const float4* w4 = reinterpret_cast<const float4*>(wtab + fb.w0);
     float4* s4 = reinterpret_cast<float4*>(W);
-#pragma unroll 4
-    for (int i = threadIdx.x; i < wn; i += NW * 32) s4[i] = w4[i];
+    for (int i = threadIdx.x; i < wn; i += NW * 32) fold_cp16(&s4[i], &w4[i]);
     const int nr = sym ? fb.npair_sym : fb.npair_all;
     for (int i = threadIdx.x; i < nr; i += NW * 32) s_rows[i] = rows[fb.row0 + i];
+    fold_cp_wait();
   }
   const int nch = sym ? fb.nch_sym : fb.nch_gen;
   if (threadIdx.x < kFoldMaxChunks) s_next[threadIdx.x] = 0;
@@ -251,8 +267,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const int s_lo = chk.x, s_hi = chk.y;
     const int l3top = l3min + 2 * (s_hi - 1);
     __syncthreads();  // the previous chunk's cT reads are done; C1 / C2 / W are staged
-    // cT rows of this chunk: c_k3[l3][m3] (m3 = 0 halved for real functions, whose T is
-    // twice the sum over m3 >= 0)
+    // cT rows of this chunk: c_k3[l3][m3] (m3 >= 0 for real functions)
     {
       int r0 = 0;
       for (int s = s_lo; s < s_hi; ++s) {
@@ -263,15 +278,11 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           const int k = k0 + lane;
           const bool live = k < Kp;
           const float2* sk = src + (size_t)(live ? k : 0) * nc + o3;
-#pragma unroll 4
-          for (int r = warp; r < cnt; r += NW) {
-            float2 v = live ? sk[r] : make_float2(0.f, 0.f);
-            if (sym && r == 0) { v.x *= 0.5f; v.y *= 0.5f; }
-            cT[(r0 + r) * ps + k] = v;
-          }
+          for (int r = warp; r < cnt; r += NW) fold_cp8(&cT[(r0 + r) * ps + k], sk + r, live);
         }
         r0 += cnt;
       }
+      fold_cp_wait();
     }
     __syncthreads();
     for (;;) {
