@@ -5,6 +5,7 @@
     python bench.py --workload ragged      # 64 chains x 16 candidates, K in 16..26, L in 12..18, own histograms
     python bench.py --workload learned     # learned vs plain annealer: time to the plain final energy
     python bench.py --no-ragged --no-learned   # the proposal line without the two extra legs
+    python bench.py --workload chains      # 64 chains x 16 candidates per CUDA-graph replay
 
 --mode tuned (and auto) runs the evaluation-variant autotuner first and benchmarks its
 choice; plain / tc / tf32 force the plain FP32, BF16 hi/lo x3 or TF32 hi/lo x3 path.
@@ -434,6 +435,52 @@ def run_learned(args):
     return 0
 
 
+def run_chains(args):
+    """--workload chains: 64 chains x 16 candidates per CUDA-graph replay on the L18 K26
+    N32 workload; CUDA-event time of --steps replays on the launch stream."""
+    import torch
+    import tp3
+    from tp3.chains import Chains
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    base = molecule_coefficients()
+    basis = tp3.calculate_basis(L, LMAX, N, K)
+    basis.set_histogram(build_histogram(basis, base))
+    if args.mode in ("auto", "tuned"):
+        basis.autotune(64)
+    else:
+        basis.set_mode({"plain": tp3.TP3_MODE_PLAIN_FP32, "tc": tp3.TP3_MODE_TC_BF16X3,
+                        "tf32": tp3.TP3_MODE_TC_TF32X3}[args.mode])
+        if args.coupling >= 0:
+            basis.set_coupling(args.coupling)
+    nch, ncand = 64, 16
+    ch = Chains(basis, np.repeat(base[None, :K], nch, axis=0), 5.0, math.pi / 4, 1.02, 0.99998, 12345 + rank,
+                ncand=ncand)
+    ch.run(max(3, args.warmup))
+    stream = torch.cuda.Stream()
+    basis.set_stream(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ch.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    basis.set_stream(None)
+    line = {"metric": "chain launches: proposals/s, 64 chains x 16 candidates per CUDA-graph replay, L18 K26 N32",
+            "value": whole_job_rate(ws, nch * ncand, args.steps, ms), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES.get(basis.mode, "fp32"), "data": "synthetic",
+            "config": {"workload": "64 chains x 16 speculative candidates (reference move) per graph replay",
+                       "mode": MODE_NAMES.get(basis.mode)}, "gpu_launches": 7 * args.steps}
+    ch.close()
+    basis.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,7 +489,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--mode", default="auto", choices=["auto", "tuned", "plain", "tc", "tf32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned"])
+    ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned", "chains"])
     ap.add_argument("--coupling", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6],
                     help="force a tensor-core coupling form (with --mode tc/tf32)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -456,6 +503,8 @@ def main():
         return run_ragged(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "chains":
+        return run_chains(args)
     args.warmup = max(args.warmup, 3)
 
     import torch
