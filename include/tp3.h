@@ -104,14 +104,16 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * two CTAs share an SM; 3: warp-local one-kernel coupling, warps taking (k1, k2-quad)
  * units from a counter with no CTA barrier, 512 threads; 4: the warp-local coupling
  * with 256 threads, two CTAs per SM in 110 KB each where that fits, else one with up
- * to 225 KB; 1: two-kernel split coupling through
- * global memory) -- selects
+ * to 225 KB; 1: two-kernel split coupling through global memory; 5, 6, 7: folded-row
+ * coupling, warps owning folded pairs of k1 rows, at 8, 7 and 13 warps per CTA with the
+ * largest per-warp D buffer that fits 225 KB; in BF16 mode it writes T order-major and
+ * the angular kernel reads it MN-major) -- selects
  * the fastest for this context and records it for the shape (L, LMAX, N, K, lambda,
  * dq) in the process, where TP3_MODE_AUTO finds it.  report (nullable): up to *nreport
  * rows of (mode, coupling form, ms per proposal); *nreport returns the number of
  * variants.  Synchronises. */
 int tp3_autotune(tp3_ctx* ctx, int n, double* report, int* nreport);
-/* Force a coupling form of the tensor-core path (0 to 4 as above). */
+/* Force a coupling form of the tensor-core path (0 to 7 as above). */
 int tp3_set_coupling(tp3_ctx* ctx, int form);
 /* Pre-size scratch for batches of up to n proposals (otherwise sized on first use). */
 int tp3_reserve(tp3_ctx* ctx, int n);

@@ -373,9 +373,9 @@ std::string setup_tc(tp3_ctx* c) {
       (e = upload(c, Fhi32, &tc.Fhi32)) != cudaSuccess || (e = upload(c, Flo32, &tc.Flo32)) != cudaSuccess ||
       (e = tp3::tc_configure()) != cudaSuccess)
     return std::string("tensor-core table upload: ") + cudaGetErrorString(e);
-  // folded-row coupling: two tilings (8 warps and 7 warps in up to 225 KB, one CTA per SM;
-  // 7 warps take a K = 26 proposal's 13 folded units in two rounds with one warp idle),
-  // each with the largest per-warp D buffer that fits
+  // folded-row coupling: three tilings in up to 225 KB, one CTA per SM (8 warps; 7 warps,
+  // which take a K = 26 proposal's 13 folded units in two rounds with one warp idle; 13
+  // warps, one round, with smaller D buffers), each with the largest D buffer that fits
   if ((e = tp3::fold_configure()) != cudaSuccess) return std::string("fold coupling: ") + cudaGetErrorString(e);
   {
     int rows_gen = 0;  // D rows of the largest block, general path (all l3 in one chunk)
@@ -385,9 +385,10 @@ std::string setup_tc(tp3_ctx* c) {
       rows_gen = std::max(rows_gen, r);
     }
     const int ps = (b.K + 5 + 31) / 32 * 32;
-    const struct { int nw; size_t budget; } fvs[2] = {{8, (size_t)tp3::kCoupleMaxDynSmem},
-                                                      {7, (size_t)tp3::kCoupleMaxDynSmem}};
-    for (int v = 0; v < 2; ++v) {
+    const struct { int nw; size_t budget; } fvs[3] = {{8, (size_t)tp3::kCoupleMaxDynSmem},
+                                                      {7, (size_t)tp3::kCoupleMaxDynSmem},
+                                                      {13, (size_t)tp3::kCoupleMaxDynSmem}};
+    for (int v = 0; v < 3; ++v) {
       tp3::FoldVariant& fv = tc.fold[v];
       std::vector<tp3::FoldBlock> fbl;
       std::vector<tp3::FoldRow> frows;
@@ -612,7 +613,8 @@ int check_ctx(tp3_ctx* c) {
 // form this shape cannot run falls back to one that it can.
 void apply_coupling(tp3_ctx* c, int form) {
   TcTables& tc = c->tc;
-  tc.use_fold = (form == 5 && tc.fold[0].ok) ? 0 : (form == 6 && tc.fold[1].ok) ? 1 : -1;
+  tc.use_fold = (form == 5 && tc.fold[0].ok) ? 0 : (form == 6 && tc.fold[1].ok) ? 1
+                 : (form == 7 && tc.fold[2].ok) ? 2 : -1;
   tc.use_small = form == 2 && tc.small_ok;
   tc.use_warp = form == 3 && tc.warp_ok;
   tc.use_warp2 = form == 4 && tc.warp2_ok;
@@ -938,6 +940,7 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
       if (c->tc.split_ok) vars.push_back({m, 1});
       if (c->tc.fold[0].ok) vars.push_back({m, 5});
       if (c->tc.fold[1].ok) vars.push_back({m, 6});
+      if (c->tc.fold[2].ok) vars.push_back({m, 7});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
   const size_t nco = (size_t)b.K * b.LMAX * b.LMAX;
@@ -1043,8 +1046,8 @@ int tp3_set_coupling(tp3_ctx* c, int form) {
   if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
   const bool ok = (form == 0 && c->tc.fused_ok) || (form == 1 && c->tc.split_ok) || (form == 2 && c->tc.small_ok) ||
                   (form == 3 && c->tc.warp_ok) || (form == 4 && c->tc.warp2_ok) || (form == 5 && c->tc.fold[0].ok) ||
-                  (form == 6 && c->tc.fold[1].ok);
-  if (!ok) return fail(c, form < 0 || form > 6 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
+                  (form == 6 && c->tc.fold[1].ok) || (form == 7 && c->tc.fold[2].ok);
+  if (!ok) return fail(c, form < 0 || form > 7 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
   apply_coupling(c, form);
   return TP3_OK;
 }

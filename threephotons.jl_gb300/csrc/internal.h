@@ -104,8 +104,9 @@ struct FoldVariant {
 
 // Device tables of the tensor-core path.
 struct TcTables {
-  // folded-row coupling: [0] 8 warps, [1] 7 warps, one CTA per SM
-  FoldVariant fold[2];
+  // folded-row coupling tilings: [0] 8 warps, [1] 7 warps, [2] 13 warps (smaller D
+  // buffers, more l3 chunks), one CTA per SM
+  FoldVariant fold[3];
   int use_fold = -1;
   int n_pb = 0, maxs = 0, SDmax = 0;
   int ncp = 0, SDp = 0, pmax = 0, nchunks = 0, wsmem = 0;  // coupling kernel shared-memory layout

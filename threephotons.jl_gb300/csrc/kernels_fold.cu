@@ -532,7 +532,8 @@ cudaError_t fold_configure() {
   cudaError_t e;
   const int cs = kCoupleMaxDynSmem;
   if ((e = cudaFuncSetAttribute(k_couple_fold<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
+      (e = cudaFuncSetAttribute(k_couple_fold<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<13>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
     return e;
   return cudaSuccess;
 }
@@ -549,6 +550,7 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
   switch (fv.nw) {
     case 7: TP3_FOLD_LAUNCH(7); break;
     case 8: TP3_FOLD_LAUNCH(8); break;
+    case 13: TP3_FOLD_LAUNCH(13); break;
     default: return cudaErrorInvalidValue;
   }
 #undef TP3_FOLD_LAUNCH

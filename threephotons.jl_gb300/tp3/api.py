@@ -150,14 +150,15 @@ class BasisTypeGB300:
 
     def set_coupling(self, form: int) -> None:
         """Tensor-core coupling form: 0 one-kernel, 1 split, 2 one-kernel on 256 threads, 3 warp-local,
-        4 warp-local on 256 threads (two CTAs per SM)."""
+        4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7 folded-row at 8 / 7 / 13 warps."""
         check(self._lib.tp3_set_coupling(self._ctx, form), self._ctx)
 
     def autotune(self, n: int = 64) -> list:
         """Time every evaluation variant on n synthetic proposals, keep the fastest (also
         for later TP3_MODE_AUTO contexts of this shape); returns [(mode, coupling form, ms/proposal)]
         with coupling form 0 one-kernel, 1 split, 2 one-kernel on 256 threads (two CTAs per SM),
-        3 warp-local one-kernel, 4 warp-local on 256 threads (two CTAs per SM)."""
+        3 warp-local one-kernel, 4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7
+        folded-row at 8 / 7 / 13 warps."""
         cap = ctypes.c_int(16)
         rep = np.zeros(3 * 16)
         check(self._lib.tp3_autotune(self._ctx, n, rep.ctypes.data, ctypes.byref(cap)), self._ctx)
