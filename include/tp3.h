@@ -54,6 +54,7 @@ extern "C" {
 #define TP3_ERR_TIMEOUT 7        /* a bounded device wait ran out */
 #define TP3_ERR_UNSUPPORTED 8    /* mode not available for this (L, K, N, lambda) */
 #define TP3_ERR_ALLOC 9          /* device or host allocation failed */
+#define TP3_ERR_BOUNDS 10        /* a TP3_DEBUG build's device index check failed (access skipped) */
 
 /* Evaluation modes (tp3_set_mode). */
 #define TP3_MODE_PLAIN_FP32 0    /* direct coupling + FP32 SIMT angular contraction, full grid */

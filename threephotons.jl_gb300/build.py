@@ -4,7 +4,8 @@
 
 Compiles every translation unit of csrc/ in parallel with nvcc
 (-gencode arch=compute_103a,code=sm_103a) and links lib/libtp3.so with the
-static CUDA runtime.  Objects go to _build/ beside this file.  Rebuilds only
+static CUDA runtime.  TP3_DEBUG=1 (with --force) builds the device index checks in.
+Objects go to _build/ beside this file.  Rebuilds only
 when a source or header is newer than the library.
 """
 from __future__ import annotations
@@ -45,6 +46,8 @@ def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
            "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+    if os.environ.get("TP3_DEBUG"):
+        cmd.insert(1, "-DTP3_DEBUG")  # device index checks (see csrc/internal.h)
     if src.endswith(".cu"):
         cmd[1:1] = ["-Xptxas", "-v"] if os.environ.get("TP3_PTXAS_V") else []
     else:

@@ -595,8 +595,11 @@ int check_device_error(tp3_ctx* c) {
     const int code = *c->h_err;
     cudaMemset(c->d_err, 0, sizeof(int));
     return fail(c, code, code == TP3_ERR_TIMEOUT ? "a bounded device wait ran out; results of this call are invalid"
-                                                 : "a device-side argument check failed (ragged limits out of range); "
-                                                   "results of this call are invalid");
+                         : code == TP3_ERR_BOUNDS
+                             ? "a device index check of the TP3_DEBUG build failed (the access was skipped); results "
+                               "of this call are invalid"
+                             : "a device-side argument check failed (ragged limits out of range); "
+                               "results of this call are invalid");
   }
   return TP3_OK;
 }
@@ -704,6 +707,7 @@ const char* tp3_status_string(int s) {
     case TP3_ERR_TIMEOUT: return "device wait timed out";
     case TP3_ERR_UNSUPPORTED: return "unsupported mode or shape";
     case TP3_ERR_ALLOC: return "allocation failed";
+    case TP3_ERR_BOUNDS: return "device index check failed (TP3_DEBUG build)";
     default: return "unknown status";
   }
 }
@@ -870,6 +874,7 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
     tp3_ctx_destroy(c);
     return fail(nullptr, TP3_ERR_CUDA, msg);
   }
+  c->tc.err = c->d_err;  // device error flag of the TP3_DEBUG index checks
   c->tc_why = setup_tc(c);
   c->tc_ok = c->tc_why.empty();
   cudaGetLastError();

@@ -9,6 +9,21 @@
 
 namespace tp3 {
 
+// TP3_DEBUG builds (TP3_DEBUG=1 python threephotons.jl_gb300/build.py --force) check the
+// indices that the gather and folded-row coupling kernels compute before each shared- or
+// global-memory access; a failed check sets TP3_ERR_BOUNDS in the context's error flag
+// (reported by the next synchronising call) and skips the access.  Release builds
+// compile the checks out.
+#ifdef TP3_DEBUG
+__device__ __forceinline__ bool tp3_dcheck(bool ok, int* err) {
+  if (!ok && err) atomicExch(err, 10 /* TP3_ERR_BOUNDS */);
+  return ok;
+}
+#define TP3_DCHECK(cond, err) tp3_dcheck((cond), (err))
+#else
+#define TP3_DCHECK(cond, err) true
+#endif
+
 // Device view of the per-context tables (all pointers are device memory).
 struct DevTables {
   int K, nc, LMAX;
@@ -108,6 +123,7 @@ struct TcTables {
   // buffers, more l3 chunks), one CTA per SM
   FoldVariant fold[3];
   int use_fold = -1;
+  int* err = nullptr;  // the context's device error flag (index checks of TP3_DEBUG builds)
   int n_pb = 0, maxs = 0, SDmax = 0;
   int ncp = 0, SDp = 0, pmax = 0, nchunks = 0, wsmem = 0;  // coupling kernel shared-memory layout
   bool w_smem = false;

@@ -107,7 +107,7 @@ template <int NE>
 __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2, int dps, int ps, int n1,
                                               const float* w, int rs2, bool valid, int a, int s0a, int s0b,
                                               int s_hi, int s_lo, int l3min, int m3a, int m3b, bool sym, float2* Dw,
-                                              int slot) {
+                                              int slot, int drows, int* err) {
   float ar0[NE], ai0[NE], ar1[NE], ai1[NE];
   fold_p1<NE>(c1, c2, dps, ps, n1, w, rs2, ar0, ai0, ar1, ai1);
   if (!valid) return;
@@ -119,8 +119,11 @@ __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2
       const int r = fold_drow(s, s_lo, l3min, sym);
       // real functions: T = 2 sum_{m3 >= 0} Re(D c) with the m3 = 0 term halved here
       const float h = (sym && m3a == 0) ? 0.5f : 1.f;
-      if (s >= s0a) Dw[(r + (sym ? m3a : m3a + l3)) * ps + slot] = make_float2(h * ar0[j], h * ai0[j]);
-      if (s >= s0b) Dw[(r + (sym ? m3b : m3b + l3)) * ps + slot] = make_float2(ar1[j], ai1[j]);
+      const int ra = r + (sym ? m3a : m3a + l3), rb = r + (sym ? m3b : m3b + l3);
+      if (s >= s0a && TP3_DCHECK(ra >= 0 && ra < drows && slot < ps, err))
+        Dw[ra * ps + slot] = make_float2(h * ar0[j], h * ai0[j]);
+      if (s >= s0b && TP3_DCHECK(rb >= 0 && rb < drows && slot < ps, err))
+        Dw[rb * ps + slot] = make_float2(ar1[j], ai1[j]);
     }
   }
 }
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const FoldRow* __restrict__ rows, const float* __restrict__ wtab, const int2* __restrict__ chunks, int ps,
     int drows, int wmax, int cmax, int stage, int klp, int KP, const int* __restrict__ symflags,
     void* __restrict__ Thi, void* __restrict__ Tlo, bool tf32out, bool ltmaj, float* __restrict__ T32, int ldT32,
-    const RagInfo* __restrict__ rag) {
+    const RagInfo* __restrict__ rag, int* __restrict__ err) {
   extern __shared__ __align__(16) float smf[];
   __shared__ int s_next[kFoldMaxChunks];
   __shared__ FoldRow s_rows[kFoldMaxRows];
@@ -236,18 +239,22 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
       const int k = k0 + lane;
       const bool live = k < Kp;
       const float2* sk = src + (size_t)(live ? k : 0) * nc;
-      for (int m = warp; m < n1r; m += NW) fold_cp8(&C1[m * ps + k], sk + o1 + m, live);
+      for (int m = warp; m < n1r; m += NW)
+        if (TP3_DCHECK(m < cmax && o1 + m < nc, err)) fold_cp8(&C1[m * ps + k], sk + o1 + m, live);
       // C2 has a zero row at each end: the union m1 range of an m3 pair reaches one row
       // past either end, where the pair's 3j value is zero
       for (int m = warp; m < n2r + 2; m += NW)
-        fold_cp8(&C2[m * ps + k], sk + o2 + (m >= 1 && m <= n2r ? m - 1 : 0), live && m >= 1 && m <= n2r);
+        if (TP3_DCHECK(m < cmax + 2 && o2 + n2r - 1 < nc, err))
+          fold_cp8(&C2[m * ps + k], sk + o2 + (m >= 1 && m <= n2r ? m - 1 : 0), live && m >= 1 && m <= n2r);
     }
-    const int wn = (sym ? fb.wsym : fb.wall) / 4;
+    int wn = (sym ? fb.wsym : fb.wall) / 4;
+    if (!TP3_DCHECK(4 * wn <= wmax, err)) wn = 0;
     const float4* w4 = reinterpret_cast<const float4*>(wtab + fb.w0);
     float4* s4 = reinterpret_cast<float4*>(W);
     for (int i = threadIdx.x; i < wn; i += NW * 32) fold_cp16(&s4[i], &w4[i]);
     const int nr = sym ? fb.npair_sym : fb.npair_all;
-    for (int i = threadIdx.x; i < nr; i += NW * 32) s_rows[i] = rows[fb.row0 + i];
+    for (int i = threadIdx.x; i < nr; i += NW * 32)
+      if (TP3_DCHECK(i < kFoldMaxRows, err)) s_rows[i] = rows[fb.row0 + i];
     fold_cp_wait();
   }
   const int nch = sym ? fb.nch_sym : fb.nch_gen;
@@ -278,7 +285,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           const int k = k0 + lane;
           const bool live = k < Kp;
           const float2* sk = src + (size_t)(live ? k : 0) * nc + o3;
-          for (int r = warp; r < cnt; r += NW) fold_cp8(&cT[(r0 + r) * ps + k], sk + r, live);
+          for (int r = warp; r < cnt; r += NW)
+            if (TP3_DCHECK(r0 + r < drows && o3 + r < nc, err)) fold_cp8(&cT[(r0 + r) * ps + k], sk + r, live);
         }
         r0 += cnt;
       }
@@ -314,10 +322,20 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           const float2* c2 = C2 + (-m3a - fr.m1lo + l2 + 1) * ps + k2;
           const int dps = m3a >= 0 ? -ps : ps;
           const float* w = W + fr.wofs + 2 * (a - fr.c0);
+#ifdef TP3_DEBUG
+          {  // the m1 loop's first and last rows of c_k1, c_k2 (both m3) and 3j values
+            const int r1 = fr.m1lo + l1, r2 = -m3a - fr.m1lo + l2 + 1, d = dps / ps;
+            const int r2z = r2 - (fr.n1 - 1);
+            const bool ok = r1 >= 0 && r1 + fr.n1 - 1 <= 2 * l1 && r2 < cmax + 2 && r2z >= 0 && r2 + d < cmax + 2 &&
+                            r2z + d >= 0 && k1 < ps && k2 < ps && ne <= 16 &&
+                            fr.wofs + 2 * (a - fr.c0) + 2 * fr.rs * (fr.n1 - 1) + 2 * ne <= (sym ? fb.wsym : fb.wall);
+            if (!TP3_DCHECK(ok, err)) continue;
+          }
+#endif
 #define TP3_FOLD_P1(NE)                                                                                  \
   case NE:                                                                                               \
     fold_p1_store<NE>(c1, c2, dps, ps, fr.n1, w, 2 * fr.rs, valid, a, fr.s0a, fr.s0b, s_hi, s_lo, l3min, \
-                      m3a, m3b, sym, Dw, slot);                                                          \
+                      m3a, m3b, sym, Dw, slot, drows, err);                                              \
     break;
           switch (ne) {
             TP3_FOLD_P1(2) TP3_FOLD_P1(4) TP3_FOLD_P1(6) TP3_FOLD_P1(8)
@@ -350,6 +368,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
             if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; lbase = na; }
             int q2, q3;
             fold_tile_of(t, q2, q3);
+            if (!TP3_DCHECK(r0 + cnt <= drows && pbase + 4 * q2 + 3 < ps && 4 * q3 + 3 < ps, err)) continue;
             float acc[4][4];
             fold_tile(reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2),
                       reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3), rstride, cnt, acc);
@@ -361,7 +380,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
               const int loc0 = k2 * (k2 + 1) / 2 + 4 * q3;
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
-                if (4 * q3 + j <= k2) {
+                if (4 * q3 + j <= k2 && TP3_DCHECK(lbase + loc0 + j < stage, err)) {
                   const float v = scale * acc[i][j];
                   Ts[lbase + loc0 + j] = v;
                   if (T32P) T32P[(size_t)(t3 + loc0 + j) * ldT32 + lt] = v;
@@ -374,6 +393,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           __nv_bfloat16* lrow = reinterpret_cast<__nv_bfloat16*>(Tlo) + ((size_t)prop * KP + lt) * klp;
           for (int idx = lane; idx < na + nb; idx += 32) {
             const int ki = idx < na ? t3a + idx : t3b + (idx - na);
+            if (!TP3_DCHECK(ki < klp && lt < KP && idx < stage, err)) continue;
             const float v = Ts[idx];
             const __nv_bfloat16 h = __float2bfloat16_rn(v);
             hrow[ki] = h;
@@ -395,6 +415,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           const int l3 = l3min + 2 * s;
           const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
           const int r0 = fold_drow(s, s_lo, l3min, sym);
+          if (!TP3_DCHECK(r0 + cnt <= drows && pbase + 4 * q2 + 3 < ps && 4 * q3 + 3 < ps, err)) continue;
           float acc[4][4];
           fold_tile(reinterpret_cast<const float4*>(Dw + r0 * ps + pbase + 4 * q2),
                     reinterpret_cast<const float4*>(cT + r0 * ps + 4 * q3), rstride, cnt, acc);
@@ -407,7 +428,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
             const int row0 = t3 + k2 * (k2 + 1) / 2 + 4 * q3;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-              if (4 * q3 + j <= k2) {
+              if (4 * q3 + j <= k2 && TP3_DCHECK(row0 + j < klp && lt < KP, err)) {
                 const float v = scale * acc[i][j];
                 fold_store_split(ThiP, TloP, (size_t)(row0 + j) * KP + lt, v, tf32out);
                 if (T32P) T32P[(size_t)(row0 + j) * ldT32 + lt] = v;
@@ -546,7 +567,7 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
 #define TP3_FOLD_LAUNCH(NW)                                                                                      \
   k_couple_fold<NW><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks,     \
                                                    fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP, sym, \
-                                                   Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag)
+                                                   Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag, tc.err)
   switch (fv.nw) {
     case 7: TP3_FOLD_LAUNCH(7); break;
     case 8: TP3_FOLD_LAUNCH(8); break;

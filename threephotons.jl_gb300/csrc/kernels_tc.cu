@@ -69,10 +69,18 @@ __global__ void __launch_bounds__(256) k_gather_sym(int K, int nc, int ncoef, co
                                                     const int* __restrict__ cm, const int* __restrict__ cmir,
                                                     const double2* __restrict__ coeff, float2* __restrict__ cc,
                                                     int* __restrict__ sym, const int* __restrict__ cl,
-                                                    const RagInfo* __restrict__ rag) {
+                                                    const RagInfo* __restrict__ rag, int* __restrict__ err) {
   const int prop = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const double2* cp = coeff + (size_t)prop * K * ncoef;
+#ifdef TP3_DEBUG
+  {  // the coefficient maps stay inside a shell's coefficients and the compact layout
+    int maps_ok = 1;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x)
+      maps_ok &= csean[c] >= 0 && csean[c] < ncoef && cmir[c] >= 0 && cmir[c] < nc;
+    if (!TP3_DCHECK(__syncthreads_and(maps_ok) != 0, err)) K = 0;  // nothing is read or written
+  }
+#endif
   int ok = 1;
   for (int k = warp; k < K; k += nw) {
     const double2* ck = cp + (size_t)k * ncoef;
@@ -851,7 +859,7 @@ cudaError_t tc_configure() {
 
 cudaError_t launch_gather_sym(const DevTables& t, const TcTables& tc, int n, const double2* coeff, CoeffLayout lay,
                               float2* cc, int* sym, cudaStream_t s, const RagInfo* rag) {
-  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, lay.stride, lay.map, tc.cm, tc.cmir, coeff, cc, sym, tc.cl, rag);
+  k_gather_sym<<<n, 256, 0, s>>>(t.K, t.nc, lay.stride, lay.map, tc.cm, tc.cmir, coeff, cc, sym, tc.cl, rag, tc.err);
   return cudaGetLastError();
 }
 
