@@ -59,16 +59,23 @@ UNIT = "proposals/s"
 MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
 COUPLING_NAMES = {0: "fused_512", 1: "split", 2: "fused_256x2", 3: "warp_local", 4: "warp_local_256x2",
                   5: "folded_8w", 6: "folded_7w", 7: "folded_13w"}
+ANGULAR_NAMES = {0: "tile", 1: "persistent"}
+ANGULAR_CODES = {v: k for k, v in ANGULAR_NAMES.items()}
 DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each stage's kernel, measured
 # with ncu on one 32-proposal launch of this workload and written as bytes per proposal plus
 # a per-launch constant (each proposal's T is written and read once; the histogram and the
 # tables are read once per launch), by (mode, coupling form).
 STAGE_TRAFFIC = {
-    ("tc_bf16x3", "folded_7w"): {"coupling": (154.2e6 / 32, 0.0), "angular": (230.2e6 / 32, 0.0),
+    ("tc_bf16x3", "folded_7w", "tile"): {"coupling": (154.2e6 / 32, 0.0), "angular": (230.2e6 / 32, 0.0),
                                  "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal "
                                            "launch, scaled in proportion to the proposals "
                                            "(profiles/traffic_L18K26N32_b32_folded7w.md)"},
+    ("tc_bf16x3", "folded_7w", "persistent"): {
+        "coupling": (154.2e6 / 32, 0.0), "angular": (231.1e6 / 32, 0.0),
+        "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal launch of each stage, "
+                  "scaled in proportion to the proposals (profiles/traffic_L18K26N32_b32_folded7w.md, "
+                  "profiles/k_angular_tp_L18K26N32_b32.md)"},
 }
 
 
@@ -352,7 +359,8 @@ def ragged_measure(reps: int, warmup: int, rank: int = 0) -> dict:
             "chain_steps_per_s": float((s1["steps"] - s0["steps"]).sum()) / (ms / 1e3),
             "Ks": Ks.tolist(), "Ls": Ls.tolist(), "mode": MODE_NAMES.get(mode),
             "autotune": [{"mode": MODE_NAMES.get(m), "coupling": COUPLING_NAMES.get(sp) if m else None,
-                          "ms_per_proposal": t} for m, sp, t in tuning],
+                          "angular": ANGULAR_NAMES.get(a) if m else None, "ms_per_proposal": t}
+                         for m, sp, a, t in tuning],
             "spot_check": {"chains": [(int(Ls[c]), int(Ks[c])) for c in picks],
                            "max_rel_energy_diff_vs_own_shape_context": float(max(rel))},
             "gpu_launches_per_replay": 7,
@@ -453,6 +461,8 @@ def run_chains(args):
                         "tf32": tp3.TP3_MODE_TC_TF32X3}[args.mode])
         if args.coupling >= 0:
             basis.set_coupling(args.coupling)
+        if args.mode in ("tc", "tf32"):
+            basis.set_angular(ANGULAR_CODES[args.angular])
     nch, ncand = 64, 16
     ch = Chains(basis, np.repeat(base[None, :K], nch, axis=0), 5.0, math.pi / 4, 1.02, 0.99998, 12345 + rank,
                 ncand=ncand)
@@ -492,6 +502,8 @@ def main():
     ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned", "chains"])
     ap.add_argument("--coupling", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6, 7],
                     help="force a tensor-core coupling form (with --mode tc/tf32)")
+    ap.add_argument("--angular", default="persistent", choices=["persistent", "tile"],
+                    help="angular-stage schedule of the tensor-core path (with --mode tc/tf32)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chains", action="store_true")
     ap.add_argument("--no-ragged", action="store_true", help="leave the ragged-chain key out of the line")
@@ -524,11 +536,14 @@ def main():
     tuning = None
     if mode is None:
         tuning = [{"mode": MODE_NAMES.get(m, str(m)), "coupling": COUPLING_NAMES.get(sp) if m else None,
-                   "ms_per_proposal": ms} for m, sp, ms in basis.autotune(args.batch)]
+                   "angular": ANGULAR_NAMES.get(a) if m else None, "ms_per_proposal": ms}
+                  for m, sp, a, ms in basis.autotune(args.batch)]
     else:
         basis.set_mode(mode)
         if args.coupling >= 0:
             basis.set_coupling(args.coupling)
+        if mode != tp3.TP3_MODE_PLAIN_FP32:
+            basis.set_angular(ANGULAR_CODES[args.angular])
     mode_used = basis.mode
     B = args.batch
     basis.reserve(B)
@@ -608,14 +623,16 @@ def main():
     per_launch_ms = ms_prof / max(1, n_prof)
     achieved = W_b * B / (per_launch_ms / 1e3) / 1e12
     cform = None
+    aname = args.angular
     if tuning:
         best = min((t for t in tuning if t["mode"] == MODE_NAMES.get(mode_used)), key=lambda t: t["ms_per_proposal"],
                    default=None)
         cform = best["coupling"] if best else None
+        aname = (best["angular"] if best else None) or aname
     elif args.coupling >= 0:
         cform = COUPLING_NAMES.get(args.coupling)
     traffic_c = traffic_a = None
-    tsrc = STAGE_TRAFFIC.get((MODE_NAMES.get(mode_used), cform))
+    tsrc = STAGE_TRAFFIC.get((MODE_NAMES.get(mode_used), cform, aname))
     if tsrc is not None:
         traffic_c = tsrc["coupling"][0] * B + tsrc["coupling"][1]
         traffic_a = tsrc["angular"][0] * B + tsrc["angular"][1]
@@ -638,7 +655,8 @@ def main():
                                "peak": fp32_peak, "frac": ach_c / fp32_peak, "unit": "TFLOP/s",
                                "peak_source": "measured FFMA (tp3_measure_fp32_peak, this run)",
                                "traffic": traffic_c},
-                  "angular": {"bound": "tensor", "kernel": "angular contraction + fused Bayes (tcgen05)",
+                  "angular": {"bound": "tensor",
+                              "kernel": f"angular contraction + fused Bayes (tcgen05, {aname} schedule)",
                               "ms_per_launch": per_launch_ms, "algorithmic_flop_per_proposal": W_b,
                               "achieved": achieved, "peak": peak, "frac": achieved / peak, "unit": "TFLOP/s",
                               "peak_source": f"{peak_src} bf16 dense burst", "traffic": traffic_a}}

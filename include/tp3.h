@@ -110,12 +110,23 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * largest per-warp D buffer that fits 225 KB; in BF16 mode it writes T order-major and
  * the angular kernel reads it MN-major) -- selects
  * the fastest for this context and records it for the shape (L, LMAX, N, K, lambda,
- * dq) in the process, where TP3_MODE_AUTO finds it.  report (nullable): up to *nreport
- * rows of (mode, coupling form, ms per proposal); *nreport returns the number of
- * variants.  Synchronises. */
+ * dq) in the process, where TP3_MODE_AUTO finds it.  Every variant is timed with the
+ * persistent angular schedule; the fastest tensor-core variant is then timed again
+ * with one CTA per angular tile, and the faster schedule is kept.  report (nullable):
+ * up to *nreport rows of four values (mode, coupling form, angular schedule, ms per
+ * proposal); *nreport returns the number of rows.  Synchronises. */
 int tp3_autotune(tp3_ctx* ctx, int n, double* report, int* nreport);
 /* Force a coupling form of the tensor-core path (0 to 7 as above). */
 int tp3_set_coupling(tp3_ctx* ctx, int form);
+/* Angular-stage schedule of the tensor-core path (no reference counterpart).
+ * TP3_ANGULAR_PERSISTENT (default): one CTA per SM walks (proposal, 128-triple tile,
+ * grid half) units with two TMEM accumulators, so the Bayes epilogue of one unit
+ * overlaps the tensor-core work of the next.  TP3_ANGULAR_TILE: one CTA per
+ * (tile, proposal), both grid halves in sequence.  Energies agree to FP32 rounding of
+ * the partial sums; the c3 output path always uses the per-tile kernel. */
+#define TP3_ANGULAR_TILE 0
+#define TP3_ANGULAR_PERSISTENT 1
+int tp3_set_angular(tp3_ctx* ctx, int schedule);
 /* Pre-size scratch for batches of up to n proposals (otherwise sized on first use). */
 int tp3_reserve(tp3_ctx* ctx, int n);
 
@@ -335,6 +346,30 @@ int tp3_sample_pictures_ex(tp3_ctx* ctx, int n_pictures, int64_t first_picture, 
  * rejection sampling is normalised by).  Synchronises. */
 int tp3_intensity_max(tp3_ctx* ctx, const void* d_coeff, int KMAX, int LMAX, double dq, int n_theta, int n_phi,
                       double* out);
+
+/* ---- structure -> SH coefficients (src/structure.jl:125-134) ------------------
+ * FP64 on the context's device and stream, for n_mol molecules at once.  atoms:
+ * [n_atoms][5] = x, y, z (Angstrom, centred as centerStructure does), R, B (the atom
+ * factor of its element, src/structure.jl:8-16); molecule i owns atoms mol_start[i] ..
+ * mol_start[i + 1] - 1 (mol_start[0] = 0).  Each shell is sampled on the reference's
+ * surface grid (getSurface / i_to_ang: 2 LMAX x 2 LMAX points) and transformed with the
+ * semantics of the s2kit forward transform at bandwidth LMAX (transform,
+ * src/spherical_harmonics.jl:127-136): orthonormal Y_lm with the Condon-Shortley phase,
+ * coefficients in seanindex order.  Outputs (host, nullable) are [n_mol][KMAX][LMAX^2]
+ * complex (re, im interleaved); shell k (1-based) of the density sits at
+ * r = k rmax / KMAX, of the amplitude and intensity at q = k pi / rmax.
+ *   TP3_SH_INTENSITY: intensity = transform of |F(q)|^2 (getIntensity_cartesian,
+ *     src/structure.jl:89-102), the reference's intensityShell route; density and
+ *     amplitude must be NULL.
+ *   TP3_SH_REFERENCE: the route of createSphericalHarmonicsStructure: density shells
+ *     (getDensity_cartesian, atoms cut at |x - a|^2 < 5) -> transform -> forward
+ *     spherical Bessel transform (sphBesselTransform, src/spherical_harmonics.jl:291-347)
+ *     = amplitude -> absoluteSquare (src/spherical_harmonics.jl:376-381) = intensity.
+ * 2 <= LMAX <= 48, 2 <= KMAX <= 4096.  Synchronises. */
+#define TP3_SH_INTENSITY 0
+#define TP3_SH_REFERENCE 1
+int tp3_structure_sh(tp3_ctx* ctx, const double* atoms, const int* mol_start, int n_mol, int LMAX, int KMAX,
+                     double rmax, int route, double* density, double* amplitude, double* intensity);
 
 /* ---- Wigner-D rotations (src/spherical_harmonics.jl:572-603) --------------- */
 /* rotationMatrix(theta, phi, gamma, l) of src/spherical_harmonics.jl:590-592:

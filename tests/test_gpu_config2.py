@@ -57,6 +57,27 @@ def test_c3_and_energy_all_modes(prod):
     basis.set_coupling(0)
 
 
+@pytest.mark.parametrize("mode", [tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3])
+def test_angular_schedules_at_production_shape(prod, mode):
+    """Both grid halves (512 unique points) and 26 tiles per proposal: the persistent and
+    per-tile angular schedules give the FP64 energy for 64 perturbed proposals."""
+    basis, coeff, ob, F, c3_64, hist = prod
+    basis.set_mode(mode)
+    basis.set_coupling(6)
+    rng = np.random.default_rng(5)
+    coeffs = np.stack([coeff * (1 + 0.02 * rng.normal(size=coeff.shape)) for _ in range(64)])
+    basis.set_angular(tp3.TP3_ANGULAR_PERSISTENT)
+    Ep = basis.energy_batch(coeffs)
+    basis.set_angular(tp3.TP3_ANGULAR_TILE)
+    Et = basis.energy_batch(coeffs)
+    basis.set_angular(tp3.TP3_ANGULAR_PERSISTENT)
+    basis.set_mode(tp3.TP3_MODE_TC_BF16X3)
+    basis.set_coupling(0)
+    np.testing.assert_allclose(Ep, Et, rtol=5e-7)  # FP32 partial sums in another order
+    for i in (0, 63):
+        assert Ep[i] == pytest.approx(_e64(ob, F, hist, coeffs[i]), rel=1e-6)
+
+
 def test_short_chain_matches_fp64_chain(prod):
     basis, coeff, ob, F, c3_64, hist = prod
     seed = 0xC0FFEE

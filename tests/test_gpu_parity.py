@@ -184,6 +184,38 @@ def test_coupling_forms_agree(basis1, config1, config1_hist, form, kind):
     basis1.set_coupling(0)
 
 
+@pytest.mark.parametrize("mode", [tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3])
+@pytest.mark.parametrize("form", [0, 6])
+def test_angular_schedules_agree(basis1, config1, config1_hist, mode, form):
+    """The persistent angular schedule (one CTA per SM over (proposal, tile, half) units,
+    two TMEM accumulators) and the one-CTA-per-tile schedule score alike: 400 proposals
+    give every CTA more than two units, so both accumulators are reused.  Form 6 feeds
+    the order-major T (MN-major A operand in BF16 mode), form 0 the K-major one."""
+    basis1.set_mode(mode)
+    basis1.set_coupling(form)
+    basis1.set_histogram(config1_hist)
+    rng = np.random.default_rng(11)
+    coeffs = np.stack([config1["coeff"] * (1 + 0.03 * rng.normal(size=config1["coeff"].shape)) for _ in range(400)])
+    basis1.set_angular(tp3.TP3_ANGULAR_PERSISTENT)
+    Ep = basis1.energy_batch(coeffs)
+    basis1.set_angular(tp3.TP3_ANGULAR_TILE)
+    Et = basis1.energy_batch(coeffs)
+    basis1.set_angular(tp3.TP3_ANGULAR_PERSISTENT)
+    basis1.set_coupling(0)
+    np.testing.assert_allclose(Ep, Et, rtol=5e-7)  # FP32 partial sums in another order
+    p = config1["params"]
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    F = lt_form_F(b)
+    for i in (0, 137, 399):
+        e64 = energy_bayes(c3_lt_form(F, triple_products(b, coeffs[i])), config1_hist, p["K"], p["N"])
+        assert Ep[i] == pytest.approx(e64, rel=1e-6)
+
+
+def test_angular_schedule_argument_checked(basis1):
+    with pytest.raises(tp3.TP3Error):
+        basis1.set_angular(2)
+
+
 def test_bounded_wait_reports_timeout_and_context_stays_usable(basis1, config1, config1_hist):
     """Failure detection without a fault: a device wait on a flag nothing sets runs out
     after ~5 ms, the status reaches the host as TP3_ERR_TIMEOUT at the next synchronising

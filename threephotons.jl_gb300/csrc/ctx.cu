@@ -30,11 +30,12 @@ using tp3::TcTables;
 namespace {
 thread_local std::string g_create_error;
 
-// Autotuned evaluation variant (mode, coupling form) per shape, shared by every
-// context of the process; TP3_MODE_AUTO uses it when present.
+// Autotuned evaluation variant (mode, coupling form, angular schedule) per shape,
+// shared by every context of the process; TP3_MODE_AUTO uses it when present.
 struct TuneEntry {
   int mode = -1;
   int split = 0;
+  bool persist = true;
 };
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int, double, double>, TuneEntry> g_tuned;
@@ -178,6 +179,8 @@ std::string setup_tc(tp3_ctx* c) {
     if (v % 2 != 0) return "3j row alignment invariant violated";
   tc.n_pb = (int)pbs.size();
   tc.maxs = maxs;
+  if (cudaDeviceGetAttribute(&tc.nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || tc.nsm < 1)
+    return "SM count query failed";
   tc.SDmax = SDmax;
   // coupling kernel shared memory: coefficients [K][ncp], 3j block, D [pmax][SDp]
   tc.ncp = b.nc | 1;
@@ -467,7 +470,9 @@ int ensure_cap(tp3_ctx* c, int n) {
       (e = cudaMalloc(&c->d_E, (size_t)n * sizeof(double))) != cudaSuccess ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Thi, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
-      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * t.klength * sizeof(double))) != cudaSuccess) ||
+      // per-slab terms (one CTA per tile) or 8 partial sums per shell triple (persistent)
+      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * std::max<size_t>(t.klength, 4 * (size_t)t.klp) *
+                                                    sizeof(double))) != cudaSuccess) ||
       (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
       (t.nqp > 0 && (e = cudaMalloc(&c->d_H, (size_t)n * t.klp * t.nqp * sizeof(float))) != cudaSuccess) ||
       (c->tc_ok && c->tc.split_ok &&
@@ -569,13 +574,24 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
   int pr = prof_begin(c, &a, &b);
   if (is_tc(c->mode)) {
     const bool tf = c->mode == TP3_MODE_TC_TF32X3;
-    if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, rag ? c->d_qt_set : c->d_qt,
-                                    rag ? c->d_Qf_set : c->d_Qfold, c->d_Eslab, nullptr, c->d_err, tf, c->stream,
-                                    rag)) != cudaSuccess)
-      return cuda_fail(c, e, "angular_tc");
-    if (pr) cudaEventRecord(b, c->stream);
-    if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream, rag)) != cudaSuccess)
-      return cuda_fail(c, e, "finalize_slabs");
+    const float* qt = rag ? c->d_qt_set : c->d_qt;
+    const double* Qf = rag ? c->d_Qf_set : c->d_Qfold;
+    if (c->tc.persist) {
+      float* part = reinterpret_cast<float*>(c->d_Eslab);
+      if ((e = tp3::launch_angular_persistent(t, c->tc, tf ? c->maps32 : c->maps, n, qt, part, c->d_err, tf, c->stream,
+                                              rag)) != cudaSuccess)
+        return cuda_fail(c, e, "angular_persistent");
+      if (pr) cudaEventRecord(b, c->stream);
+      if ((e = tp3::launch_finalize_parts(t, c->tc, n, part, Qf, d_E, c->stream, rag)) != cudaSuccess)
+        return cuda_fail(c, e, "finalize_parts");
+    } else {
+      if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, qt, Qf, c->d_Eslab, nullptr, c->d_err,
+                                      tf, c->stream, rag)) != cudaSuccess)
+        return cuda_fail(c, e, "angular_tc");
+      if (pr) cudaEventRecord(b, c->stream);
+      if ((e = tp3::launch_finalize_slabs(n, t.klength, c->d_Eslab, d_E, c->stream, rag)) != cudaSuccess)
+        return cuda_fail(c, e, "finalize_slabs");
+    }
   } else {
     const int ncg = tp3::plain_ncg(t);
     if ((e = tp3::launch_angular_plain(t, n, plain_A(c), c->d_qfull, c->d_part, ncg, nullptr, c->stream)) != cudaSuccess)
@@ -916,7 +932,10 @@ int tp3_set_mode(tp3_ctx* c, int mode) {
     }
     if (te.mode >= 0 && (te.mode == TP3_MODE_PLAIN_FP32 || c->tc_ok)) {
       c->mode = te.mode;
-      if (c->tc_ok) apply_coupling(c, te.split);
+      if (c->tc_ok) {
+        apply_coupling(c, te.split);
+        c->tc.persist = te.persist;
+      }
       return TP3_OK;
     }
     mode = c->tc_ok ? TP3_MODE_TC_BF16X3 : TP3_MODE_PLAIN_FP32;
@@ -935,17 +954,21 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   // variants: the plain path, and each tensor-core mode with each coupling form it can run
   // coupling forms: 0 one-kernel (512 threads, one CTA per SM), 1 two-kernel split,
   // 2 one-kernel small tiling (256 threads, two CTAs per SM)
-  std::vector<std::pair<int, int>> vars = {{TP3_MODE_PLAIN_FP32, 0}};
+  struct Var {
+    int mode, form;
+    bool persist;
+  };
+  std::vector<Var> vars = {{TP3_MODE_PLAIN_FP32, 0, true}};
   if (c->tc_ok)
     for (int m : {TP3_MODE_TC_BF16X3, TP3_MODE_TC_TF32X3}) {
-      if (c->tc.fused_ok) vars.push_back({m, 0});
-      if (c->tc.small_ok) vars.push_back({m, 2});
-      if (c->tc.warp_ok) vars.push_back({m, 3});
-      if (c->tc.warp2_ok) vars.push_back({m, 4});
-      if (c->tc.split_ok) vars.push_back({m, 1});
-      if (c->tc.fold[0].ok) vars.push_back({m, 5});
-      if (c->tc.fold[1].ok) vars.push_back({m, 6});
-      if (c->tc.fold[2].ok) vars.push_back({m, 7});
+      if (c->tc.fused_ok) vars.push_back({m, 0, true});
+      if (c->tc.small_ok) vars.push_back({m, 2, true});
+      if (c->tc.warp_ok) vars.push_back({m, 3, true});
+      if (c->tc.warp2_ok) vars.push_back({m, 4, true});
+      if (c->tc.split_ok) vars.push_back({m, 1, true});
+      if (c->tc.fold[0].ok) vars.push_back({m, 5, true});
+      if (c->tc.fold[1].ok) vars.push_back({m, 6, true});
+      if (c->tc.fold[2].ok) vars.push_back({m, 7, true});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
   const size_t nco = (size_t)b.K * b.LMAX * b.LMAX;
@@ -986,30 +1009,52 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
   const bool warp0 = c->tc_ok ? c->tc.use_warp : false;
   const bool warp20 = c->tc_ok ? c->tc.use_warp2 : false;
   const int fold0 = c->tc_ok ? c->tc.use_fold : -1;
+  const bool persist0 = c->tc_ok ? c->tc.persist : true;
   const bool prof0 = c->prof;
   c->prof = false;
   int best = -1, rc = TP3_OK;
   double best_ms = 0.0;
-  std::vector<double> ms(vars.size(), -1.0);
-  for (size_t v = 0; v < vars.size() && rc == TP3_OK; ++v) {
-    c->mode = vars[v].first;
-    if (c->tc_ok) apply_coupling(c, vars[v].second);
-    if ((rc = ensure_cap(c, n)) != TP3_OK) break;
-    if ((rc = run_energy(c, n, d_c, d_e)) != TP3_OK) break;  // warm-up
+  std::vector<double> ms;
+  // ms per proposal of one variant (best of 3 after a warm-up), or a negative status
+  auto time_var = [&](const Var& va, double& out) -> int {
+    c->mode = va.mode;
+    if (c->tc_ok) {
+      apply_coupling(c, va.form);
+      c->tc.persist = va.persist;
+    }
+    int r;
+    if ((r = ensure_cap(c, n)) != TP3_OK) return r;
+    if ((r = run_energy(c, n, d_c, d_e)) != TP3_OK) return r;  // warm-up
     double mn = 1e300;
-    for (int rep = 0; rep < 3 && rc == TP3_OK; ++rep) {
+    for (int rep = 0; rep < 3; ++rep) {
       cudaEventRecord(e0, c->stream);
-      rc = run_energy(c, n, d_c, d_e);
+      if ((r = run_energy(c, n, d_c, d_e)) != TP3_OK) return r;
       cudaEventRecord(e1, c->stream);
-      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) { rc = cuda_fail(c, e, "autotune timing"); break; }
+      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return cuda_fail(c, e, "autotune timing");
       float t = 0.f;
       cudaEventElapsedTime(&t, e0, e1);
       mn = std::min(mn, (double)t);
     }
-    if (rc == TP3_OK) rc = check_device_error(c);
-    if (rc != TP3_OK) break;
-    ms[v] = mn / n;
-    if (best < 0 || ms[v] < best_ms) { best = (int)v; best_ms = ms[v]; }
+    if ((r = check_device_error(c)) != TP3_OK) return r;
+    out = mn / n;
+    return TP3_OK;
+  };
+  // pass 1: every (mode, coupling form) with the persistent angular schedule
+  for (size_t v = 0; v < vars.size() && rc == TP3_OK; ++v) {
+    double t = -1.0;
+    if ((rc = time_var(vars[v], t)) != TP3_OK) break;
+    ms.push_back(t);
+    if (best < 0 || t < best_ms) { best = (int)v; best_ms = t; }
+  }
+  // pass 2: the winner, if it is a tensor-core variant, with one CTA per angular tile
+  if (rc == TP3_OK && best >= 0 && vars[best].mode != TP3_MODE_PLAIN_FP32) {
+    const Var alt{vars[best].mode, vars[best].form, false};
+    double t = -1.0;
+    if ((rc = time_var(alt, t)) == TP3_OK) {
+      vars.push_back(alt);
+      ms.push_back(t);
+      if (t < best_ms) { best = (int)vars.size() - 1; best_ms = t; }
+    }
   }
   cudaFree(d_c); cudaFree(d_e);
   cudaEventDestroy(e0); cudaEventDestroy(e1);
@@ -1018,17 +1063,21 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
     c->mode = mode0;
     if (c->tc_ok) {
       c->tc.split = split0; c->tc.use_small = small0; c->tc.use_warp = warp0;
-      c->tc.use_warp2 = warp20; c->tc.use_fold = fold0;
+      c->tc.use_warp2 = warp20; c->tc.use_fold = fold0; c->tc.persist = persist0;
     }
     return rc != TP3_OK ? rc : fail(c, TP3_ERR_UNSUPPORTED, "no variant ran");
   }
-  c->mode = vars[best].first;
-  if (c->tc_ok) apply_coupling(c, vars[best].first == TP3_MODE_PLAIN_FP32 ? 0 : vars[best].second);
+  c->mode = vars[best].mode;
+  if (c->tc_ok) {
+    apply_coupling(c, vars[best].mode == TP3_MODE_PLAIN_FP32 ? 0 : vars[best].form);
+    c->tc.persist = vars[best].persist;
+  }
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     TuneEntry te;
-    te.mode = vars[best].first;
-    te.split = vars[best].second;
+    te.mode = vars[best].mode;
+    te.split = vars[best].form;
+    te.persist = vars[best].persist;
     g_tuned[tune_key(b)] = te;
   }
   if (nreport) {
@@ -1036,9 +1085,10 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
     int k = 0;
     for (size_t v = 0; v < vars.size() && k < cap; ++v, ++k) {
       if (report) {
-        report[3 * k] = vars[v].first;
-        report[3 * k + 1] = vars[v].second;
-        report[3 * k + 2] = ms[v];
+        report[4 * k] = vars[v].mode;
+        report[4 * k + 1] = vars[v].form;
+        report[4 * k + 2] = vars[v].persist ? 1.0 : 0.0;
+        report[4 * k + 3] = ms[v];
       }
     }
     *nreport = (int)vars.size();
@@ -1054,6 +1104,15 @@ int tp3_set_coupling(tp3_ctx* c, int form) {
                   (form == 6 && c->tc.fold[1].ok) || (form == 7 && c->tc.fold[2].ok);
   if (!ok) return fail(c, form < 0 || form > 7 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
   apply_coupling(c, form);
+  return TP3_OK;
+}
+
+int tp3_set_angular(tp3_ctx* c, int schedule) {
+  if (int r = check_ctx(c)) return r;
+  if (schedule != TP3_ANGULAR_TILE && schedule != TP3_ANGULAR_PERSISTENT)
+    return fail(c, TP3_ERR_ARG, "unknown angular schedule");
+  if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
+  c->tc.persist = schedule == TP3_ANGULAR_PERSISTENT;
   return TP3_OK;
 }
 

@@ -166,6 +166,8 @@ struct TcTables {
   const int* cmir = nullptr;     // [nc] compact index of (l, -m)
   int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
   int NP = 0, nhalf = 0;   // unique grid points padded to 256 * nhalf
+  int nsm = 0;             // SMs of the context's device (persistent angular grid)
+  bool persist = true;     // angular stage: persistent kernel (true) or one CTA per tile
   const int* coff = nullptr;
   const PairBlock* pbs = nullptr;
   const int* eofs = nullptr;
@@ -206,6 +208,13 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
                               const RagInfo* rag = nullptr);
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s,
                                   const RagInfo* rag = nullptr);
+// Persistent angular stage: compensated partial sums into part ([n][klp][8] floats);
+// launch_finalize_parts turns them into slab terms and their sum per proposal.
+cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n,
+                                      const float* qt, float* part, int* err, bool tf32, cudaStream_t s,
+                                      const RagInfo* rag = nullptr);
+cudaError_t launch_finalize_parts(const DevTables& t, const TcTables& tc, int n, const float* part, const double* Qs,
+                                  double* E, cudaStream_t s, const RagInfo* rag = nullptr);
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
 size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
 cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);

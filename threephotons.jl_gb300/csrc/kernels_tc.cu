@@ -782,6 +782,201 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
   }
 }
 
+// Persistent schedule of the same contraction (Bayes terms only).  A unit is one
+// (proposal, 128-shell-triple tile, 256-column half of the grid), half fastest; CTA c
+// takes units c, c + gridDim.x, ...  TMEM holds two 256-column accumulators: the i-th
+// unit of a CTA accumulates into buffer i & 1, so the epilogue warps drain one unit
+// while the MMA warp fills the other.  tmem_full[b] (one arrival, tcgen05.commit) hands
+// a buffer to the epilogue; tmem_empty[b] (one arrival per epilogue warp) hands it back.
+// The epilogue writes compensated partial sums per (row, half, column block) to
+// part [prop][klp][2 halves][2 blocks][Sp, Sql]; k_finalize_parts forms the slab terms.
+template <bool TF32, bool AMN>
+__global__ void __launch_bounds__(kThreads, 1) k_angular_tp(
+    const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
+    const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
+    int Gu, int nhalf, int nunits, const float* __restrict__ qt, float* __restrict__ part, int* __restrict__ err,
+    const RagInfo* __restrict__ rag) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t tmem_empty[2];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stages = base;
+  TcSmemHeader* hd = (TcSmemHeader*)(base + kStages * kStageBytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nmt = klp / kBM;
+  constexpr int kbk = TF32 ? kBK / 2 : kBK;
+  const int nk = KP / kbk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&hd->full[s], 1);
+      mbar_init(&hd->empty[s], 1);
+    }
+    mbar_init(&hd->tmem_full[0], 1);
+    mbar_init(&hd->tmem_full[1], 1);
+    mbar_init(&tmem_empty[0], kEpiWarps);
+    mbar_init(&tmem_empty[1], kEpiWarps);
+    hd->abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&hd->tmem_base)),
+                 "r"(512u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = hd->tmem_base;
+  volatile int* abort_flag = &hd->abort_flag;
+
+  // unit -> (prop, mtile, h); false for tiles past a ragged proposal's scored triples
+  auto decode = [&](int u, int& prop, int& mtile, int& h) -> bool {
+    h = u % nhalf;
+    const int tile = u / nhalf;
+    mtile = tile % nmt;
+    prop = tile / nmt;
+    return !rag || mtile * kBM < rag[prop].klen;
+  };
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      int last[kStages];
+#pragma unroll
+      for (int s = 0; s < kStages; ++s) last[s] = -1;
+      for (int u = blockIdx.x; u < nunits && !*abort_flag; u += gridDim.x) {
+        int prop, mtile, h;
+        if (!decode(u, prop, mtile, h)) continue;
+        const int row0 = prop * klp + mtile * kBM;
+        for (int kc = 0; kc < nk; ++kc, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)((it / kStages) & 1);
+          if (!mbar_wait(&hd->empty[s], ph ^ 1u, abort_flag, err)) break;
+          last[s] = it;
+          uint8_t* st = stages + s * kStageBytes;
+          mbar_expect_tx(&hd->full[s], kStageBytes);
+          if (AMN) {
+            const int y = prop * KP + kc * kbk;
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+              tma_load_2d(st + g * (kABytes / 2), &tmA_hi, &hd->full[s], mtile * kBM + g * 64, y);
+              tma_load_2d(st + kABytes + g * (kABytes / 2), &tmA_lo, &hd->full[s], mtile * kBM + g * 64, y);
+            }
+          } else {
+            tma_load_2d(st, &tmA_hi, &hd->full[s], kc * kbk, row0);
+            tma_load_2d(st + kABytes, &tmA_lo, &hd->full[s], kc * kbk, row0);
+          }
+          tma_load_2d(st + 2 * kABytes, &tmB_hi, &hd->full[s], kc * kbk, h * kBN);
+          tma_load_2d(st + 2 * kABytes + kBBytes, &tmB_lo, &hd->full[s], kc * kbk, h * kBN);
+        }
+      }
+      if (*abort_flag) {
+        for (int s = 0; s < kStages; ++s) {
+          if (last[s] < 0) continue;
+          const long long t0 = clock64();
+          while (!mbar_try_wait(&hd->full[s], (uint32_t)((last[s] / kStages) & 1)) &&
+                 clock64() - t0 < kTimeoutCycles) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_m128_n256(TF32 ? 2u : 1u) | (AMN ? (1u << 15) : 0u);
+      int it = 0, i = 0;
+      for (int u = blockIdx.x; u < nunits && !*abort_flag; u += gridDim.x) {
+        int prop, mtile, h;
+        if (!decode(u, prop, mtile, h)) continue;
+        const int b = i & 1;
+        // the buffer's previous unit (i - 2) must have been read out by the epilogue
+        if (!mbar_wait(&tmem_empty[b], (uint32_t)(((i >> 1) & 1) ^ 1), abort_flag, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dt = tmem + (uint32_t)(b * kBN);
+        bool ok = true;
+        for (int kc = 0; kc < nk; ++kc, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)((it / kStages) & 1);
+          if (!mbar_wait(&hd->full[s], ph, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(stages + s * kStageBytes);
+          const uint64_t ahi = AMN ? smem_desc_mn_sw128(st, kABytes / 2) : smem_desc_sw64(st);
+          const uint64_t alo = AMN ? smem_desc_mn_sw128(st + kABytes, kABytes / 2) : smem_desc_sw64(st + kABytes);
+          const uint64_t bhi = smem_desc_sw64(st + 2 * kABytes), blo = smem_desc_sw64(st + 2 * kABytes + kBBytes);
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t dk = (uint64_t)(ks * 2);
+            const uint64_t da = AMN ? (uint64_t)(ks * 128) : dk;
+            mma_issue<TF32>(dt, ahi + da, bhi + dk, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+            mma_issue<TF32>(dt, ahi + da, blo + dk, idesc, 1u);
+            mma_issue<TF32>(dt, alo + da, bhi + dk, idesc, 1u);
+          }
+          mma_commit(&hd->empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&hd->tmem_full[b]);
+        ++i;
+      }
+    }
+  } else {
+    // ---------------- epilogue: 8 warps ----------------
+    const int ew = warp - 2;
+    const int quarter = warp & 3;
+    const int cblk = ew >> 2;
+    const int r = quarter * 32 + lane;
+    int i = 0;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+      int prop, mtile, h;
+      if (!decode(u, prop, mtile, h)) continue;
+      const int b = i & 1;
+      if (!mbar_wait(&hd->tmem_full[b], (uint32_t)((i >> 1) & 1), abort_flag, err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const float* qrow = qt + (rag ? (size_t)rag[prop].hist * klp * Gu : 0) + ((size_t)mtile * Gu) * kBM + r;
+      float sp = 0.f, sq = 0.f, csp = 0.f, csq = 0.f;
+      for (int cc = 0; cc < 4; ++cc) {
+        const int col = cblk * 128 + cc * 32;  // column inside the half
+        const int u0 = h * kBN + col;          // unique grid point of column 0
+        float q[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) q[j] = u0 + j < Gu ? qrow[(size_t)(u0 + j) * kBM] : 0.f;
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * kBN + col), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          if (u0 + j < Gu) {
+            const float p = fmaxf(v[j], 1e-30f);
+            const float y1 = p - csp;
+            const float t1 = sp + y1;
+            csp = (t1 - sp) - y1;
+            sp = t1;
+            const float y2 = q[j] * __logf(p) - csq;
+            const float t2 = sq + y2;
+            csq = (t2 - sq) - y2;
+            sq = t2;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tmem_empty[b])) : "memory");
+      reinterpret_cast<float2*>(part)[((size_t)prop * klp + mtile * kBM + r) * 4 + h * 2 + cblk] =
+          make_float2(sp - csp, sq - csq);
+      ++i;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+  }
+}
+
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
   s = a + b;
   const double bb = s - a;
@@ -818,6 +1013,50 @@ __global__ void __launch_bounds__(256) k_finalize_slabs(const double* __restrict
   if (threadIdx.x == 0) E[prop] = ss[0] + sc[0];
 }
 
+// grid: n; block 256.  Slab terms tf (Qs log(mult Sp) - Sql) from the persistent
+// kernel's partial sums (FP64 from here on), then the same compensated sum.
+__global__ void __launch_bounds__(256) k_finalize_parts(const float* __restrict__ part, int klp, int klength,
+                                                        int nhalf, const double* __restrict__ Qs,
+                                                        const double* __restrict__ tf, int mult,
+                                                        double* __restrict__ E, const RagInfo* __restrict__ rag) {
+  __shared__ double ss[256], sc[256];
+  const int prop = blockIdx.x;
+  int nk = klength;
+  if (rag) {
+    nk = rag[prop].klen;
+    Qs += (size_t)rag[prop].hist * klength;
+  }
+  const float4* p4 = reinterpret_cast<const float4*>(part) + (size_t)prop * klp * 2;
+  double s = 0.0, c = 0.0;
+  for (int ki = threadIdx.x; ki < nk; ki += blockDim.x) {
+    const float4 a = p4[(size_t)ki * 2];  // half 0: (Sp, Sql) of column blocks 0 and 1
+    double Sp = (double)a.x + (double)a.z, Sq = (double)a.y + (double)a.w;
+    if (nhalf == 2) {
+      const float4 b = p4[(size_t)ki * 2 + 1];
+      Sp += (double)b.x + (double)b.z;
+      Sq += (double)b.y + (double)b.w;
+    }
+    const double e = tf[ki] * (Qs[ki] * log((double)mult * Sp) - Sq);
+    double t, err;
+    two_sum(s, e, t, err);
+    s = t;
+    c += err;
+  }
+  ss[threadIdx.x] = s;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      double t, err;
+      two_sum(ss[threadIdx.x], ss[threadIdx.x + h], t, err);
+      ss[threadIdx.x] = t;
+      sc[threadIdx.x] += sc[threadIdx.x + h] + err;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) E[prop] = ss[0] + sc[0];
+}
+
 }  // namespace
 
 size_t tc_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(TcSmemHeader); }
@@ -831,7 +1070,10 @@ cudaError_t tc_configure() {
       (e = cudaFuncSetAttribute(k_angular_tc<false, true, false>, ds, smem)) != cudaSuccess ||
       (e = cudaFuncSetAttribute(k_angular_tc<true, true, false>, ds, smem)) != cudaSuccess ||
       (e = cudaFuncSetAttribute(k_angular_tc<false, false, true>, ds, smem)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tc<true, false, true>, ds, smem)) != cudaSuccess)
+      (e = cudaFuncSetAttribute(k_angular_tc<true, false, true>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<false, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<true, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<false, true>, ds, smem)) != cudaSuccess)
     return e;
   const int cs = kCoupleMaxDynSmem, css = kCoupleSmallSmem;
 #define TP3_CP_ATTR(S, W)                                                                                    \
@@ -958,6 +1200,29 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s,
                                   const RagInfo* rag) {
   k_finalize_slabs<<<n, 256, 0, s>>>(Eslab, klength, E, rag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n,
+                                      const float* qt, float* part, int* err, bool tf32, cudaStream_t s,
+                                      const RagInfo* rag) {
+  const int nunits = n * (t.klp / kBM) * tc.nhalf;
+  const int ctas = std::max(1, std::min(nunits, tc.nsm));
+  const size_t smem = tc_smem_bytes();
+  const bool amn = t_order_major(tc, tf32);
+#define TP3_ANGP(TF, MN, AH, AL)                                                                                     \
+  k_angular_tp<TF, MN><<<ctas, kThreads, smem, s>>>(AH, AL, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, tc.nhalf, nunits, \
+                                                    qt, part, err, rag)
+  if (tf32) TP3_ANGP(true, false, maps.a_hi, maps.a_lo);
+  else if (amn) TP3_ANGP(false, true, maps.a_hi_mn, maps.a_lo_mn);
+  else TP3_ANGP(false, false, maps.a_hi, maps.a_lo);
+#undef TP3_ANGP
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_parts(const DevTables& t, const TcTables& tc, int n, const float* part, const double* Qs,
+                                  double* E, cudaStream_t s, const RagInfo* rag) {
+  k_finalize_parts<<<n, 256, 0, s>>>(part, t.klp, t.klength, tc.nhalf, Qs, t.tf, t.mult, E, rag);
   return cudaGetLastError();
 }
 

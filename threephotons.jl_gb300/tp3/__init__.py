@@ -7,8 +7,9 @@ so it is a source directory, not an importable package name)::
     import tp3
 """
 from ._lib import TP3Error, load, LIB_PATH, SIGNATURES  # noqa: F401
-from ._lib import (TP3_MODE_AUTO, TP3_MODE_PLAIN_FP32, TP3_MODE_TC_BF16X3, TP3_MODE_TC_TF32X3,  # noqa: F401
-                   TP3_MOVE_DRIFT, TP3_MOVE_LEARNED, TP3_MOVE_REFERENCE, TP3_MOVE_SHELL_SO3)
+from ._lib import (TP3_ANGULAR_PERSISTENT, TP3_ANGULAR_TILE, TP3_MODE_AUTO, TP3_MODE_PLAIN_FP32,  # noqa: F401
+                   TP3_MODE_TC_BF16X3, TP3_MODE_TC_TF32X3, TP3_MOVE_DRIFT, TP3_MOVE_LEARNED, TP3_MOVE_REFERENCE,
+                   TP3_MOVE_SHELL_SO3)
 from .api import (BasisTypeGB300, CUDA_init, FullCorrelation_parallized, SphericalHarmonicsVolume,  # noqa: F401
                   Umat, calculate_basis, complexBasis_choice, dq, energy, rotateStructure, rotationMatrix)
 from . import structure  # noqa: F401

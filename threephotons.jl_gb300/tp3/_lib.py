@@ -35,6 +35,10 @@ TP3_MOVE_REFERENCE = 0
 TP3_MOVE_SHELL_SO3 = 1
 TP3_MOVE_LEARNED = 2
 TP3_MOVE_DRIFT = 3
+TP3_ANGULAR_TILE = 0
+TP3_ANGULAR_PERSISTENT = 1
+TP3_SH_INTENSITY = 0
+TP3_SH_REFERENCE = 1
 
 # name -> (restype, argtypes); every symbol include/tp3.h declares
 SIGNATURES = {
@@ -52,6 +56,9 @@ SIGNATURES = {
     "tp3_reserve": (c_int, [c_void_p, c_int]),
     "tp3_autotune": (c_int, [c_void_p, c_int, c_void_p, P(c_int)]),
     "tp3_set_coupling": (c_int, [c_void_p, c_int]),
+    "tp3_set_angular": (c_int, [c_void_p, c_int]),
+    "tp3_structure_sh": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_int, c_void_p,
+                                 c_void_p, c_void_p]),
     "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),
     "tp3_c3": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tp3_c3_batch_device": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),

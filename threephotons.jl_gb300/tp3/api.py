@@ -155,14 +155,22 @@ class BasisTypeGB300:
 
     def autotune(self, n: int = 64) -> list:
         """Time every evaluation variant on n synthetic proposals, keep the fastest (also
-        for later TP3_MODE_AUTO contexts of this shape); returns [(mode, coupling form, ms/proposal)]
-        with coupling form 0 one-kernel, 1 split, 2 one-kernel on 256 threads (two CTAs per SM),
-        3 warp-local one-kernel, 4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7
-        folded-row at 8 / 7 / 13 warps."""
-        cap = ctypes.c_int(16)
-        rep = np.zeros(3 * 16)
+        for later TP3_MODE_AUTO contexts of this shape); returns
+        [(mode, coupling form, angular schedule, ms/proposal)] with coupling form 0 one-kernel,
+        1 split, 2 one-kernel on 256 threads (two CTAs per SM), 3 warp-local one-kernel,
+        4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7 folded-row at 8 / 7 / 13
+        warps, and angular schedule TP3_ANGULAR_PERSISTENT or TP3_ANGULAR_TILE (the
+        fastest tensor-core variant is timed with both)."""
+        cap = ctypes.c_int(24)
+        rep = np.zeros(4 * 24)
         check(self._lib.tp3_autotune(self._ctx, n, rep.ctypes.data, ctypes.byref(cap)), self._ctx)
-        return [(int(rep[3 * i]), int(rep[3 * i + 1]), float(rep[3 * i + 2])) for i in range(min(cap.value, 16))]
+        return [(int(rep[4 * i]), int(rep[4 * i + 1]), int(rep[4 * i + 2]), float(rep[4 * i + 3]))
+                for i in range(min(cap.value, 24))]
+
+    def set_angular(self, schedule: int) -> None:
+        """Angular-stage schedule of the tensor-core path: TP3_ANGULAR_PERSISTENT
+        (default) or TP3_ANGULAR_TILE."""
+        check(self._lib.tp3_set_angular(self._ctx, schedule), self._ctx)
 
     def _adopt(self, obj) -> None:
         """Register an object holding library handles on this context (chains, networks);

@@ -6,14 +6,20 @@ Host-side FP64 code (runs once per run, not per proposal).
   reference parser reads (src/structure.jl:30-55: serial in columns 9-11, x/y/z in
   31-38/39-46/47-54, B-factor in 62-66, element in column 78), centred on the mean
   position (structure.jl:58-70).
+* ``structure_sh`` / ``createSphericalHarmonicsStructure``: the reference's route on the
+  GPU (tp3_structure_sh): density shells -> s2kit-semantics transform -> spherical Bessel
+  transform -> absoluteSquare, for many molecules in one call.
 * ``intensity_coefficients``: SH coefficients of the intensity shells
   I(q) = |sum_j B_j exp(-R_j^2 q^2 / 2) exp(i q.r_j)|^2 (getIntensity_cartesian,
   structure.jl:80-94, atom factors structure.jl:8-16) at q_k = k pi / rmax, the
   shell spacing createSphericalHarmonicsStructure produces (forward() sets the
   Fourier-space rmax to qmax = pi KMAX / rmax, spherical_harmonics.jl:92-96, 336).
-  The reference reaches the same intensity through density shells, s2kit and a
-  discrete Hankel transform; here the intensity is evaluated analytically on a
-  Gauss-Legendre x uniform-phi grid and projected onto Y_lm = sphPlm(l,m,theta) e^{i m phi}.
+  The intensity is evaluated analytically on a Gauss-Legendre x uniform-phi grid and
+  projected onto Y_lm = sphPlm(l,m,theta) e^{i m phi}: the coefficients of the
+  reference's intensityShell route (s2kit transform of getIntensity_cartesian samples)
+  up to the two grids' aliasing of orders >= LMAX.  createSphericalHarmonicsStructure's
+  own route band-limits the density at LMAX before its Hankel transform, so its
+  intensity differs from this one; ``structure_sh`` reproduces that route.
   The hot path's triple products are invariant under the (-1)^m and conjugation
   conventions of the coefficients, so the coefficient convention does not change c3.
 * ``poisson_histogram`` / ``loadHistograms``: the target histogram (model c3 scaled
@@ -174,9 +180,61 @@ def intensity_coefficients(atoms: list, LMAX: int, KMAX: int, rmax: float, n_the
     return out
 
 
-def createSphericalHarmonicsStructure(pdb_path: str, LMAX: int, KMAX: int, rmax: float) -> np.ndarray:
-    """Intensity coefficients of a PDB structure (role of structure.jl:125-134)."""
-    return intensity_coefficients(loadPDB(pdb_path), LMAX, KMAX, rmax)
+_SH_BASIS = None
+
+
+def _sh_basis():
+    """A small context that carries the stream and error state of structure_sh calls."""
+    global _SH_BASIS
+    if _SH_BASIS is None:
+        from .api import calculate_basis
+        _SH_BASIS = calculate_basis(2, 3, 4, 2)
+    return _SH_BASIS
+
+
+def atom_table(atoms: list) -> np.ndarray:
+    """[n][5] rows (x, y, z, R, B) with the element's atom factor (structure.jl:8-16)."""
+    return np.array([[*a.pos, *ATOM_FACTORS.get(a.element, _DEFAULT_FACTOR)] for a in atoms],
+                    dtype=np.float64).reshape(-1, 5)
+
+
+def structure_sh(molecules: list, LMAX: int, KMAX: int, rmax: float, route: str = "reference",
+                 basis=None) -> dict:
+    """SH coefficients of many molecules on the GPU (tp3_structure_sh), complex128
+    [n_mol, KMAX, LMAX^2] in seanindex order.
+
+    route "reference": the route of createSphericalHarmonicsStructure (structure.jl:125-134):
+    density shells at r_k = k rmax / KMAX -> s2kit-semantics transform -> forward spherical
+    Bessel transform -> absoluteSquare; returns {"density", "amplitude", "intensity"}.
+    route "intensity": transform of |F(q_k)|^2 sampled on the same grid (intensityShell);
+    returns {"intensity"}.  Amplitude and intensity shells sit at q_k = k pi / rmax."""
+    from . import _lib
+    b = basis or _sh_basis()
+    code = {"reference": _lib.TP3_SH_REFERENCE, "intensity": _lib.TP3_SH_INTENSITY}[route]
+    tabs = [atom_table(m) for m in molecules]
+    atoms = np.ascontiguousarray(np.concatenate(tabs) if tabs else np.zeros((0, 5)))
+    start = np.zeros(len(molecules) + 1, dtype=np.int32)
+    start[1:] = np.cumsum([t.shape[0] for t in tabs])
+    shape = (len(molecules), KMAX, LMAX * LMAX)
+    outs = {k: np.zeros(shape, dtype=np.complex128) for k in
+            (("density", "amplitude", "intensity") if code == _lib.TP3_SH_REFERENCE else ("intensity",))}
+    ptr = lambda k: outs[k].ctypes.data if k in outs else None  # noqa: E731
+    _lib.check(b._lib.tp3_structure_sh(b._ctx, atoms.ctypes.data, start.ctypes.data, len(molecules), LMAX, KMAX,
+                                       float(rmax), code, ptr("density"), ptr("amplitude"), ptr("intensity")),
+               b._ctx)
+    return outs
+
+
+def createSphericalHarmonicsStructure(pdb_path: str, LMAX: int, KMAX: int, rmax: float):
+    """(density, fourierTransform, intensity) of a PDB structure as SphericalHarmonicsVolume
+    objects, by the reference's route on the GPU (structure.jl:125-134): the density with
+    rmax, the amplitude and intensity with rmax = qmax = pi KMAX / rmax."""
+    from .api import SphericalHarmonicsVolume
+    out = structure_sh([loadPDB(pdb_path)], LMAX, KMAX, rmax, route="reference")
+    qmax = math.pi * KMAX / rmax
+    return (SphericalHarmonicsVolume(out["density"][0], LMAX, KMAX, rmax),
+            SphericalHarmonicsVolume(out["amplitude"][0], LMAX, KMAX, qmax),
+            SphericalHarmonicsVolume(out["intensity"][0], LMAX, KMAX, qmax))
 
 
 def tripletFactor(k1: int, k2: int, k3: int) -> float:
