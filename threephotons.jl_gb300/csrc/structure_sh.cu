@@ -1,0 +1,362 @@
+// Structure -> spherical-harmonic coefficients on the device, FP64: the role of
+// createSphericalHarmonicsStructure (src/structure.jl:125-134), the step that turns a
+// molecule into the intensity coefficients the hot path scores, for many molecules
+// at once.
+//
+// Surfaces are sampled on the reference's grid (getSurface / i_to_ang,
+// src/spherical_harmonics.jl:203-210, 228-235: size = 2 LMAX, sample
+// itheta * size + iphi at phi = 2 pi iphi / size, theta = pi (2 itheta + 1) / (2 size))
+// and transformed with the semantics of the s2kit forward / inverse transforms the
+// reference calls with bandwidth LMAX (transform / backtransform,
+// src/spherical_harmonics.jl:127-148; src/sh/s2kit_interface.c:72-178):
+//   c(l, m) = sum_theta w_theta Ptilde_l^|m|(cos theta) s_m F_m(theta),
+//   F_m(theta) = sqrt(2 pi) / size sum_phi f(theta, phi) e^{-i m phi},
+// with the Driscoll-Healy weights w, Legendre functions normalised to unit L2 norm on
+// [-1, 1] with the Condon-Shortley phase, and s_m = (-1)^|m| for m < 0 (1 otherwise);
+// the inverse is the exact synthesis sum c(l, m) Y_lm on the same grid.  Sums are
+// direct (no FFT): size (2 LMAX - 1) terms per Fourier value, size per coefficient.
+//
+// Routes:
+//   TP3_SH_INTENSITY: intensity shells |F(q)|^2 of Gaussian atoms (getIntensity_cartesian,
+//     src/structure.jl:89-102) at q_k = k pi / rmax (the reference's intensityShell).
+//   TP3_SH_REFERENCE: density shells at r_k = k rmax / KMAX (getDensity_cartesian,
+//     src/structure.jl:72-86, atoms cut at |x - a|^2 < 5) -> forward transform ->
+//     spherical Bessel transform (sphBesselTransform with frdr and the J_{l+1/2} matrices,
+//     src/spherical_harmonics.jl:291-347) -> inverse transform, |.|^2, forward transform
+//     (absoluteSquare, src/spherical_harmonics.jl:376-381).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "ctx_internal.h"
+
+namespace {
+
+constexpr int kShMaxLMAX = 48;  // Fourier table of one surface: 2 LMAX x (2 LMAX - 1) complex in shared memory
+constexpr double kPi = 3.141592653589793;
+
+// grid: (ceil(P / 256), KMAX, n_mol); block 256.  atoms [n][5] = x, y, z, R, B.
+__global__ void __launch_bounds__(256) k_sh_sample(const double* __restrict__ atoms, const int* __restrict__ mol_start,
+                                                   int size, int KMAX, double rmax, int density,
+                                                   double2* __restrict__ out) {
+  const int P = size * size;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y + 1, mol = blockIdx.z;
+  if (p >= P) return;
+  const int it = p / size, ip = p - it * size;
+  const double phi = 2.0 * kPi * ip / size;
+  const double theta = kPi * (2 * it + 1) / (2.0 * size);
+  const double st = sin(theta);
+  const double ux = cos(phi) * st, uy = sin(phi) * st, uz = cos(theta);
+  const int a0 = mol_start[mol], a1 = mol_start[mol + 1];
+  double v;
+  if (density) {
+    const double r = k * (rmax / KMAX);
+    const double x = r * ux, y = r * uy, z = r * uz;
+    v = 0.0;
+    for (int a = a0; a < a1; ++a) {
+      const double* at = atoms + 5 * (size_t)a;
+      const double dx = x - at[0], dy = y - at[1], dz = z - at[2];
+      const double d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 < 5.0) {
+        const double R = at[3], s = R * sqrt(2.0 * kPi);
+        v += at[4] / (s * s * s) * exp(-d2 / (2.0 * R * R));
+      }
+    }
+  } else {
+    const double q = k * kPi / rmax;
+    const double x = q * ux, y = q * uy, z = q * uz;
+    double sc = 0.0, ss = 0.0;
+    for (int a = a0; a < a1; ++a) {
+      const double* at = atoms + 5 * (size_t)a;
+      const double f = at[4] * exp(-0.5 * at[3] * at[3] * q * q);
+      double sn, cs;
+      sincos(x * at[0] + y * at[1] + z * at[2], &sn, &cs);
+      sc += f * cs;
+      ss += f * sn;
+    }
+    v = sc * sc + ss * ss;
+  }
+  out[((size_t)mol * KMAX + (k - 1)) * P + p] = make_double2(v, 0.0);
+}
+
+// grid: surfaces; block 256; dynamic shared memory size (2 bw - 1) double2.
+// Forward transform of complex samples [surface][size^2] into [surface][bw^2] (seanindex).
+// plm [l][m][theta] (0 <= m <= l < bw), w [theta], root [size] = e^{2 pi i j / size},
+// lm [bw^2] = (l, m) of each seanindex slot.
+__global__ void __launch_bounds__(256) k_sht_forward(const double2* __restrict__ in, int bw,
+                                                     const double* __restrict__ plm, const double* __restrict__ w,
+                                                     const double2* __restrict__ root, const int2* __restrict__ lm,
+                                                     double2* __restrict__ out) {
+  extern __shared__ double2 sF[];  // [theta][m + bw - 1]
+  const int size = 2 * bw, nm = 2 * bw - 1;
+  const double2* f = in + (size_t)blockIdx.x * size * size;
+  const double sc = sqrt(2.0 * kPi) / size;
+  for (int i = threadIdx.x; i < size * nm; i += blockDim.x) {
+    const int t = i / nm, m = i - t * nm - (bw - 1);
+    double re = 0.0, im = 0.0;
+    const int mm = ((m % size) + size) % size;
+    for (int j = 0; j < size; ++j) {
+      const double2 v = f[t * size + j];
+      const double2 e = root[(size - (mm * j) % size) % size];  // e^{-i m phi_j}
+      re += v.x * e.x - v.y * e.y;
+      im += v.x * e.y + v.y * e.x;
+    }
+    sF[i] = make_double2(re * sc, im * sc);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < bw * bw; i += blockDim.x) {
+    const int2 q = lm[i];
+    const int l = q.x, m = q.y, ma = m < 0 ? -m : m;
+    const double* pl = plm + ((size_t)l * bw + ma) * size;
+    double re = 0.0, im = 0.0;
+    for (int t = 0; t < size; ++t) {
+      const double c = w[t] * pl[t];
+      const double2 v = sF[t * nm + m + bw - 1];
+      re += c * v.x;
+      im += c * v.y;
+    }
+    if (m < 0 && (ma & 1)) re = -re, im = -im;
+    out[(size_t)blockIdx.x * bw * bw + i] = make_double2(re, im);
+  }
+}
+
+// grid: surfaces; block 256; dynamic shared memory size (2 bw - 1) double2.
+// Synthesis sum_lm c(l, m) Y_lm on the grid, Y_lm = Ptilde_l^|m| s_m e^{i m phi} / sqrt(2 pi).
+// idx [m + bw - 1][l] = seanindex slot of (l, m) (read only for l >= |m|).
+__global__ void __launch_bounds__(256) k_sht_inverse(const double2* __restrict__ in, int bw,
+                                                     const double* __restrict__ plm, const double2* __restrict__ root,
+                                                     const int* __restrict__ idx, double2* __restrict__ out) {
+  extern __shared__ double2 sG[];  // [theta][m + bw - 1]
+  const int size = 2 * bw, nm = 2 * bw - 1;
+  const double2* c = in + (size_t)blockIdx.x * bw * bw;
+  const double isq = 1.0 / sqrt(2.0 * kPi);
+  for (int i = threadIdx.x; i < size * nm; i += blockDim.x) {
+    const int t = i / nm, mi = i - t * nm, m = mi - (bw - 1), ma = m < 0 ? -m : m;
+    double re = 0.0, im = 0.0;
+    for (int l = ma; l < bw; ++l) {
+      const double p = plm[((size_t)l * bw + ma) * size + t];
+      const double2 v = c[idx[mi * bw + l]];
+      re += p * v.x;
+      im += p * v.y;
+    }
+    const double s = (m < 0 && (ma & 1)) ? -isq : isq;
+    sG[i] = make_double2(re * s, im * s);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < size * size; i += blockDim.x) {
+    const int t = i / size, j = i - t * size;
+    double re = 0.0, im = 0.0;
+    for (int mi = 0; mi < nm; ++mi) {
+      const int m = mi - (bw - 1);
+      const int mm = ((m % size) + size) % size;
+      const double2 e = root[(mm * j) % size];  // e^{+i m phi_j}
+      const double2 v = sG[t * nm + mi];
+      re += v.x * e.x - v.y * e.y;
+      im += v.x * e.y + v.y * e.x;
+    }
+    out[(size_t)blockIdx.x * size * size + i] = make_double2(re, im);
+  }
+}
+
+// In place: |f|^2 of every sample (the square of absoluteSquare).
+__global__ void k_abs2(double2* __restrict__ f, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double2 v = f[i];
+    f[i] = make_double2(v.x * v.x + v.y * v.y, 0.0);
+  }
+}
+
+// grid: (ceil(bw^2 / 128), KMAX, n_mol); block 128.  Forward spherical Bessel transform
+// along the shells of every coefficient: out[k'] = i^l sqrt(1/k') sum_k J[l][k'][k] h[k] in[k].
+__global__ void __launch_bounds__(128) k_sh_hankel(const double2* __restrict__ in, int bw, int KMAX,
+                                                   const double* __restrict__ J, const double* __restrict__ h,
+                                                   const int2* __restrict__ lm, double2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int kp = blockIdx.y, mol = blockIdx.z;
+  const int nco = bw * bw;
+  if (i >= nco) return;
+  const int l = lm[i].x;
+  const double* Jr = J + ((size_t)l * KMAX + kp) * KMAX;
+  const double2* src = in + (size_t)mol * KMAX * nco + i;
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < KMAX; ++k) {
+    const double2 v = src[(size_t)k * nco];
+    const double c = Jr[k] * h[k];
+    re += c * v.x;
+    im += c * v.y;
+  }
+  const double s = sqrt(1.0 / (kp + 1));
+  re *= s;
+  im *= s;
+  double2 o;
+  switch (l & 3) {  // multiply by i^l
+    case 0: o = make_double2(re, im); break;
+    case 1: o = make_double2(-im, re); break;
+    case 2: o = make_double2(-re, -im); break;
+    default: o = make_double2(im, -re); break;
+  }
+  out[((size_t)mol * KMAX + kp) * nco + i] = o;
+}
+
+int seanindex0(int l, int m, int bw) {
+  const int bigL = bw - 1;
+  if (m >= 0) return m * (bigL + 1) - (m * (m - 1)) / 2 + (l - m);
+  return (bigL * (bigL + 3)) / 2 + 1 + ((bigL + m) * (bigL + m + 1)) / 2 + (l - (m < 0 ? -m : m));
+}
+
+// Host tables, FP64.
+struct ShTables {
+  std::vector<double> plm, w, J, h;
+  std::vector<double2> root;
+  std::vector<int2> lm;
+  std::vector<int> idx;
+};
+
+void build_sh_tables(int bw, int KMAX, bool hankel, ShTables& T) {
+  const int size = 2 * bw;
+  T.plm.assign((size_t)bw * bw * size, 0.0);
+  T.w.assign(size, 0.0);
+  for (int t = 0; t < size; ++t) {
+    const double th = kPi * (2 * t + 1) / (2.0 * size);
+    double s = 0.0;
+    for (int k = 0; k < bw; ++k) s += std::sin((2 * k + 1) * th) / (2 * k + 1);
+    T.w[t] = 2.0 / bw * std::sin(th) * s;
+    // normalised associated Legendre functions by the standard three-term recurrence in l
+    const double x = std::cos(th), sx = std::sqrt(std::fmax(0.0, 1.0 - x * x));
+    double pmm = std::sqrt(0.5);
+    for (int m = 0; m < bw; ++m) {
+      if (m > 0) pmm = -pmm * sx * std::sqrt((2.0 * m + 1.0) / (2.0 * m));
+      double p2 = 0.0, p1 = pmm;
+      T.plm[((size_t)m * bw + m) * size + t] = pmm;
+      for (int l = m + 1; l < bw; ++l) {
+        double p;
+        if (l == m + 1) {
+          p = x * std::sqrt(2.0 * m + 3.0) * pmm;
+        } else {
+          const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+          const double b = std::sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+          p = a * (x * p1 - b * p2);
+        }
+        T.plm[((size_t)l * bw + m) * size + t] = p;
+        p2 = p1;
+        p1 = p;
+      }
+    }
+  }
+  T.root.resize(size);
+  for (int j = 0; j < size; ++j) {
+    const double a = 2.0 * kPi * j / size;
+    T.root[j] = make_double2(std::cos(a), std::sin(a));
+  }
+  T.lm.resize((size_t)bw * bw);
+  T.idx.assign((size_t)(2 * bw - 1) * bw, 0);
+  for (int l = 0; l < bw; ++l)
+    for (int m = -l; m <= l; ++m) {
+      T.lm[seanindex0(l, m, bw)] = make_int2(l, m);
+      T.idx[(size_t)(m + bw - 1) * bw + l] = seanindex0(l, m, bw);
+    }
+  if (hankel) {
+    // J_{l+1/2}(pi k' k / KMAX) = sqrt(2x / pi) j_l(x); frdr weights on r = 1..KMAX
+    T.J.assign((size_t)bw * KMAX * KMAX, 0.0);
+    for (int l = 0; l < bw; ++l)
+      for (int kp = 1; kp <= KMAX; ++kp)
+        for (int k = 1; k <= KMAX; ++k) {
+          const double x = kPi / KMAX * kp * k;
+          T.J[((size_t)l * KMAX + (kp - 1)) * KMAX + (k - 1)] =
+              std::sqrt(2.0 * x / kPi) * std::sph_bessel((unsigned)l, x);
+        }
+    T.h.assign(KMAX, 0.0);
+    for (int j = 1; j <= KMAX; ++j) {
+      double res;
+      if (j == 1) res = std::sqrt(0.5) * 9.0;                         // sqrt(1/2) (r1 + r2)^2
+      else if (j == KMAX) res = 4.0 * j * j - (2.0 * j - 1.0) * (2.0 * j - 1.0);  // 4 r_l^2 - (r_{l-1} + r_l)^2
+      else res = 2.0 * 4.0 * j;                                        // (r_{j+1} - r_{j-1})(r_{j-1} + 2 r_j + r_{j+1})
+      T.h[j - 1] = kPi / 4.0 * std::pow(res, 1.5);
+    }
+  }
+}
+
+template <class T>
+cudaError_t upload(const std::vector<T>& v, T** d, cudaStream_t s) {
+  cudaError_t e = cudaMalloc(d, v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace
+
+int tp3_structure_sh(tp3_ctx* c, const double* atoms, const int* mol_start, int n_mol, int LMAX, int KMAX,
+                     double rmax, int route, double* density, double* amplitude, double* intensity) {
+  if (int r = tp3::ctx_check(c)) return r;
+  if (!atoms || !mol_start || n_mol < 1 || n_mol > 65535 || LMAX < 2 || LMAX > kShMaxLMAX || KMAX < 2 ||
+      KMAX > 4096 || !(rmax > 0.0) ||
+      (route != TP3_SH_INTENSITY && route != TP3_SH_REFERENCE) ||
+      (route == TP3_SH_INTENSITY && (density || amplitude)) || (!density && !amplitude && !intensity))
+    return tp3::ctx_fail(c, TP3_ERR_ARG, "bad structure_sh arguments");
+  if (mol_start[0] != 0) return tp3::ctx_fail(c, TP3_ERR_ARG, "mol_start[0] must be 0");
+  for (int i = 0; i < n_mol; ++i)
+    if (mol_start[i + 1] < mol_start[i]) return tp3::ctx_fail(c, TP3_ERR_ARG, "mol_start must not decrease");
+  const int n_atoms = mol_start[n_mol];
+  for (int64_t i = 0; i < 5LL * n_atoms; ++i)
+    if (!std::isfinite(atoms[i])) return tp3::ctx_fail(c, TP3_ERR_ARG, "non-finite atom data");
+  for (int a = 0; a < n_atoms; ++a)
+    if (!(atoms[5 * a + 3] > 0.0)) return tp3::ctx_fail(c, TP3_ERR_ARG, "atom width R must be > 0");
+  const int bw = LMAX, size = 2 * bw, P = size * size, nco = bw * bw;
+  const bool ref = route == TP3_SH_REFERENCE;
+  ShTables T;
+  build_sh_tables(bw, KMAX, ref, T);
+  cudaStream_t s = c->stream;
+  const size_t nsurf = (size_t)n_mol * KMAX;
+  double *d_atoms = nullptr, *d_plm = nullptr, *d_w = nullptr, *d_J = nullptr, *d_h = nullptr;
+  double2 *d_root = nullptr, *d_samp = nullptr, *d_c0 = nullptr, *d_c1 = nullptr;
+  int2* d_lm = nullptr;
+  int *d_idx = nullptr, *d_ms = nullptr;
+  const size_t smem = (size_t)size * (2 * bw - 1) * sizeof(double2);
+  std::vector<int> ms(mol_start, mol_start + n_mol + 1);
+  std::vector<double> at(atoms, atoms + 5 * (size_t)n_atoms);
+  if (at.empty()) at.assign(5, 1.0);  // keeps the device copy non-empty; no molecule reads it
+  cudaError_t e;
+  auto cleanup = [&]() {
+    cudaFree(d_atoms); cudaFree(d_plm); cudaFree(d_w); cudaFree(d_J); cudaFree(d_h); cudaFree(d_root);
+    cudaFree(d_samp); cudaFree(d_c0); cudaFree(d_c1); cudaFree(d_lm); cudaFree(d_idx); cudaFree(d_ms);
+  };
+  if ((e = upload(at, &d_atoms, s)) != cudaSuccess || (e = upload(ms, &d_ms, s)) != cudaSuccess ||
+      (e = upload(T.plm, &d_plm, s)) != cudaSuccess || (e = upload(T.w, &d_w, s)) != cudaSuccess ||
+      (e = upload(T.root, &d_root, s)) != cudaSuccess || (e = upload(T.lm, &d_lm, s)) != cudaSuccess ||
+      (e = upload(T.idx, &d_idx, s)) != cudaSuccess ||
+      (ref && ((e = upload(T.J, &d_J, s)) != cudaSuccess || (e = upload(T.h, &d_h, s)) != cudaSuccess)) ||
+      (e = cudaMalloc(&d_samp, nsurf * P * sizeof(double2))) != cudaSuccess ||
+      (e = cudaMalloc(&d_c0, nsurf * nco * sizeof(double2))) != cudaSuccess ||
+      (e = cudaMalloc(&d_c1, nsurf * nco * sizeof(double2))) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_sht_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_sht_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess) {
+    cleanup();
+    cudaGetLastError();
+    return tp3::ctx_cuda_fail(c, e, "structure_sh setup");
+  }
+  const dim3 gs((P + 255) / 256, KMAX, n_mol);
+  const size_t nbytes = nsurf * nco * sizeof(double2);
+  k_sh_sample<<<gs, 256, 0, s>>>(d_atoms, d_ms, size, KMAX, rmax, ref ? 1 : 0, d_samp);
+  k_sht_forward<<<(unsigned)nsurf, 256, smem, s>>>(d_samp, bw, d_plm, d_w, d_root, d_lm, d_c0);
+  if (ref) {
+    if (density) e = cudaMemcpyAsync(density, d_c0, nbytes, cudaMemcpyDeviceToHost, s);
+    k_sh_hankel<<<dim3((nco + 127) / 128, KMAX, n_mol), 128, 0, s>>>(d_c0, bw, KMAX, d_J, d_h, d_lm, d_c1);
+    if (e == cudaSuccess && amplitude) e = cudaMemcpyAsync(amplitude, d_c1, nbytes, cudaMemcpyDeviceToHost, s);
+    k_sht_inverse<<<(unsigned)nsurf, 256, smem, s>>>(d_c1, bw, d_plm, d_root, d_idx, d_samp);
+    const size_t ns = nsurf * P;
+    k_abs2<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(d_samp, ns);
+    k_sht_forward<<<(unsigned)nsurf, 256, smem, s>>>(d_samp, bw, d_plm, d_w, d_root, d_lm, d_c0);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess && intensity) e = cudaMemcpyAsync(intensity, d_c0, nbytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "structure_sh");
+  return TP3_OK;
+}
