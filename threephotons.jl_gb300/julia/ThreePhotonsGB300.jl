@@ -12,12 +12,13 @@
 module ThreePhotonsGB300
 
 import ThreePhotons: AbstractBasisType, SphericalHarmonicsVolume, FullCorrelation_parallized, energy,
-                     Umat, C3, num_coeff
+                     Umat, C3, num_coeff, loadPDB, atomfactorlist
 
 export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_run, GB300_chains_state,
        GB300_energy_batch, GB300_set_mode, GB300_autotune, GB300_chains_log, GB300_chains_snapshot,
        GB300_chains_restore, GB300_chains_coeff, GB300_chains_destroy, GB300_chains_set_move,
-       GB300_chains_enable_move_log, GB300_mlp_create, GB300_mlp_destroy
+       GB300_chains_enable_move_log, GB300_mlp_create, GB300_mlp_destroy, GB300_set_angular,
+       GB300_createSphericalHarmonicsStructure
 
 const libtp3 = joinpath(@__DIR__, "..", "lib", "libtp3.so")
 
@@ -137,14 +138,41 @@ GB300_set_mode(basis::BasisTypeGB300, mode::Int) =
     check(ccall((:tp3_set_mode, libtp3), Int32, (Ptr{Void}, Int32), basis.ctx, mode), basis.ctx)
 
 """Time every evaluation variant on n synthetic proposals and keep the fastest
-(tp3_autotune); rows (mode, coupling form, ms per proposal)."""
+(tp3_autotune); columns (mode, coupling form, angular schedule, ms per proposal)."""
 function GB300_autotune(basis::BasisTypeGB300, n::Int=64)
     cap = 32
-    rep = zeros(Float64, 3, cap)
+    rep = zeros(Float64, 4, cap)
     nrep = Ref{Int32}(cap)
     check(ccall((:tp3_autotune, libtp3), Int32, (Ptr{Void}, Int32, Ptr{Float64}, Ref{Int32}),
                 basis.ctx, n, rep, nrep), basis.ctx)
     return rep[:, 1:min(nrep[], cap)]
+end
+
+"""Angular-stage schedule of the tensor-core path (tp3_set_angular): 1 persistent
+(default), 0 one CTA per tile."""
+GB300_set_angular(basis::BasisTypeGB300, schedule::Int) =
+    check(ccall((:tp3_set_angular, libtp3), Int32, (Ptr{Void}, Int32), basis.ctx, schedule), basis.ctx)
+
+"""createSphericalHarmonicsStructure (src/structure.jl:125-134) on the GPU through
+tp3_structure_sh (route 1: density -> transform -> spherical Bessel transform ->
+absoluteSquare); returns (density, fourierTransform, intensity) like the reference."""
+function GB300_createSphericalHarmonicsStructure(basis::BasisTypeGB300, moleculepdb, LMAX::Integer,
+                                                 KMAX::Integer, rmax::Float64)
+    atomlist = loadPDB(moleculepdb)
+    atoms = zeros(Float64, 5, length(atomlist))
+    for (i, a) in enumerate(atomlist)
+        f = atomfactorlist[a.t]
+        atoms[:, i] = [a.pos[1], a.pos[2], a.pos[3], f.R, f.B]
+    end
+    start = Int32[0, length(atomlist)]
+    out = [zeros(Complex{Float64}, LMAX^2, KMAX) for _ = 1:3]
+    check(ccall((:tp3_structure_sh, libtp3), Int32,
+                (Ptr{Void}, Ptr{Float64}, Ptr{Int32}, Int32, Int32, Int32, Float64, Int32,
+                 Ptr{Complex{Float64}}, Ptr{Complex{Float64}}, Ptr{Complex{Float64}}),
+                basis.ctx, atoms, start, 1, LMAX, KMAX, rmax, 1, out[1], out[2], out[3]), basis.ctx)
+    qmax = pi * KMAX / rmax
+    vol(c, r) = SphericalHarmonicsVolume([c[:, k] for k = 1:KMAX], LMAX, KMAX, r)
+    return vol(out[1], rmax), vol(out[2], qmax), vol(out[3], qmax)
 end
 
 # ---- device-resident chains (rotate_all_at_once on the GPU) ---------------------------
