@@ -4,7 +4,7 @@
     python bench.py --impl reference [--steps K] [--warmup W]
     python bench.py --workload ragged      # 64 chains x 16 candidates, K in 16..26, L in 12..18, own histograms
     python bench.py --workload learned     # learned vs plain annealer: time to the plain final energy
-    python bench.py --no-ragged --no-learned   # the proposal line without the two extra legs
+    python bench.py --no-ragged --no-learned --no-lambda   # the proposal line without the extra legs
     python bench.py --workload chains      # 64 chains x 16 candidates per CUDA-graph replay
 
 --mode tuned (and auto) runs the evaluation-variant autotuner first and benchmarks its
@@ -24,8 +24,10 @@ benchmark datasets).  The L2 cache (129 MB) is flushed by a 512 MB write between
 timed steps, outside the per-step event window.
 
 The line also carries `ragged` (64 chains of mixed L and K, one ragged launch per graph
-replay, with a spot check of three chains against contexts of their own shape) and
-`learned` (the learned-proposal experiment with its network-free drift ablation).
+replay, with a spot check of three chains against contexts of their own shape),
+`lambda` (the same workload at lambda = 2.5 through the tensor-core and plain FP32
+paths) and `learned` (the learned-proposal experiment with its network-free drift
+ablation).
 
 Rank 0 prints one JSON line.  --gpus N > 1 runs N independent replicas (one per
 GPU, launched by torchrun); the path has no collective (annealing chains and
@@ -269,12 +271,6 @@ def reference_cuda_rate(ref, props, hist, calls: int = 3):
         return {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
 
 
-def _molecule_job(args):
-    n_atoms, seed, kcount = args
-    from tp3.structure import synthetic_molecule, intensity_coefficients
-    return intensity_coefficients(synthetic_molecule(n_atoms, seed=seed), LMAX, KMAX, RMAX, kcount=kcount)
-
-
 def ragged_measure(reps: int, warmup: int, rank: int = 0) -> dict:
     """64 chains x 16 speculative candidates per launch; chain c has its own K (16..26), L
     (12..18), molecule (200-400 atoms) and 1e9-triplet histogram; all candidates of a
@@ -282,19 +278,19 @@ def ragged_measure(reps: int, warmup: int, rank: int = 0) -> dict:
     from a CUDA graph.  A spot check scores three chains' current states through the
     ragged launch and through contexts of their own (L, K) and reports the largest
     relative energy difference."""
-    import multiprocessing as mp
     import torch
     import tp3
     from tp3.chains import Chains
-    from tp3.structure import poisson_histogram, loadHistograms, seanindex0
+    from tp3.structure import poisson_histogram, loadHistograms, seanindex0, structure_sh, synthetic_molecule
     nch, ncand = 64, 16
     rng = np.random.default_rng(20250301 + rank)
     Ks = rng.integers(16, K + 1, nch)
     Ls = rng.choice([12, 14, 16, 18], nch)
     atoms = rng.integers(200, 401, nch)
-    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        coeffs = pool.map(_molecule_job, [(int(a), 5000 + 97 * c + rank, K) for c, a in enumerate(atoms)])
-    coeffs = np.stack([c[:K] for c in coeffs])
+    # every chain's molecule expanded to intensity coefficients in one device call
+    # (tp3_structure_sh, intensityShell route, FP64)
+    mols = [synthetic_molecule(int(a), seed=5000 + 97 * c + rank) for c, a in enumerate(atoms)]
+    coeffs = np.ascontiguousarray(structure_sh(mols, LMAX, KMAX, RMAX, route="intensity")["intensity"][:, :K])
     basis = tp3.calculate_basis(L, LMAX, N, K)
     hists = []
     for c in range(nch):
@@ -388,6 +384,50 @@ def run_ragged(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def lambda_measure(reps: int = 10, lam: float = 2.5, dq: float = 0.15) -> dict:
+    """Ewald curvature: the same L18 K26 N32 workload at lambda = 2.5, dq = 0.15 (theta_k =
+    acos(k lambda dq / 4 pi); the reference's own GPU test runs at lambda = 2.5), 64
+    proposals per step through the tensor-core path (coupling, H from FP32 T, persistent
+    tcgen05 contraction with the cosine table on the 2 048-point grid) and through the plain
+    FP32 path; CUDA-event time of `reps` steps each on the launch stream, and the largest
+    relative energy difference between the two paths."""
+    import torch
+    import tp3
+    base = molecule_coefficients()
+    basis = tp3.calculate_basis(L, LMAX, N, K, lam, dq)
+    basis.set_histogram(build_histogram(basis, base))
+    props = proposals(base, 64, PROP_SEED)
+    stream = torch.cuda.Stream()
+    basis.set_stream(stream.cuda_stream)
+    d_coeff = torch.from_numpy(props.view(np.float64)).cuda()
+    out = {"workload": f"L{L} K{K} N{N} LMAX{LMAX}, lambda {lam}, dq {dq}, 64 proposals per step", "steps": reps}
+    E = {}
+    for name, mode, form in (("tc_bf16x3", tp3.TP3_MODE_TC_BF16X3, 6), ("plain_fp32", tp3.TP3_MODE_PLAIN_FP32, None)):
+        basis.set_mode(mode)
+        if form is not None:
+            basis.set_coupling(form)
+        d_E = torch.empty(64, dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            n = reps if mode != tp3.TP3_MODE_PLAIN_FP32 else max(2, reps // 5)
+            basis.energy_batch_device(64, d_coeff.data_ptr(), d_E.data_ptr())  # warm-up
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(n):
+                basis.energy_batch_device(64, d_coeff.data_ptr(), d_E.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        E[name] = d_E.cpu().numpy()
+        out[name] = {"proposals_per_s": 64 / (ms / 1e3), "ms_per_step": ms, "steps": n}
+    basis.set_stream(None)
+    basis.close()
+    out["speedup_vs_plain_fp32"] = out["tc_bf16x3"]["proposals_per_s"] / out["plain_fp32"]["proposals_per_s"]
+    out["max_rel_energy_diff_tc_vs_plain"] = float(np.max(np.abs(E["tc_bf16x3"] - E["plain_fp32"]) /
+                                                          np.abs(E["plain_fp32"])))
+    return out
 
 
 def tp3_mode_id(name):
@@ -508,6 +548,7 @@ def main():
     ap.add_argument("--no-chains", action="store_true")
     ap.add_argument("--no-ragged", action="store_true", help="leave the ragged-chain key out of the line")
     ap.add_argument("--no-learned", action="store_true", help="leave the learned-proposal key out of the line")
+    ap.add_argument("--no-lambda", action="store_true", help="leave the lambda != 0 key out of the line")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -739,6 +780,11 @@ def main():
             line["ragged"] = ragged_measure(10, 2, rank)
         except Exception as exc:  # informational keys: report why they are missing
             line["ragged"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+    if rank == 0 and not args.no_lambda:
+        try:
+            line["lambda"] = lambda_measure()
+        except Exception as exc:
+            line["lambda"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
     if rank == 0 and not args.no_learned:
         try:
             line["learned"] = learned_measure(rank)

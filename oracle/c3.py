@@ -161,3 +161,42 @@ def c3_pair_form(b: OracleBasis, coeff: np.ndarray) -> np.ndarray:
     keys = sorted(qid, key=qid.get)
     Cq = np.cos(np.outer(a, [k[0] for k in keys]) + np.outer(be, [k[1] for k in keys]))
     return Cq @ np.stack(Hrows)
+
+
+def c3_pair_form_fast(b: OracleBasis, T: np.ndarray, chunk: int = 2048) -> np.ndarray:
+    """``c3_pair_form`` for a given FP64 T [klength, n_lt], vectorised over basis entries in
+    chunks (the same sum: H[q, ki] = sum_{j in q} P_j(ki) T[ki, lt(j)], c3 = Cq H), for
+    shapes where the per-entry loop is too slow (L18 K26)."""
+    from .basis import qlist
+    from .sh import sphPlm, alpharange, alpharange_2pi
+    th = qlist(b)
+    L = max(b.lrange)
+    Yk = np.zeros((b.K, L + 1, 2 * L + 1))
+    for k in range(b.K):
+        for l in b.lrange:
+            for m in range(-l, l + 1):
+                Yk[k, l, m + L] = sphPlm(l, m, th[k])
+    lt = lt_of_entry(b)
+    l1, m1, l2, m2, l3, m3 = (b.indices[r].astype(np.int64) for r in range(3, 9))
+    flip = (m2 < 0) | ((m2 == 0) & (m3 < 0))
+    qm2, qm3 = np.where(flip, -m2, m2), np.where(flip, -m3, m3)
+    keys, qid = np.unique(qm2 * 4096 + qm3, return_inverse=True)
+    ks = b.klist - 1
+    H = np.zeros((keys.size, b.klength))
+    from scipy.sparse import csr_matrix
+    for c0 in range(0, b.basislen, chunk):
+        sl = slice(c0, min(b.basislen, c0 + chunk))
+        P = (b.wignerlist[sl][None, :] * Yk[ks[:, 0:1], l1[None, sl], m1[None, sl] + L]
+             * Yk[ks[:, 1:2], l2[None, sl], m2[None, sl] + L] * Yk[ks[:, 2:3], l3[None, sl], m3[None, sl] + L])
+        P *= T[:, lt[sl]]
+        n = P.shape[1]
+        S = csr_matrix((np.ones(n), (qid[sl], np.arange(n))), shape=(keys.size, n))
+        H += S @ P.T
+    N = b.N
+    A, Bg = np.meshgrid(alpharange(N), alpharange_2pi(2 * N), indexing="ij")
+    a = A.reshape(-1, order="F")
+    be = Bg.reshape(-1, order="F")
+    km2 = np.floor_divide(keys + 2048, 4096)
+    km3 = keys - km2 * 4096
+    Cq = np.cos(np.outer(a, km2) + np.outer(be, km3))
+    return Cq @ H

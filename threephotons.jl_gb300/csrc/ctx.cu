@@ -163,9 +163,14 @@ std::string setup_tc(tp3_ctx* c) {
   const Basis& b = c->b;
   DevTables& t = c->t;
   TcTables& tc = c->tc;
-  if (b.lambda != 0.0) return "needs lambda = 0";
-  if (b.mult != 4) return "needs even N (grid fold)";
-  if (b.Gu > 512) return "more than 512 unique grid points (N > 32)";
+  // lambda = 0: F on the 4:1-folded grid; lambda != 0: the cosine table of the Fourier
+  // pairs on the full grid (the persistent angular kernel walks any number of halves)
+  tc.hform = b.lambda != 0.0;
+  if (!tc.hform && b.mult != 4) return "needs even N (grid fold)";
+  if (!tc.hform && b.Gu > 512) return "more than 512 unique grid points (N > 32)";
+  if (tc.hform && (b.Gu > 8192 || c->qpairs.empty())) return "lambda != 0: more than 8192 grid points";
+  if (tc.hform && tp3::build_H_split_smem(c->t, 1) > (size_t)tp3::kPlainMaxSmem)
+    return "lambda != 0: the l-triples of a shell triple exceed the H kernel's shared memory";
   std::vector<PairBlock> pbs;
   std::vector<int> eofs;
   std::vector<float> wtab;
@@ -332,17 +337,29 @@ std::string setup_tc(tp3_ctx* c) {
   tc.n_units_gen = (int)units_gen.size();
   std::vector<int> cmir(b.nc);
   for (int i = 0; i < b.nc; ++i) cmir[i] = b.coff[b.c_l[i] / 2] + b.c_l[i] - b.c_m[i];
-  tc.KP = (b.n_lt() + 31) / 32 * 32;
+  const int kcols = tc.hform ? (int)c->qpairs.size() : b.n_lt();  // K extent before padding
+  tc.KP = (std::max(kcols, b.n_lt()) + 31) / 32 * 32;
   tc.nhalf = (b.Gu + 255) / 256;
   tc.NP = 256 * tc.nhalf;
-  // F on the unique grid points, split into bf16 hi + lo and into tf32 hi + fp32 lo
+  // B operand on the unique grid points, split into bf16 hi + lo and into tf32 hi + fp32
+  // lo: F[u][lt] (lambda = 0) or cos(m2 alpha + m3 beta) of each Fourier pair (lambda != 0)
   std::vector<double> F;
-  tp3::build_F(b, F);
+  if (tc.hform) {
+    F.assign((size_t)b.Gu * kcols, 0.0);
+    for (int u = 0; u < b.Gu; ++u) {
+      const int g = b.u_to_g[u], a = g % b.N, bb = g / b.N;
+      const double al = (a + 0.5) * M_PI / b.N, be = (bb + 0.5) * M_PI / b.N;
+      for (int q = 0; q < kcols; ++q)
+        F[(size_t)u * kcols + q] = std::cos(c->qpairs[q].first * al + c->qpairs[q].second * be);
+    }
+  } else {
+    tp3::build_F(b, F);
+  }
   std::vector<__nv_bfloat16> Fhi((size_t)tc.NP * tc.KP, __float2bfloat16(0.f)), Flo(Fhi);
   std::vector<float> Fhi32((size_t)tc.NP * tc.KP, 0.f), Flo32(Fhi32);
   for (int u = 0; u < b.Gu; ++u)
-    for (int l = 0; l < b.n_lt(); ++l) {
-      const double v64 = F[(size_t)u * b.n_lt() + l];
+    for (int l = 0; l < kcols; ++l) {
+      const double v64 = F[(size_t)u * kcols + l];
       const float v = (float)v64;
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
       Fhi[(size_t)u * tc.KP + l] = hi;
@@ -470,8 +487,10 @@ int ensure_cap(tp3_ctx* c, int n) {
       (e = cudaMalloc(&c->d_E, (size_t)n * sizeof(double))) != cudaSuccess ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Thi, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
-      // per-slab terms (one CTA per tile) or 8 partial sums per shell triple (persistent)
-      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n * std::max<size_t>(t.klength, 4 * (size_t)t.klp) *
+      // per-slab terms (one CTA per tile) or 4 partial sums per grid half and shell triple
+      // (persistent)
+      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n *
+                                                    std::max<size_t>(t.klength, 2 * (size_t)c->tc.nhalf * t.klp) *
                                                     sizeof(double))) != cudaSuccess) ||
       (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
       (t.nqp > 0 && (e = cudaMalloc(&c->d_H, (size_t)n * t.klp * t.nqp * sizeof(float))) != cudaSuccess) ||
@@ -529,6 +548,8 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
   cudaError_t e;
   const tp3::CoeffLayout lay = compact ? tp3::CoeffLayout{t.cident, t.nc} : tp3::CoeffLayout{t.csean, t.LMAX * t.LMAX};
   if (is_tc(c->mode)) {
+    // lambda != 0: the coupling also writes FP32 T, from which H (the angular operand) is built
+    if (c->tc.hform) want_T32 = true;
     if ((e = tp3::launch_gather_sym(t, c->tc, n, d_coeff, lay, c->d_cc, c->d_sym, c->stream, rag)) != cudaSuccess)
       return cuda_fail(c, e, "gather_sym");
     cudaEvent_t ca, cb;
@@ -543,6 +564,9 @@ int run_coupling(tp3_ctx* c, int n, const double2* d_coeff, bool want_T32, bool 
       e = tp3::launch_couple_pair(t, c->tc, n, c->d_cc, c->d_sym, c->d_Thi, c->d_Tlo, c->mode == TP3_MODE_TC_TF32X3,
                                   want_T32 ? c->d_T : nullptr, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "coupling");
+    if (c->tc.hform && (e = tp3::launch_build_H_split(t, c->tc.KP, n, c->d_T, c->d_Thi, c->d_Tlo,
+                                                      c->mode == TP3_MODE_TC_TF32X3, c->stream)) != cudaSuccess)
+      return cuda_fail(c, e, "build_H_split");
     if (pc) cudaEventRecord(cb, c->stream);
   } else {
     if ((e = tp3::launch_gather(t, n, d_coeff, lay, c->d_cc, c->stream)) != cudaSuccess) return cuda_fail(c, e, "gather");
@@ -564,8 +588,9 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
   cudaError_t e;
   if (rag) {
     if (c->nhist == 0) return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histograms has not been called");
-    if (!is_tc(c->mode) || (!c->tc.fused_ok && c->tc.use_fold < 0))
-      return fail(c, TP3_ERR_UNSUPPORTED, "ragged batches need a tensor-core mode with the one-kernel coupling");
+    if (!is_tc(c->mode) || (!c->tc.fused_ok && c->tc.use_fold < 0) || c->tc.hform)
+      return fail(c, TP3_ERR_UNSUPPORTED,
+                  "ragged batches need a tensor-core mode with the one-kernel coupling at lambda = 0");
   } else if (!c->has_hist) {
     return fail(c, TP3_ERR_NO_HISTOGRAM, "tp3_set_histogram has not been called");
   }
@@ -576,7 +601,7 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
     const bool tf = c->mode == TP3_MODE_TC_TF32X3;
     const float* qt = rag ? c->d_qt_set : c->d_qt;
     const double* Qf = rag ? c->d_Qf_set : c->d_Qfold;
-    if (c->tc.persist) {
+    if (c->tc.persist || c->tc.nhalf > 2) {
       float* part = reinterpret_cast<float*>(c->d_Eslab);
       if ((e = tp3::launch_angular_persistent(t, c->tc, tf ? c->maps32 : c->maps, n, qt, part, c->d_err, tf, c->stream,
                                               rag)) != cudaSuccess)
@@ -772,7 +797,7 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   }
   if (b.nc > 1024) { delete c; return fail(nullptr, TP3_ERR_UNSUPPORTED, "L too large: more than 1024 coefficients per shell"); }
   if ((size_t)b.K * b.nc * sizeof(float2) > (size_t)tp3::kPlainMaxSmem ||
-      (lambda != 0.0 && ((size_t)b.K * b.nc + 32 * ((size_t)(b.n_lt() + 63) / 64 * 64)) * sizeof(float) >
+      (lambda != 0.0 && ((size_t)b.K * b.nc + 32 * ((size_t)(b.n_lt() + 63) / 64 * 64 + 1)) * sizeof(float) >
                             (size_t)tp3::kPlainMaxSmem)) {
     delete c;
     return fail(nullptr, TP3_ERR_UNSUPPORTED, "K x coefficients per shell exceed the coupling kernel's shared memory");
@@ -820,6 +845,7 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   // and the cosine table of those pairs on the full grid
   std::vector<float> Ytab, Cq;
   std::vector<int> lt_of_j, qstart, qlist;
+  std::vector<int4> qent;  // per entry in pair order: packed shell-coefficient indices, w bits, l-triple
   if (lambda == 0.0) {
     Basis bf = b;
     tp3::fold_grid(bf, false);
@@ -849,12 +875,20 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
     }
     t.nq = (int)qs.size();
     t.nqp = (t.nq + 15) / 16 * 16;
+    c->qpairs = qs;
     qstart.assign(t.nq + 1, 0);
     for (int j = 0; j < b.basislen(); ++j) qstart[q_of_j[j] + 1]++;
     for (int q = 0; q < t.nq; ++q) qstart[q + 1] += qstart[q];
     qlist.resize(b.basislen());
     std::vector<int> fillp(qstart.begin(), qstart.end() - 1);
     for (int j = 0; j < b.basislen(); ++j) qlist[fillp[q_of_j[j]]++] = j;
+    qent.resize(b.basislen());
+    for (int e = 0; e < b.basislen(); ++e) {
+      const int j = qlist[e];
+      int wb;
+      std::memcpy(&wb, &w32[j], 4);
+      qent[e] = make_int4((int)idx[j], wb, lt_of_j[j], 0);
+    }
     Cq.assign((size_t)t.G * t.nqp, 0.f);
     for (int g = 0; g < t.G; ++g) {
       const int a = g % N, bb = g / N;
@@ -883,6 +917,7 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
       (e = upload(c, b.g_to_u, &t.g_to_u)) != cudaSuccess || (e = tp3::plain_configure()) != cudaSuccess ||
       (e = upload(c, Ytab, &t.Ytab)) != cudaSuccess || (e = upload(c, lt_of_j, &t.lt_of_j)) != cudaSuccess ||
       (e = upload(c, qstart, &t.qstart)) != cudaSuccess || (e = upload(c, qlist, &t.qlist)) != cudaSuccess ||
+      (e = upload(c, qent, &t.qent)) != cudaSuccess ||
       (e = upload(c, Cq, &t.Cq)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess || (e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess ||
       (e = cudaMallocHost(&c->h_err, sizeof(int))) != cudaSuccess) {
@@ -1047,7 +1082,7 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
     if (best < 0 || t < best_ms) { best = (int)v; best_ms = t; }
   }
   // pass 2: the winner, if it is a tensor-core variant, with one CTA per angular tile
-  if (rc == TP3_OK && best >= 0 && vars[best].mode != TP3_MODE_PLAIN_FP32) {
+  if (rc == TP3_OK && best >= 0 && vars[best].mode != TP3_MODE_PLAIN_FP32 && c->tc.nhalf <= 2) {
     const Var alt{vars[best].mode, vars[best].form, false};
     double t = -1.0;
     if ((rc = time_var(alt, t)) == TP3_OK) {
@@ -1112,6 +1147,8 @@ int tp3_set_angular(tp3_ctx* c, int schedule) {
   if (schedule != TP3_ANGULAR_TILE && schedule != TP3_ANGULAR_PERSISTENT)
     return fail(c, TP3_ERR_ARG, "unknown angular schedule");
   if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
+  if (schedule == TP3_ANGULAR_TILE && c->tc.nhalf > 2)
+    return fail(c, TP3_ERR_UNSUPPORTED, "the per-tile angular schedule holds at most 512 grid points in TMEM");
   c->tc.persist = schedule == TP3_ANGULAR_PERSISTENT;
   return TP3_OK;
 }

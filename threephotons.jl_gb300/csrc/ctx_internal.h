@@ -33,6 +33,7 @@ struct tp3_ctx {
   tp3::EncodeTiledFn encode = nullptr;
   tp3::TcMaps maps{};    // bf16 operands
   tp3::TcMaps maps32{};  // tf32 operands
+  std::vector<std::pair<int, int>> qpairs;  // lambda != 0: the Fourier pairs (m2, m3) of H's columns
 
   // histogram
   bool has_hist = false;

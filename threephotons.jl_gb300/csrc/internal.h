@@ -45,6 +45,7 @@ struct DevTables {
   const int* lt_of_j = nullptr;  // [basislen]
   const int* qstart = nullptr;   // [nq + 1] ranges of qlist
   const int* qlist = nullptr;    // [basislen] basis entries grouped by pair
+  const int4* qent = nullptr;    // [basislen] in qlist order: packed indices, w (float bits), l-triple
   const float* Cq = nullptr;     // [G][nqp] cos(m2 alpha + m3 beta)
   const int* g_to_u;    // [G]
 };
@@ -64,6 +65,11 @@ cudaError_t launch_couple_direct(const DevTables& t, int n, const float2* cc, fl
 cudaError_t launch_angular_plain(const DevTables& t, int n, const float* T, const float* q,
                                  double2* part, int ncg, float* c3out, cudaStream_t s);
 cudaError_t launch_build_H(const DevTables& t, int n, const float* T, float* H, cudaStream_t s);
+// lambda != 0 on the tensor-core path: H of a batch from FP32 T, written as split rows
+// [n][klp][KP] (bf16 hi + lo, or tf32 hi + fp32 lo); pair columns past nq are zero.
+size_t build_H_split_smem(const DevTables& t, int ppl);
+cudaError_t launch_build_H_split(const DevTables& t, int KP, int n, const float* T32, void* Hhi, void* Hlo, bool tf32,
+                                 cudaStream_t s);
 cudaError_t launch_finalize(const DevTables& t, int n, const double2* part, int ncg,
                             const double* Qs, int mult, double* E, cudaStream_t s);
 
@@ -164,9 +170,11 @@ struct TcTables {
   const int* cm = nullptr;       // [nc] m of each compact coefficient
   const int* cl = nullptr;       // [nc] l of each compact coefficient
   const int* cmir = nullptr;     // [nc] compact index of (l, -m)
-  int KP = 0;              // K extent of the angular GEMM (l-triples padded to 32)
+  int KP = 0;              // K extent of the angular GEMM: l-triples (lambda = 0) or Fourier
+                           // pairs (lambda != 0), padded to 32; also the row stride of T hi / lo
   int NP = 0, nhalf = 0;   // unique grid points padded to 256 * nhalf
   int nsm = 0;             // SMs of the context's device (persistent angular grid)
+  bool hform = false;      // lambda != 0: the angular A operand is H (Fourier pairs), B the cosine table
   bool persist = true;     // angular stage: persistent kernel (true) or one CTA per tile
   const int* coff = nullptr;
   const PairBlock* pbs = nullptr;
@@ -208,11 +216,12 @@ cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMa
                               const RagInfo* rag = nullptr);
 cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, double* E, cudaStream_t s,
                                   const RagInfo* rag = nullptr);
-// Persistent angular stage: compensated partial sums into part ([n][klp][8] floats);
+// Persistent angular stage: compensated partial sums into part ([n][klp][4 nhalf] floats),
+// or (c3out) c3 rows [n][klength][2N^2];
 // launch_finalize_parts turns them into slab terms and their sum per proposal.
 cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n,
                                       const float* qt, float* part, int* err, bool tf32, cudaStream_t s,
-                                      const RagInfo* rag = nullptr);
+                                      const RagInfo* rag = nullptr, float* c3out = nullptr);
 cudaError_t launch_finalize_parts(const DevTables& t, const TcTables& tc, int n, const float* part, const double* Qs,
                                   double* E, cudaStream_t s, const RagInfo* rag = nullptr);
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
@@ -226,7 +235,7 @@ size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage)
 // [lt][ki] (shell triples contiguous), read by the angular kernel as an MN-major operand;
 // every other coupling form and the TF32 mode use [ki][lt].
 inline bool t_order_major(const TcTables& tc, bool tf32) {
-  return !tf32 && tc.use_fold >= 0 && tc.fold[tc.use_fold].ok;
+  return !tf32 && !tc.hform && tc.use_fold >= 0 && tc.fold[tc.use_fold].ok;
 }
 cudaError_t fold_configure();
 cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const FoldVariant& fv, int n, const float2* cc,

@@ -13,6 +13,8 @@
 //   * Bayes: per slab, Sp = sum_g max(c3, 1e-30) and Sql = sum_g q^[g] log max(c3, 1e-30)
 //     (q^ = the L1-normalised histogram slab); E = sum_ki tf (Qs log Sp - Sql), which
 //     equals sum_ki tf * (-sum_g q^ log p^) of correlations.jl:210-220 with Qs = sum_g q^.
+#include <cuda_bf16.h>
+
 #include "internal.h"
 
 #include <cstdint>
@@ -264,14 +266,16 @@ __global__ void __launch_bounds__(256) k_build_H(const float* __restrict__ T, in
                                                  int klength, float* __restrict__ H, int nqp, int64_t H_stride) {
   extern __shared__ float sm[];
   float* sY = sm;                      // [K][nc]
-  float* sT = sm + (size_t)K * nc;     // [32][n_ltp]
+  float* sT = sm + (size_t)K * nc;     // [32][n_ltp + 1]: an odd row stride keeps the lanes'
+                                       // reads of one l-triple in different banks
+  const int rs = n_ltp + 1;
   const int prop = blockIdx.z;
   const int ki0 = blockIdx.x * 32;
   for (int i = threadIdx.x; i < K * nc; i += blockDim.x) sY[i] = Ytab[i];
   const float* Tp = T + (int64_t)prop * T_stride;
   for (int i = threadIdx.x; i < 32 * n_ltp; i += blockDim.x) {
     const int r = i / n_ltp, c = i - r * n_ltp;
-    sT[i] = ki0 + r < klength ? Tp[(int64_t)(ki0 + r) * n_ltp + c] : 0.f;
+    sT[r * rs + c] = ki0 + r < klength ? Tp[(int64_t)(ki0 + r) * n_ltp + c] : 0.f;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -282,7 +286,7 @@ __global__ void __launch_bounds__(256) k_build_H(const float* __restrict__ T, in
   const float* y1 = sY + k.x * nc;
   const float* y2 = sY + k.y * nc;
   const float* y3 = sY + k.z * nc;
-  const float* trow = sT + lane * n_ltp;
+  const float* trow = sT + lane * rs;
   float acc = 0.f;
   for (int e = qstart[q]; e < qstart[q + 1]; ++e) {
     const int j = qlist[e];
@@ -293,7 +297,7 @@ __global__ void __launch_bounds__(256) k_build_H(const float* __restrict__ T, in
 }
 
 cudaError_t launch_build_H(const DevTables& t, int n, const float* T, float* H, cudaStream_t s) {
-  const size_t smem = ((size_t)t.K * t.nc + 32 * (size_t)t.n_ltp) * sizeof(float);
+  const size_t smem = ((size_t)t.K * t.nc + 32 * (size_t)(t.n_ltp + 1)) * sizeof(float);
   dim3 grid((t.klength + 31) / 32, (t.nq + 7) / 8, n);
   k_build_H<<<grid, 256, smem, s>>>(T, t.n_ltp, (int64_t)t.klp * t.n_ltp, t.Ytab, t.K, t.nc, t.w, t.idx, t.lt_of_j,
                                     t.qstart, t.qlist, t.nq, t.kl, t.klength, H, t.nqp, (int64_t)t.klp * t.nqp);
@@ -306,10 +310,167 @@ cudaError_t launch_finalize(const DevTables& t, int n, const double2* part, int 
   return cudaGetLastError();
 }
 
+// Tensor-core path at lambda != 0: the Fourier-pair operand H of a batch, written as the
+// angular kernel's split A operand.  grid: (klength, ceil(n / PB)); block kHWarps warps;
+// PB = 32 PPL proposals per block, PPL per lane.  One block = one shell triple ki:
+//   H[prop][ki][q] = sum_{j with (m2, m3) = +-q} T[prop][ki][lt(j)] w_j Y1 Y2 Y3,
+// the Legendre product of entry j at the triple's three shells formed once per block and
+// applied to all PB proposals.  T rows are staged transposed (l-triple major, proposals
+// fastest, row stride PB + 2 or PB + 1 so the lanes' loads and the transposing stores
+// stay in distinct banks), with the triple's three Legendre rows.  Warps take pairs q;
+// per pair, the lanes first form the products of up to kHChunk entries (independent
+// 16-byte entry loads, packed indices / w / l-triple in pair order) into the warp's
+// buffer, then stream them as broadcasts against the staged T.  Results go through a
+// 64-pair tile in shared memory and leave as rows of consecutive pairs, split into
+// hi + lo (bf16, or tf32-rounded fp32 + fp32 remainder).  Pair columns nq..KP-1 are zero.
+constexpr int kHWarps = 16;
+constexpr int kHChunk = 128;
+
+template <int PPL>
+__global__ void __launch_bounds__(kHWarps * 32, 1) k_build_H_split(
+    const float* __restrict__ T32, int ldT, int64_t Tstride, int n, int n_lt, const float* __restrict__ Ytab, int nc,
+    const int4* __restrict__ qent, const int* __restrict__ qstart, int nq, const int4* __restrict__ kl, int klp, int KP,
+    int tf32, void* __restrict__ Hhi, void* __restrict__ Hlo) {
+  constexpr int PB = 32 * PPL;
+  constexpr int RS = PB + (PPL == 2 ? 2 : 1);
+  constexpr int HS = PB + 1;
+  extern __shared__ float smh[];
+  float* Ts = smh;                     // [n_lt][RS]
+  float* Hs = Ts + (size_t)n_lt * RS;  // [64][HS]
+  // [kHWarps][kHChunk] (P, T-row offset bits), 16-byte aligned for the float4 reads
+  float2* Pb = reinterpret_cast<float2*>(smh + (((size_t)n_lt * RS + 64 * HS + 3) & ~(size_t)3));
+  float* Ys = reinterpret_cast<float*>(Pb + kHWarps * kHChunk);  // [3][nc]
+  const int ki = blockIdx.x, p0 = blockIdx.y * PB;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int4 k = kl[ki];
+  for (int i = threadIdx.x; i < 3 * nc; i += blockDim.x) {
+    const int r = i / nc, cix = i - r * nc;
+    Ys[i] = Ytab[(size_t)(r == 0 ? k.x : r == 1 ? k.y : k.z) * nc + cix];
+  }
+  for (int i = threadIdx.x; i < n_lt * PB; i += blockDim.x) {
+    const int pr = i / n_lt, l = i - pr * n_lt;
+    Ts[l * RS + pr] = p0 + pr < n ? T32[(int64_t)(p0 + pr) * Tstride + (int64_t)ki * ldT + l] : 0.f;
+  }
+  __syncthreads();
+  float2* pw = Pb + warp * kHChunk;
+  for (int qb = 0; qb < KP; qb += 64) {
+    for (int qq = warp; qq < 64; qq += kHWarps) {
+      const int q = qb + qq;
+      // two accumulator sets (even / odd entries) per proposal of the lane
+      float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+      if (q < nq) {
+        const int e1 = qstart[q + 1];
+        for (int e0 = qstart[q]; e0 < e1; e0 += kHChunk) {
+          const int cnt = min(kHChunk, e1 - e0);
+          const int cnt8 = (cnt + 7) & ~7;
+          // products and the l-triple's T-row offset (in floats); padding entries are 0
+#pragma unroll 4
+          for (int i = lane; i < cnt8; i += 32) {
+            float P = 0.f;
+            int off = 0;
+            if (i < cnt) {
+              const int4 en = qent[e0 + i];
+              const uint32_t id = (uint32_t)en.x;
+              P = __int_as_float(en.y) * Ys[id & 1023u] * Ys[nc + ((id >> 10) & 1023u)] *
+                  Ys[2 * nc + ((id >> 20) & 1023u)];
+              off = en.z * RS;
+            }
+            pw[i] = make_float2(P, __int_as_float(off));
+          }
+          __syncwarp();
+          const float4* pw4 = reinterpret_cast<const float4*>(pw);
+          for (int i = 0; i < cnt8; i += 8) {
+            float pv[8];
+            int po[8];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float4 v = pw4[i / 2 + u];
+              pv[2 * u] = v.x;
+              po[2 * u] = __float_as_int(v.y);
+              pv[2 * u + 1] = v.z;
+              po[2 * u + 1] = __float_as_int(v.w);
+            }
+            if (PPL == 2) {
+              float2 tv[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) tv[u] = *reinterpret_cast<const float2*>(Ts + po[u] + 2 * lane);
+#pragma unroll
+              for (int u = 0; u < 8; u += 2) {
+                a0 = fmaf(pv[u], tv[u].x, a0);
+                a1 = fmaf(pv[u], tv[u].y, a1);
+                b0 = fmaf(pv[u + 1], tv[u + 1].x, b0);
+                b1 = fmaf(pv[u + 1], tv[u + 1].y, b1);
+              }
+            } else {
+              float tv[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) tv[u] = Ts[po[u] + lane];
+#pragma unroll
+              for (int u = 0; u < 8; u += 2) {
+                a0 = fmaf(pv[u], tv[u], a0);
+                b0 = fmaf(pv[u + 1], tv[u + 1], b0);
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      Hs[qq * HS + PPL * lane] = a0 + b0;
+      if (PPL == 2) Hs[qq * HS + 2 * lane + 1] = a1 + b1;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < PB * 64; i += blockDim.x) {
+      const int pr = i >> 6, qq = i & 63, q = qb + qq;
+      if (p0 + pr >= n || q >= KP) continue;
+      const float v = q < nq ? Hs[qq * HS + pr] : 0.f;
+      const size_t o = ((size_t)(p0 + pr) * klp + ki) * KP + q;
+      if (tf32) {
+        uint32_t h;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+        const float hf = __uint_as_float(h);
+        reinterpret_cast<float*>(Hhi)[o] = hf;
+        reinterpret_cast<float*>(Hlo)[o] = v - hf;
+      } else {
+        const __nv_bfloat16 hb = __float2bfloat16_rn(v);
+        reinterpret_cast<__nv_bfloat16*>(Hhi)[o] = hb;
+        reinterpret_cast<__nv_bfloat16*>(Hlo)[o] = __float2bfloat16_rn(v - __bfloat162float(hb));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+size_t build_H_split_smem(const DevTables& t, int ppl) {
+  const int PB = 32 * ppl;
+  const size_t pbo = ((size_t)t.n_lt * (PB + (ppl == 2 ? 2 : 1)) + 64 * (size_t)(PB + 1) + 3) & ~(size_t)3;
+  return (pbo + 2 * (size_t)kHWarps * kHChunk + 3 * (size_t)t.nc) * sizeof(float);
+}
+
+cudaError_t launch_build_H_split(const DevTables& t, int KP, int n, const float* T32, void* Hhi, void* Hlo, bool tf32,
+                                 cudaStream_t s) {
+  const int ppl = build_H_split_smem(t, 2) <= (size_t)kPlainMaxSmem ? 2 : 1;
+  const size_t smem = build_H_split_smem(t, ppl);
+  if (smem > (size_t)kPlainMaxSmem) return cudaErrorInvalidConfiguration;
+  const dim3 grid(t.klength, (n + 32 * ppl - 1) / (32 * ppl));
+  const int64_t Ts = (int64_t)t.klp * t.n_ltp;
+  if (ppl == 2)
+    k_build_H_split<2><<<grid, kHWarps * 32, smem, s>>>(T32, t.n_ltp, Ts, n, t.n_lt, t.Ytab, t.nc, t.qent, t.qstart,
+                                                        t.nq, t.kl, t.klp, KP, tf32 ? 1 : 0, Hhi, Hlo);
+  else
+    k_build_H_split<1><<<grid, kHWarps * 32, smem, s>>>(T32, t.n_ltp, Ts, n, t.n_lt, t.Ytab, t.nc, t.qent, t.qstart,
+                                                        t.nq, t.kl, t.klp, KP, tf32 ? 1 : 0, Hhi, Hlo);
+  return cudaGetLastError();
+}
+
 cudaError_t plain_configure() {
-  cudaError_t e = cudaFuncSetAttribute(k_couple_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, kPlainMaxSmem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_build_H, cudaFuncAttributeMaxDynamicSharedMemorySize, kPlainMaxSmem);
+  const cudaFuncAttribute ds = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_couple_direct, ds, kPlainMaxSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_build_H, ds, kPlainMaxSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_build_H_split<1>, ds, kPlainMaxSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_build_H_split<2>, ds, kPlainMaxSmem)) != cudaSuccess)
+    return e;
+  return cudaSuccess;
 }
 
 }  // namespace tp3

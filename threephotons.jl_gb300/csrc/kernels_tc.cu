@@ -789,13 +789,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tc(
 // while the MMA warp fills the other.  tmem_full[b] (one arrival, tcgen05.commit) hands
 // a buffer to the epilogue; tmem_empty[b] (one arrival per epilogue warp) hands it back.
 // The epilogue writes compensated partial sums per (row, half, column block) to
-// part [prop][klp][2 halves][2 blocks][Sp, Sql]; k_finalize_parts forms the slab terms.
-template <bool TF32, bool AMN>
+// part [prop][klp][nhalf halves][2 blocks][Sp, Sql]; k_finalize_parts forms the slab
+// terms.  STORE: the epilogue writes c3 instead (all images of every unique point).
+// Any number of halves (the unfolded 2N^2-point grid of lambda != 0 has 8 at N = 32).
+template <bool STORE, bool TF32, bool AMN>
 __global__ void __launch_bounds__(kThreads, 1) k_angular_tp(
     const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
     const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, int klp, int KP,
     int Gu, int nhalf, int nunits, const float* __restrict__ qt, float* __restrict__ part, int* __restrict__ err,
-    const RagInfo* __restrict__ rag) {
+    const RagInfo* __restrict__ rag, int klength, float* __restrict__ c3out, const int* __restrict__ u_to_g, int N,
+    int mult) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t tmem_empty[2];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -936,15 +939,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tp(
       const int b = i & 1;
       if (!mbar_wait(&hd->tmem_full[b], (uint32_t)((i >> 1) & 1), abort_flag, err)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const float* qrow = qt + (rag ? (size_t)rag[prop].hist * klp * Gu : 0) + ((size_t)mtile * Gu) * kBM + r;
+      const float* qrow =
+          STORE ? nullptr : qt + (rag ? (size_t)rag[prop].hist * klp * Gu : 0) + ((size_t)mtile * Gu) * kBM + r;
+      const int ki = mtile * kBM + r;
       float sp = 0.f, sq = 0.f, csp = 0.f, csq = 0.f;
       for (int cc = 0; cc < 4; ++cc) {
         const int col = cblk * 128 + cc * 32;  // column inside the half
         const int u0 = h * kBN + col;          // unique grid point of column 0
+        float v[32];
+        if (STORE) {
+          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * kBN + col), v);
+          if (ki < klength) {
+            float* o = c3out + ((size_t)prop * klength + ki) * (size_t)(2 * N * N);
+#pragma unroll 4
+            for (int j = 0; j < 32; ++j) {
+              const int u = u0 + j;
+              if (u < Gu) {
+                const int g = u_to_g[u];
+                const int a = g % N, bb = g / N;
+                o[g] = v[j];
+                if (mult == 4) {
+                  o[a + N * (bb + N)] = v[j];
+                  o[(N - 1 - a) + N * (N - 1 - bb)] = v[j];
+                  o[(N - 1 - a) + N * (2 * N - 1 - bb)] = v[j];
+                }
+              }
+            }
+          }
+          continue;
+        }
         float q[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) q[j] = u0 + j < Gu ? qrow[(size_t)(u0 + j) * kBM] : 0.f;
-        float v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * kBN + col), v);
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -964,8 +990,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_angular_tp(
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tmem_empty[b])) : "memory");
-      reinterpret_cast<float2*>(part)[((size_t)prop * klp + mtile * kBM + r) * 4 + h * 2 + cblk] =
-          make_float2(sp - csp, sq - csq);
+      if (!STORE)
+        reinterpret_cast<float2*>(part)[(((size_t)prop * klp + ki) * nhalf + h) * 2 + cblk] =
+            make_float2(sp - csp, sq - csq);
       ++i;
     }
   }
@@ -1014,7 +1041,8 @@ __global__ void __launch_bounds__(256) k_finalize_slabs(const double* __restrict
 }
 
 // grid: n; block 256.  Slab terms tf (Qs log(mult Sp) - Sql) from the persistent
-// kernel's partial sums (FP64 from here on), then the same compensated sum.
+// kernel's partial sums [klp][nhalf][2][2] per proposal (FP64 from here on), then the
+// same compensated sum.
 __global__ void __launch_bounds__(256) k_finalize_parts(const float* __restrict__ part, int klp, int klength,
                                                         int nhalf, const double* __restrict__ Qs,
                                                         const double* __restrict__ tf, int mult,
@@ -1026,15 +1054,14 @@ __global__ void __launch_bounds__(256) k_finalize_parts(const float* __restrict_
     nk = rag[prop].klen;
     Qs += (size_t)rag[prop].hist * klength;
   }
-  const float4* p4 = reinterpret_cast<const float4*>(part) + (size_t)prop * klp * 2;
+  const float4* p4 = reinterpret_cast<const float4*>(part) + (size_t)prop * klp * nhalf;
   double s = 0.0, c = 0.0;
   for (int ki = threadIdx.x; ki < nk; ki += blockDim.x) {
-    const float4 a = p4[(size_t)ki * 2];  // half 0: (Sp, Sql) of column blocks 0 and 1
-    double Sp = (double)a.x + (double)a.z, Sq = (double)a.y + (double)a.w;
-    if (nhalf == 2) {
-      const float4 b = p4[(size_t)ki * 2 + 1];
-      Sp += (double)b.x + (double)b.z;
-      Sq += (double)b.y + (double)b.w;
+    double Sp = 0.0, Sq = 0.0;
+    for (int h = 0; h < nhalf; ++h) {
+      const float4 a = p4[(size_t)ki * nhalf + h];  // (Sp, Sql) of column blocks 0 and 1
+      Sp += (double)a.x + (double)a.z;
+      Sq += (double)a.y + (double)a.w;
     }
     const double e = tf[ki] * (Qs[ki] * log((double)mult * Sp) - Sq);
     double t, err;
@@ -1071,9 +1098,12 @@ cudaError_t tc_configure() {
       (e = cudaFuncSetAttribute(k_angular_tc<true, true, false>, ds, smem)) != cudaSuccess ||
       (e = cudaFuncSetAttribute(k_angular_tc<false, false, true>, ds, smem)) != cudaSuccess ||
       (e = cudaFuncSetAttribute(k_angular_tc<true, false, true>, ds, smem)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tp<false, false>, ds, smem)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tp<true, false>, ds, smem)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_angular_tp<false, true>, ds, smem)) != cudaSuccess)
+      (e = cudaFuncSetAttribute(k_angular_tp<false, false, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<false, true, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<false, false, true>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<true, false, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<true, true, false>, ds, smem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_angular_tp<true, false, true>, ds, smem)) != cudaSuccess)
     return e;
   const int cs = kCoupleMaxDynSmem, css = kCoupleSmallSmem;
 #define TP3_CP_ATTR(S, W)                                                                                    \
@@ -1177,6 +1207,10 @@ cudaError_t launch_couple_pair(const DevTables& t, const TcTables& tc, int n, co
 cudaError_t launch_angular_tc(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n, const float* qt,
                               const double* Qs, double* Eslab, float* c3out, int* err, bool tf32, cudaStream_t s,
                               const RagInfo* rag) {
+  // more than two grid halves do not fit one CTA's TMEM: the persistent kernel walks them
+  if (tc.nhalf > 2)
+    return c3out ? launch_angular_persistent(t, tc, maps, n, qt, nullptr, err, tf32, s, rag, c3out)
+                 : cudaErrorInvalidValue;
   dim3 grid(t.klp / kBM, n);
   const size_t smem = tc_smem_bytes();
   const bool amn = t_order_major(tc, tf32);
@@ -1205,17 +1239,24 @@ cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, doubl
 
 cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n,
                                       const float* qt, float* part, int* err, bool tf32, cudaStream_t s,
-                                      const RagInfo* rag) {
+                                      const RagInfo* rag, float* c3out) {
   const int nunits = n * (t.klp / kBM) * tc.nhalf;
   const int ctas = std::max(1, std::min(nunits, tc.nsm));
   const size_t smem = tc_smem_bytes();
   const bool amn = t_order_major(tc, tf32);
-#define TP3_ANGP(TF, MN, AH, AL)                                                                                     \
-  k_angular_tp<TF, MN><<<ctas, kThreads, smem, s>>>(AH, AL, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, tc.nhalf, nunits, \
-                                                    qt, part, err, rag)
-  if (tf32) TP3_ANGP(true, false, maps.a_hi, maps.a_lo);
-  else if (amn) TP3_ANGP(false, true, maps.a_hi_mn, maps.a_lo_mn);
-  else TP3_ANGP(false, false, maps.a_hi, maps.a_lo);
+#define TP3_ANGP(ST, TF, MN, AH, AL)                                                                          \
+  k_angular_tp<ST, TF, MN><<<ctas, kThreads, smem, s>>>(AH, AL, maps.b_hi, maps.b_lo, t.klp, tc.KP, t.Gu, tc.nhalf, \
+                                                        nunits, qt, part, err, rag, t.klength, c3out, t.u_to_g, t.N,  \
+                                                        t.mult)
+  if (c3out) {
+    if (tf32) TP3_ANGP(true, true, false, maps.a_hi, maps.a_lo);
+    else if (amn) TP3_ANGP(true, false, true, maps.a_hi_mn, maps.a_lo_mn);
+    else TP3_ANGP(true, false, false, maps.a_hi, maps.a_lo);
+  } else {
+    if (tf32) TP3_ANGP(false, true, false, maps.a_hi, maps.a_lo);
+    else if (amn) TP3_ANGP(false, false, true, maps.a_hi_mn, maps.a_lo_mn);
+    else TP3_ANGP(false, false, false, maps.a_hi, maps.a_lo);
+  }
 #undef TP3_ANGP
   return cudaGetLastError();
 }
