@@ -60,6 +60,11 @@ extern "C" {
 #define TP3_MODE_PLAIN_FP32 0    /* direct coupling + FP32 SIMT angular contraction, full grid */
 #define TP3_MODE_TC_BF16X3 1     /* pair-factorised coupling + tcgen05 BF16 hi/lo x3 */
 #define TP3_MODE_TC_TF32X3 2     /* pair-factorised coupling + tcgen05 TF32 hi/lo x3 */
+/* At lambda != 0 the tensor-core modes contract over Fourier pairs (m2, m3): the coupling
+ * also writes FP32 T, a SIMT kernel forms H[ki][(m2, m3)] = sum_j T w_j Y1 Y2 Y3 with the
+ * shells' Legendre factors (src/correlations.jl:137-148), and the persistent tcgen05
+ * kernel contracts H with cos(m2 alpha + m3 beta) on the full N x 2N grid; ragged
+ * batches and the per-tile angular schedule above 512 grid points need lambda = 0. */
 #define TP3_MODE_AUTO (-1)       /* fastest available mode for this shape */
 
 typedef struct tp3_ctx tp3_ctx;

@@ -192,3 +192,14 @@ def test_kat6_lambda_forms_agree(config1):
     c3r = c3_reference_form(b, config1["coeff"], B32, P32)
     c3q = c3_pair_form(b, config1["coeff"])
     assert np.abs(c3r - c3q).sum() / np.abs(c3q).sum() < 1e-6
+
+
+def test_pair_form_vectorised_equals_loop_form(config1):
+    """The chunked pair form used at the production shape equals the per-entry loop form."""
+    import math
+    from oracle.c3 import c3_pair_form, c3_pair_form_fast, triple_products
+    p = config1["params"]
+    b = enumerate_basis(p["L"], p["LMAX"], p["N"], p["K"], lam=2.5, dq=math.pi / 8)
+    c3q = c3_pair_form(b, config1["coeff"])
+    c3v = c3_pair_form_fast(b, triple_products(b, config1["coeff"]), chunk=333)
+    assert np.abs(c3q - c3v).max() / np.abs(c3q).max() < 1e-13
