@@ -154,8 +154,19 @@ int tp3_triple_products(tp3_ctx* ctx, const double* coeff, float* out);
 
 /* Bayes energy of one coefficient set. */
 int tp3_energy(tp3_ctx* ctx, const double* coeff, double* E);
-/* Bayes energies of n coefficient sets stored back to back (n * K * LMAX^2 complex). */
+/* Bayes energies of n coefficient sets stored back to back (n * K * LMAX^2 complex).
+ * Where the device reads pageable host memory through the host page tables (Grace
+ * systems with NVLink-C2C), a kernel fetches the coefficients the path uses (even
+ * l <= L) straight from coeffs; elsewhere the host packs them into pinned memory and
+ * copies them (tp3_set_host_input chooses).  coeffs must stay valid until the call
+ * returns, which it does after the energies are in E. */
 int tp3_energy_batch(tp3_ctx* ctx, int n, const double* coeffs, double* E);
+/* How tp3_energy_batch reaches host coefficients (no reference counterpart):
+ * TP3_HOST_INPUT_DIRECT (default where the device supports it) or TP3_HOST_INPUT_STAGED
+ * (host packing + one pinned copy).  Both give identical energies. */
+#define TP3_HOST_INPUT_STAGED 0
+#define TP3_HOST_INPUT_DIRECT 1
+int tp3_set_host_input(tp3_ctx* ctx, int mode);
 /* Same with device pointers: d_coeffs = n * K * LMAX^2 complex doubles in device
  * memory, d_E = n doubles in device memory.  Asynchronous on the context stream. */
 int tp3_energy_batch_device(tp3_ctx* ctx, int n, const void* d_coeffs, void* d_E);

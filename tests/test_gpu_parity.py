@@ -211,6 +211,25 @@ def test_angular_schedules_agree(basis1, config1, config1_hist, mode, form):
         assert Ep[i] == pytest.approx(e64, rel=1e-6)
 
 
+def test_host_input_routes_agree(basis1, config1, config1_hist):
+    """tp3_energy_batch reading the host array in place (where the device reads pageable
+    host memory) and through host packing + a pinned copy give identical energies."""
+    basis1.set_mode(tp3.TP3_MODE_TC_BF16X3)
+    basis1.set_histogram(config1_hist)
+    rng = np.random.default_rng(13)
+    coeffs = np.stack([config1["coeff"] * (1 + 0.03 * rng.normal(size=config1["coeff"].shape)) for _ in range(70)])
+    basis1.set_host_input(tp3.TP3_HOST_INPUT_STAGED)
+    Es = basis1.energy_batch(coeffs)
+    try:
+        basis1.set_host_input(tp3.TP3_HOST_INPUT_DIRECT)
+    except tp3.TP3Error:
+        pytest.skip("this device does not read pageable host memory")
+    Ed = basis1.energy_batch(coeffs)
+    np.testing.assert_array_equal(Ed, Es)
+    with pytest.raises(tp3.TP3Error):
+        basis1.set_host_input(5)
+
+
 def test_angular_schedule_argument_checked(basis1):
     with pytest.raises(tp3.TP3Error):
         basis1.set_angular(2)

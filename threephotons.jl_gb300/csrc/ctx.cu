@@ -716,6 +716,18 @@ __global__ void k_rag_info(const int* __restrict__ lkh, int n, int Lmax, int Kma
   out[i] = r;
 }
 
+// The coefficients the kernels use (even l <= L of every shell), read in place from the
+// caller's [n][K][LMAX^2] buffer -- host memory the device reaches through the host page
+// tables -- into the compact device layout [n][K][nc]; one thread per value, so every
+// read of a batch is in flight at once.
+__global__ void k_stage_coeff(const double2* __restrict__ src, int64_t total, int nc, int ncoef,
+                              const int* __restrict__ csean, double2* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % nc);
+    dst[i] = src[(i / nc) * ncoef + csean[c]];
+  }
+}
+
 }  // namespace
 
 int tp3::ctx_fail(tp3_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
@@ -788,6 +800,14 @@ int tp3_ctx_create(int L, int LMAX, int N, int K, double lambda, double dq, tp3_
   }
   tp3_ctx* c = new tp3_ctx();
   cudaGetDevice(&c->device);
+  {  // kernels may read pageable host buffers in place only where the device says so
+    int pa = 0, pt = 0;
+    cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, c->device);
+    cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->device);
+    cudaGetLastError();
+    c->pageable_ok = pa == 1 && pt == 1;
+    c->host_direct = c->pageable_ok;
+  }
   std::string m = tp3::build_basis(c->b, L, LMAX, N, K, lambda, dq);
   if (!m.empty()) { delete c; return fail(nullptr, TP3_ERR_ARG, m); }
   Basis& b = c->b;
@@ -1364,7 +1384,15 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
   double2* pin = (double2*)c->h_coeff;
   double2* dev = c->d_coeff;
   cudaError_t e;
-  for (int p0 = 0; p0 < n; p0 += per) {
+  if (c->host_direct) {
+    // the device reads the caller's buffer in place: no host packing and no staging copy
+    const int64_t total = (int64_t)n * t.K * t.nc;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 65535);
+    k_stage_coeff<<<blocks, 256, 0, c->stream>>>(src, total, t.nc, (int)ncoef, t.csean, dev);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "stage coefficients");
+    if (int r = run_energy(c, n, dev, c->d_E, true)) return r;
+  }
+  for (int p0 = 0; p0 < n && !c->host_direct; p0 += per) {
     const int m = std::min(per, n - p0);
     // host threads pack the proposals of a chunk (the previous chunk's kernels run meanwhile)
 #pragma omp parallel for schedule(static) if (m >= 8)
@@ -1389,6 +1417,15 @@ int tp3_energy_batch(tp3_ctx* c, int n, const double* coeffs, double* E) {
 }
 
 int tp3_energy(tp3_ctx* c, const double* coeff, double* E) { return tp3_energy_batch(c, 1, coeff, E); }
+
+int tp3_set_host_input(tp3_ctx* c, int mode) {
+  if (int r = check_ctx(c)) return r;
+  if (mode != TP3_HOST_INPUT_STAGED && mode != TP3_HOST_INPUT_DIRECT) return fail(c, TP3_ERR_ARG, "unknown host input mode");
+  if (mode == TP3_HOST_INPUT_DIRECT && !c->pageable_ok)
+    return fail(c, TP3_ERR_UNSUPPORTED, "the device cannot read pageable host memory");
+  c->host_direct = mode == TP3_HOST_INPUT_DIRECT;
+  return TP3_OK;
+}
 
 int tp3_energy_batch_device(tp3_ctx* c, int n, const void* d_coeffs, void* d_E) {
   if (int r = check_ctx(c)) return r;

@@ -80,6 +80,8 @@ struct tp3_ctx {
   // profiling: event pairs around each launch of the angular + Bayes kernel (ev) and
   // of the coupling kernel of the tensor-core path (ev_c)
   bool prof = false;
+  bool pageable_ok = false;    // the device reads pageable host memory through the host page tables
+  bool host_direct = false;    // tp3_energy_batch reads the caller's buffer in place
   std::vector<cudaEvent_t> ev;  // pairs
   size_t ev_used = 0;
   std::vector<cudaEvent_t> ev_c;

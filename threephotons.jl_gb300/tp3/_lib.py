@@ -37,6 +37,8 @@ TP3_MOVE_LEARNED = 2
 TP3_MOVE_DRIFT = 3
 TP3_ANGULAR_TILE = 0
 TP3_ANGULAR_PERSISTENT = 1
+TP3_HOST_INPUT_STAGED = 0
+TP3_HOST_INPUT_DIRECT = 1
 TP3_SH_INTENSITY = 0
 TP3_SH_REFERENCE = 1
 
@@ -57,6 +59,7 @@ SIGNATURES = {
     "tp3_autotune": (c_int, [c_void_p, c_int, c_void_p, P(c_int)]),
     "tp3_set_coupling": (c_int, [c_void_p, c_int]),
     "tp3_set_angular": (c_int, [c_void_p, c_int]),
+    "tp3_set_host_input": (c_int, [c_void_p, c_int]),
     "tp3_structure_sh": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_int, c_void_p,
                                  c_void_p, c_void_p]),
     "tp3_set_histogram": (c_int, [c_void_p, c_void_p, c_int]),

@@ -167,6 +167,12 @@ class BasisTypeGB300:
         return [(int(rep[4 * i]), int(rep[4 * i + 1]), int(rep[4 * i + 2]), float(rep[4 * i + 3]))
                 for i in range(min(cap.value, 24))]
 
+    def set_host_input(self, mode: int) -> None:
+        """How energy_batch reaches host coefficients: TP3_HOST_INPUT_DIRECT (kernels read
+        the array in place; the default where the device reads pageable host memory) or
+        TP3_HOST_INPUT_STAGED (host packing + one pinned copy)."""
+        check(self._lib.tp3_set_host_input(self._ctx, mode), self._ctx)
+
     def set_angular(self, schedule: int) -> None:
         """Angular-stage schedule of the tensor-core path: TP3_ANGULAR_PERSISTENT
         (default) or TP3_ANGULAR_TILE."""
