@@ -74,31 +74,30 @@ __device__ __forceinline__ int fold_drow(int s, int s_lo, int l3min, bool sym) {
 // Phase-1 inner loop for one m3 pair: n1 values of m1, NE 3j columns (even count).
 // c1 / c2 point at this lane's shells in rows m1lo and m2(m1lo) of the first m3; the
 // second m3's c_k2 row is dps away; rows are ps apart.  w holds (w_a, w_b) per column.
+// Accumulators are packed over the m3 pair -- R[j] = (Re D_a, Re D_b), I[j] = (Im D_a,
+// Im D_b) of column j -- so each (w_a, w_b) half of a 16-byte load feeds one packed FMA
+// (fma.rn.f32x2: both lanes rounded as two fmaf, the same values as scalar FMAs).
 template <int NE>
 __device__ __forceinline__ void fold_p1(const float2* __restrict__ c1, const float2* __restrict__ c2, int dps, int ps,
-                                        int n1, const float* __restrict__ w, int rs2, float* ar0, float* ai0,
-                                        float* ar1, float* ai1) {
+                                        int n1, const float* __restrict__ w, int rs2, float2* R, float2* I) {
 #pragma unroll
-  for (int j = 0; j < NE; ++j) { ar0[j] = 0.f; ai0[j] = 0.f; ar1[j] = 0.f; ai1[j] = 0.f; }
+  for (int j = 0; j < NE; ++j) { R[j] = make_float2(0.f, 0.f); I[j] = make_float2(0.f, 0.f); }
 #pragma unroll 2
   for (int i = 0; i < n1; ++i) {
     const float2 a = c1[i * ps];
     const float2 b0 = c2[-i * ps];
     const float2 b1 = c2[-i * ps + dps];
-    const float x0r = fmaf(a.x, b0.x, -a.y * b0.y), x0i = fmaf(a.x, b0.y, a.y * b0.x);
-    const float x1r = fmaf(a.x, b1.x, -a.y * b1.y), x1i = fmaf(a.x, b1.y, a.y * b1.x);
+    const float2 xr = make_float2(fmaf(a.x, b0.x, -a.y * b0.y), fmaf(a.x, b1.x, -a.y * b1.y));
+    const float2 xi = make_float2(fmaf(a.x, b0.y, a.y * b0.x), fmaf(a.x, b1.y, a.y * b1.x));
     const float4* wr = reinterpret_cast<const float4*>(w + i * rs2);
 #pragma unroll
     for (int j2 = 0; j2 < NE / 2; ++j2) {
       const float4 wv = wr[j2];  // (w_a, w_b) of columns 2 j2 and 2 j2 + 1
-      ar0[2 * j2] = fmaf(wv.x, x0r, ar0[2 * j2]);
-      ai0[2 * j2] = fmaf(wv.x, x0i, ai0[2 * j2]);
-      ar1[2 * j2] = fmaf(wv.y, x1r, ar1[2 * j2]);
-      ai1[2 * j2] = fmaf(wv.y, x1i, ai1[2 * j2]);
-      ar0[2 * j2 + 1] = fmaf(wv.z, x0r, ar0[2 * j2 + 1]);
-      ai0[2 * j2 + 1] = fmaf(wv.z, x0i, ai0[2 * j2 + 1]);
-      ar1[2 * j2 + 1] = fmaf(wv.w, x1r, ar1[2 * j2 + 1]);
-      ai1[2 * j2 + 1] = fmaf(wv.w, x1i, ai1[2 * j2 + 1]);
+      const float2 w0 = make_float2(wv.x, wv.y), w1 = make_float2(wv.z, wv.w);
+      R[2 * j2] = __ffma2_rn(w0, xr, R[2 * j2]);
+      I[2 * j2] = __ffma2_rn(w0, xi, I[2 * j2]);
+      R[2 * j2 + 1] = __ffma2_rn(w1, xr, R[2 * j2 + 1]);
+      I[2 * j2 + 1] = __ffma2_rn(w1, xi, I[2 * j2 + 1]);
     }
   }
 }
@@ -108,8 +107,8 @@ __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2
                                               const float* w, int rs2, bool valid, int a, int s0a, int s0b,
                                               int s_hi, int s_lo, int l3min, int m3a, int m3b, bool sym, float2* Dw,
                                               int slot, int drows, int* err) {
-  float ar0[NE], ai0[NE], ar1[NE], ai1[NE];
-  fold_p1<NE>(c1, c2, dps, ps, n1, w, rs2, ar0, ai0, ar1, ai1);
+  float2 R[NE], I[NE];
+  fold_p1<NE>(c1, c2, dps, ps, n1, w, rs2, R, I);
   if (!valid) return;
 #pragma unroll
   for (int j = 0; j < NE; ++j) {
@@ -117,36 +116,46 @@ __device__ __forceinline__ void fold_p1_store(const float2* c1, const float2* c2
     if (s >= s_lo && s < s_hi) {
       const int l3 = l3min + 2 * s;
       const int r = fold_drow(s, s_lo, l3min, sym);
-      // real functions: T = 2 sum_{m3 >= 0} Re(D c) with the m3 = 0 term halved here
+      // real functions: T = 2 sum_{m3 >= 0} Re(D c) with the m3 = 0 term halved here;
+      // D is stored conjugated, (Re D, -Im D), for the packed phase-2 products
       const float h = (sym && m3a == 0) ? 0.5f : 1.f;
       const int ra = r + (sym ? m3a : m3a + l3), rb = r + (sym ? m3b : m3b + l3);
       if (s >= s0a && TP3_DCHECK(ra >= 0 && ra < drows && slot < ps, err))
-        Dw[ra * ps + slot] = make_float2(h * ar0[j], h * ai0[j]);
+        Dw[ra * ps + slot] = make_float2(h * R[j].x, -(h * I[j].x));
       if (s >= s0b && TP3_DCHECK(rb >= 0 && rb < drows && slot < ps, err))
-        Dw[rb * ps + slot] = make_float2(ar1[j], ai1[j]);
+        Dw[rb * ps + slot] = make_float2(R[j].y, -I[j].y);
     }
   }
 }
 
 // Phase-2 tile: acc[i][j] = Re sum_r D[row r][pair slot + i] cT[row r][shell + j] over the
 // cnt rows of one order (dp, cp at the order's first row; rows are rstride float4 apart).
+// D is stored conjugated, so (Re D, -Im D) * (Re c, Im c) lane by lane is a pair whose sum
+// is Re(D c): one packed FMA per (i, j) and row, the two lanes summed at the end.
 __device__ __forceinline__ void fold_tile(const float4* __restrict__ dp, const float4* __restrict__ cp, int rstride,
                                           int cnt, float (&acc)[4][4]) {
+  float2 a2[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4; ++j) a2[i][j] = make_float2(0.f, 0.f);
 #pragma unroll 2
   for (int r = 0; r < cnt; ++r) {
     const float4 d01 = dp[r * rstride], d23 = dp[r * rstride + 1];
     const float4 c01 = cp[r * rstride], c23 = cp[r * rstride + 1];
-    const float xr[4] = {d01.x, d01.z, d23.x, d23.z}, xi[4] = {d01.y, d01.w, d23.y, d23.w};
-    const float yr[4] = {c01.x, c01.z, c23.x, c23.z}, yi[4] = {c01.y, c01.w, c23.y, c23.w};
+    const float2 x[4] = {make_float2(d01.x, d01.y), make_float2(d01.z, d01.w), make_float2(d23.x, d23.y),
+                         make_float2(d23.z, d23.w)};
+    const float2 y[4] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w), make_float2(c23.x, c23.y),
+                         make_float2(c23.z, c23.w)};
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xr[i], yr[j], fmaf(-xi[i], yi[j], acc[i][j]));
+      for (int j = 0; j < 4; ++j) a2[i][j] = __ffma2_rn(x[i], y[j], a2[i][j]);
   }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = a2[i][j].x + a2[i][j].y;
 }
 
 // Tile (q2, q3) of a unit's tile index t (tiles of one k1 row: q2 = 0.., q3 <= q2).
