@@ -431,6 +431,8 @@ std::string setup_tc(tp3_ctx* c) {
       fv.wmax = wmx;
       fv.cmax = cmx;
       fv.stage = stage;
+      fv.maxne = 0;
+      for (const auto& pb : pbs) fv.maxne = std::max(fv.maxne, (pb.nl3 + 1) & ~1);
       fv.smem = tp3::fold_smem_bytes(fv.nw, ps, drows, wmx, cmx, stage);
       fv.ok = fv.smem <= fvs[v].budget;
     }

@@ -116,6 +116,7 @@ struct FoldVariant {
   bool ok = false;
   int nw = 0, drows = 0, ps = 0, wmax = 0, cmax = 0;
   int stage = 0;  // floats of a warp's staging row (1 + K(K+1)/2 shell triples, rounded to 4)
+  int maxne = 0;  // widest phase-1 column run of any block (even l3 count, rounded up to even)
   size_t smem = 0;
   const FoldBlock* blks = nullptr;
   const FoldRow* rows = nullptr;

@@ -169,7 +169,9 @@ __device__ __forceinline__ void fold_tile_of(int t, int& q2, int& q3) {
 // T layout: ltmaj = false: [prop][ki][lt] (row stride KP); ltmaj = true (BF16 only):
 // [prop][lt][ki] (row stride klp), written through a per-warp staging row of `stage`
 // floats so that each order's values of the unit's shell triples leave as contiguous runs.
-template <int NW>
+// MAXNE: the widest phase-1 column run compiled in (10 covers L <= 18); registers are sized
+// for it, so the narrower instance fits 13 warps without spilling.
+template <int NW, int MAXNE>
 __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff, const FoldBlock* __restrict__ blks,
     const FoldRow* __restrict__ rows, const float* __restrict__ wtab, const int2* __restrict__ chunks, int ps,
@@ -346,10 +348,16 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     fold_p1_store<NE>(c1, c2, dps, ps, fr.n1, w, 2 * fr.rs, valid, a, fr.s0a, fr.s0b, s_hi, s_lo, l3min, \
                       m3a, m3b, sym, Dw, slot, drows, err);                                              \
     break;
-          switch (ne) {
-            TP3_FOLD_P1(2) TP3_FOLD_P1(4) TP3_FOLD_P1(6) TP3_FOLD_P1(8)
-            TP3_FOLD_P1(10) TP3_FOLD_P1(12) TP3_FOLD_P1(14) TP3_FOLD_P1(16)
-            default: break;
+          if (ne <= 10) {
+            switch (ne) {
+              TP3_FOLD_P1(2) TP3_FOLD_P1(4) TP3_FOLD_P1(6) TP3_FOLD_P1(8) TP3_FOLD_P1(10)
+              default: break;
+            }
+          } else if constexpr (MAXNE > 10) {
+            switch (ne) {
+              TP3_FOLD_P1(12) TP3_FOLD_P1(14) TP3_FOLD_P1(16)
+              default: break;
+            }
           }
 #undef TP3_FOLD_P1
         }
@@ -561,9 +569,13 @@ size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage)
 cudaError_t fold_configure() {
   cudaError_t e;
   const int cs = kCoupleMaxDynSmem;
-  if ((e = cudaFuncSetAttribute(k_couple_fold<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<13>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs)) != cudaSuccess)
+  const cudaFuncAttribute ds = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if ((e = cudaFuncSetAttribute(k_couple_fold<7, 10>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<8, 10>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<13, 10>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<7, 16>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<8, 16>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<13, 16>, ds, cs)) != cudaSuccess)
     return e;
   return cudaSuccess;
 }
@@ -573,14 +585,15 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
                                const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
   const bool ltmaj = t_order_major(tc, tf32);
-#define TP3_FOLD_LAUNCH(NW)                                                                                      \
-  k_couple_fold<NW><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks,     \
-                                                   fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP, sym, \
-                                                   Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag, tc.err)
+#define TP3_FOLD_LAUNCH(NW, MX)                                                                                  \
+  k_couple_fold<NW, MX><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks, \
+                                                       fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP,   \
+                                                       sym, Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag, tc.err)
+  const bool narrow = fv.maxne <= 10;
   switch (fv.nw) {
-    case 7: TP3_FOLD_LAUNCH(7); break;
-    case 8: TP3_FOLD_LAUNCH(8); break;
-    case 13: TP3_FOLD_LAUNCH(13); break;
+    case 7: if (narrow) TP3_FOLD_LAUNCH(7, 10); else TP3_FOLD_LAUNCH(7, 16); break;
+    case 8: if (narrow) TP3_FOLD_LAUNCH(8, 10); else TP3_FOLD_LAUNCH(8, 16); break;
+    case 13: if (narrow) TP3_FOLD_LAUNCH(13, 10); else TP3_FOLD_LAUNCH(13, 16); break;
     default: return cudaErrorInvalidValue;
   }
 #undef TP3_FOLD_LAUNCH
