@@ -489,10 +489,9 @@ int ensure_cap(tp3_ctx* c, int n) {
       (e = cudaMalloc(&c->d_E, (size_t)n * sizeof(double))) != cudaSuccess ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Thi, tcb)) != cudaSuccess) ||
       (c->tc_ok && (e = cudaMalloc(&c->d_Tlo, tcb)) != cudaSuccess) ||
-      // per-slab terms (one CTA per tile) or 4 partial sums per grid half and shell triple
-      // (persistent)
-      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, (size_t)n *
-                                                    std::max<size_t>(t.klength, 2 * (size_t)c->tc.nhalf * t.klp) *
+      // per-slab terms [n][klength], then (persistent schedule) 4 partial sums per grid half
+      // and shell triple [n][klp][nhalf][4] floats
+      (c->tc_ok && (e = cudaMalloc(&c->d_Eslab, ((size_t)n * (t.klength + 2 * (size_t)c->tc.nhalf * t.klp) + 1) *
                                                     sizeof(double))) != cudaSuccess) ||
       (e = cudaMalloc(&c->d_sym, (size_t)n * sizeof(int))) != cudaSuccess ||
       (t.nqp > 0 && (e = cudaMalloc(&c->d_H, (size_t)n * t.klp * t.nqp * sizeof(float))) != cudaSuccess) ||
@@ -604,12 +603,13 @@ int run_energy(tp3_ctx* c, int n, const double2* d_coeff, double* d_E, bool comp
     const float* qt = rag ? c->d_qt_set : c->d_qt;
     const double* Qf = rag ? c->d_Qf_set : c->d_Qfold;
     if (c->tc.persist || c->tc.nhalf > 2) {
-      float* part = reinterpret_cast<float*>(c->d_Eslab);
+      // the partial sums start 16-byte aligned after the slab terms (float4 reads)
+      float* part = reinterpret_cast<float*>(c->d_Eslab + (((size_t)c->cap * t.klength + 1) & ~(size_t)1));
       if ((e = tp3::launch_angular_persistent(t, c->tc, tf ? c->maps32 : c->maps, n, qt, part, c->d_err, tf, c->stream,
                                               rag)) != cudaSuccess)
         return cuda_fail(c, e, "angular_persistent");
       if (pr) cudaEventRecord(b, c->stream);
-      if ((e = tp3::launch_finalize_parts(t, c->tc, n, part, Qf, d_E, c->stream, rag)) != cudaSuccess)
+      if ((e = tp3::launch_finalize_parts(t, c->tc, n, part, Qf, c->d_Eslab, d_E, c->stream, rag)) != cudaSuccess)
         return cuda_fail(c, e, "finalize_parts");
     } else {
       if ((e = tp3::launch_angular_tc(t, c->tc, tf ? c->maps32 : c->maps, n, qt, Qf, c->d_Eslab, nullptr, c->d_err,

@@ -219,12 +219,13 @@ cudaError_t launch_finalize_slabs(int n, int klength, const double* Eslab, doubl
                                   const RagInfo* rag = nullptr);
 // Persistent angular stage: compensated partial sums into part ([n][klp][4 nhalf] floats),
 // or (c3out) c3 rows [n][klength][2N^2];
-// launch_finalize_parts turns them into slab terms and their sum per proposal.
+// launch_finalize_parts turns them into slab terms (Eslab [n][klength]) and sums those
+// per proposal in a fixed order.
 cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, const TcMaps& maps, int n,
                                       const float* qt, float* part, int* err, bool tf32, cudaStream_t s,
                                       const RagInfo* rag = nullptr, float* c3out = nullptr);
 cudaError_t launch_finalize_parts(const DevTables& t, const TcTables& tc, int n, const float* part, const double* Qs,
-                                  double* E, cudaStream_t s, const RagInfo* rag = nullptr);
+                                  double* Eslab, double* E, cudaStream_t s, const RagInfo* rag = nullptr);
 size_t couple_split_smem_d(const DevTables& t, const TcTables& tc);
 size_t couple_split_smem_t(const DevTables& t, const TcTables& tc);
 cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);

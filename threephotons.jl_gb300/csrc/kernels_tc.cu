@@ -1040,48 +1040,29 @@ __global__ void __launch_bounds__(256) k_finalize_slabs(const double* __restrict
   if (threadIdx.x == 0) E[prop] = ss[0] + sc[0];
 }
 
-// grid: n; block 256.  Slab terms tf (Qs log(mult Sp) - Sql) from the persistent
-// kernel's partial sums [klp][nhalf][2][2] per proposal (FP64 from here on), then the
-// same compensated sum.
-__global__ void __launch_bounds__(256) k_finalize_parts(const float* __restrict__ part, int klp, int klength,
-                                                        int nhalf, const double* __restrict__ Qs,
-                                                        const double* __restrict__ tf, int mult,
-                                                        double* __restrict__ E, const RagInfo* __restrict__ rag) {
-  __shared__ double ss[256], sc[256];
-  const int prop = blockIdx.x;
+// grid: (ceil(klength / 256), n); block 256.  Slab terms tf (Qs log(mult Sp) - Sql) in
+// FP64 from the persistent kernel's partial sums [klp][nhalf][2][2] per proposal, one
+// thread per shell triple; k_finalize_slabs then adds them in its fixed order.
+__global__ void __launch_bounds__(256) k_slab_terms(const float* __restrict__ part, int klp, int klength, int nhalf,
+                                                    const double* __restrict__ Qs, const double* __restrict__ tf,
+                                                    int mult, double* __restrict__ Eslab,
+                                                    const RagInfo* __restrict__ rag) {
+  const int prop = blockIdx.y;
+  const int ki = blockIdx.x * blockDim.x + threadIdx.x;
   int nk = klength;
   if (rag) {
     nk = rag[prop].klen;
     Qs += (size_t)rag[prop].hist * klength;
   }
-  const float4* p4 = reinterpret_cast<const float4*>(part) + (size_t)prop * klp * nhalf;
-  double s = 0.0, c = 0.0;
-  for (int ki = threadIdx.x; ki < nk; ki += blockDim.x) {
-    double Sp = 0.0, Sq = 0.0;
-    for (int h = 0; h < nhalf; ++h) {
-      const float4 a = p4[(size_t)ki * nhalf + h];  // (Sp, Sql) of column blocks 0 and 1
-      Sp += (double)a.x + (double)a.z;
-      Sq += (double)a.y + (double)a.w;
-    }
-    const double e = tf[ki] * (Qs[ki] * log((double)mult * Sp) - Sq);
-    double t, err;
-    two_sum(s, e, t, err);
-    s = t;
-    c += err;
+  if (ki >= nk) return;
+  const float4* p4 = reinterpret_cast<const float4*>(part) + ((size_t)prop * klp + ki) * nhalf;
+  double Sp = 0.0, Sq = 0.0;
+  for (int h = 0; h < nhalf; ++h) {
+    const float4 a = p4[h];  // (Sp, Sql) of column blocks 0 and 1
+    Sp += (double)a.x + (double)a.z;
+    Sq += (double)a.y + (double)a.w;
   }
-  ss[threadIdx.x] = s;
-  sc[threadIdx.x] = c;
-  __syncthreads();
-  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-    if (threadIdx.x < h) {
-      double t, err;
-      two_sum(ss[threadIdx.x], ss[threadIdx.x + h], t, err);
-      ss[threadIdx.x] = t;
-      sc[threadIdx.x] += sc[threadIdx.x + h] + err;
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) E[prop] = ss[0] + sc[0];
+  Eslab[(size_t)prop * klength + ki] = tf[ki] * (Qs[ki] * log((double)mult * Sp) - Sq);
 }
 
 }  // namespace
@@ -1262,8 +1243,12 @@ cudaError_t launch_angular_persistent(const DevTables& t, const TcTables& tc, co
 }
 
 cudaError_t launch_finalize_parts(const DevTables& t, const TcTables& tc, int n, const float* part, const double* Qs,
-                                  double* E, cudaStream_t s, const RagInfo* rag) {
-  k_finalize_parts<<<n, 256, 0, s>>>(part, t.klp, t.klength, tc.nhalf, Qs, t.tf, t.mult, E, rag);
+                                  double* Eslab, double* E, cudaStream_t s, const RagInfo* rag) {
+  k_slab_terms<<<dim3((t.klength + 255) / 256, n), 256, 0, s>>>(part, t.klp, t.klength, tc.nhalf, Qs, t.tf, t.mult,
+                                                                 Eslab, rag);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_finalize_slabs<<<n, 256, 0, s>>>(Eslab, t.klength, E, rag);
   return cudaGetLastError();
 }
 
