@@ -60,7 +60,7 @@ METRIC = "c3+Bayes proposal evals/s at L18 K26 N32"
 UNIT = "proposals/s"
 MODE_NAMES = {0: "plain_fp32", 1: "tc_bf16x3", 2: "tc_tf32x3"}
 COUPLING_NAMES = {0: "fused_512", 1: "split", 2: "fused_256x2", 3: "warp_local", 4: "warp_local_256x2",
-                  5: "folded_8w", 6: "folded_7w", 7: "folded_13w"}
+                  5: "folded_8w", 6: "folded_7w", 7: "folded_13w", 8: "folded_14w_pairs"}
 ANGULAR_NAMES = {0: "tile", 1: "persistent"}
 ANGULAR_CODES = {v: k for k, v in ANGULAR_NAMES.items()}
 DTYPES = {0: "fp32", 1: "bf16x3 (fp32 accumulate)", 2: "tf32x3 (fp32 accumulate)"}
@@ -540,7 +540,7 @@ def main():
     ap.add_argument("--mode", default="auto", choices=["auto", "tuned", "plain", "tc", "tf32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="proposals", choices=["proposals", "ragged", "learned", "chains"])
-    ap.add_argument("--coupling", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6, 7],
+    ap.add_argument("--coupling", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6, 7, 8],
                     help="force a tensor-core coupling form (with --mode tc/tf32)")
     ap.add_argument("--angular", default="persistent", choices=["persistent", "tile"],
                     help="angular-stage schedule of the tensor-core path (with --mode tc/tf32)")

@@ -112,8 +112,9 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * with 256 threads, two CTAs per SM in 110 KB each where that fits, else one with up
  * to 225 KB; 1: two-kernel split coupling through global memory; 5, 6, 7: folded-row
  * coupling, warps owning folded pairs of k1 rows, at 8, 7 and 13 warps per CTA with the
- * largest per-warp D buffer that fits 225 KB; in BF16 mode it writes T order-major and
- * the angular kernel reads it MN-major) -- selects
+ * largest per-warp D buffer that fits 225 KB; 8: the same at 14 warps in pairs, the two
+ * warps of a pair sharing one unit and one D buffer (7 buffers); in BF16 mode it writes
+ * T order-major and the angular kernel reads it MN-major) -- selects
  * the fastest for this context and records it for the shape (L, LMAX, N, K, lambda,
  * dq) in the process, where TP3_MODE_AUTO finds it.  Every variant is timed with the
  * persistent angular schedule; the fastest tensor-core variant is then timed again
@@ -121,7 +122,7 @@ int tp3_get_mode(const tp3_ctx* ctx, int* mode);
  * up to *nreport rows of four values (mode, coupling form, angular schedule, ms per
  * proposal); *nreport returns the number of rows.  Synchronises. */
 int tp3_autotune(tp3_ctx* ctx, int n, double* report, int* nreport);
-/* Force a coupling form of the tensor-core path (0 to 7 as above). */
+/* Force a coupling form of the tensor-core path (0 to 8 as above). */
 int tp3_set_coupling(tp3_ctx* ctx, int form);
 /* Angular-stage schedule of the tensor-core path (no reference counterpart).
  * TP3_ANGULAR_PERSISTENT (default): one CTA per SM walks (proposal, 128-triple tile,

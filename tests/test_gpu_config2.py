@@ -43,7 +43,7 @@ def test_c3_and_energy_all_modes(prod):
     assert np.abs(ref - c3_64).sum() / np.abs(c3_64).sum() < 1e-7
     E64 = energy_bayes(c3_64, hist, K, N)
     variants = [(tp3.TP3_MODE_PLAIN_FP32, None)] + [(m, f) for m in (tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3)
-                                                    for f in (0, 1, 3, 4, 5, 6, 7)]
+                                                    for f in (0, 1, 3, 4, 5, 6, 7, 8)]
     for mode, form in variants:
         basis.set_mode(mode)
         if form is not None:

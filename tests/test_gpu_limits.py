@@ -32,7 +32,7 @@ def test_largest_shapes_agree_with_plain_path(L, LMAX, N, K):
         checked = 0
         for mode in (tp3.TP3_MODE_TC_BF16X3, tp3.TP3_MODE_TC_TF32X3):
             basis.set_mode(mode)
-            for form in range(8):
+            for form in range(9):
                 try:
                     basis.set_coupling(form)
                 except tp3.TP3Error:

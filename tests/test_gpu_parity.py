@@ -155,12 +155,12 @@ def test_errors_are_statuses(config1):
         tp3.calculate_basis(8, 8, 16, 8)  # LMAX must exceed L
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 @pytest.mark.parametrize("kind", ["general", "real_function"])
 def test_coupling_forms_agree(basis1, config1, config1_hist, form, kind):
     """Every coupling form the autotuner may pick (one-kernel 512 threads, split, one-kernel
     256 threads x 2 CTAs per SM, warp-local 512 threads, warp-local 256 threads x 2 CTAs
-    per SM, folded-row 8, 7 and 13 warps) gives the oracle's
+    per SM, folded-row 8, 7 and 13 warps and 14 warps in pairs) gives the oracle's
     triple products and the same energy."""
     basis1.set_mode(tp3.TP3_MODE_TC_BF16X3)
     basis1.set_coupling(form)

@@ -129,7 +129,7 @@ def test_precision_over_common_rotations(cfg_id):
             out["forms"] = {}
             for name, mode in (("tc_bf16x3", tp3.TP3_MODE_TC_BF16X3), ("tc_tf32x3", tp3.TP3_MODE_TC_TF32X3)):
                 basis.set_mode(mode)
-                for form in range(8):
+                for form in range(9):
                     try:
                         basis.set_coupling(form)
                     except tp3.TP3Error:

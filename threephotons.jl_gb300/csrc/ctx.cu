@@ -405,10 +405,12 @@ std::string setup_tc(tp3_ctx* c) {
       rows_gen = std::max(rows_gen, r);
     }
     const int ps = (b.K + 5 + 31) / 32 * 32;
-    const struct { int nw; size_t budget; } fvs[3] = {{8, (size_t)tp3::kCoupleMaxDynSmem},
-                                                      {7, (size_t)tp3::kCoupleMaxDynSmem},
-                                                      {13, (size_t)tp3::kCoupleMaxDynSmem}};
-    for (int v = 0; v < 3; ++v) {
+    // tilings: warps per CTA and warps per unit (the D buffers are nw / grp)
+    const struct { int nw, grp; size_t budget; } fvs[4] = {{8, 1, (size_t)tp3::kCoupleMaxDynSmem},
+                                                           {7, 1, (size_t)tp3::kCoupleMaxDynSmem},
+                                                           {13, 1, (size_t)tp3::kCoupleMaxDynSmem},
+                                                           {14, 2, (size_t)tp3::kCoupleMaxDynSmem}};
+    for (int v = 0; v < 4; ++v) {
       tp3::FoldVariant& fv = tc.fold[v];
       std::vector<tp3::FoldBlock> fbl;
       std::vector<tp3::FoldRow> frows;
@@ -417,8 +419,9 @@ std::string setup_tc(tp3_ctx* c) {
       int wmx = 0, cmx = 0;
       if (!tp3::build_fold_tables(pbs, rows_gen, fbl, frows, fw, fch, wmx, cmx).empty()) continue;
       const int stage = (1 + b.K * (b.K + 1) / 2 + 3) / 4 * 4;
-      const size_t fixed = tp3::fold_smem_bytes(fvs[v].nw, ps, 0, wmx, cmx, stage);
-      const size_t per_row = (size_t)(1 + fvs[v].nw) * ps * sizeof(float2);
+      const int ngroups = fvs[v].nw / fvs[v].grp;
+      const size_t fixed = tp3::fold_smem_bytes(ngroups, ps, 0, wmx, cmx, stage);
+      const size_t per_row = (size_t)(1 + ngroups) * ps * sizeof(float2);
       if (fixed + per_row > fvs[v].budget) continue;
       const int drows = (int)std::min<size_t>((size_t)rows_gen, (fvs[v].budget - fixed) / per_row);
       if (!tp3::build_fold_tables(pbs, drows, fbl, frows, fw, fch, wmx, cmx).empty()) continue;
@@ -426,6 +429,7 @@ std::string setup_tc(tp3_ctx* c) {
           (e = upload(c, fw, &fv.w)) != cudaSuccess || (e = upload(c, fch, &fv.chunks)) != cudaSuccess)
         return std::string("fold coupling tables: ") + cudaGetErrorString(e);
       fv.nw = fvs[v].nw;
+      fv.grp = fvs[v].grp;
       fv.drows = drows;
       fv.ps = ps;
       fv.wmax = wmx;
@@ -433,7 +437,7 @@ std::string setup_tc(tp3_ctx* c) {
       fv.stage = stage;
       fv.maxne = 0;
       for (const auto& pb : pbs) fv.maxne = std::max(fv.maxne, (pb.nl3 + 1) & ~1);
-      fv.smem = tp3::fold_smem_bytes(fv.nw, ps, drows, wmx, cmx, stage);
+      fv.smem = tp3::fold_smem_bytes(ngroups, ps, drows, wmx, cmx, stage);
       fv.ok = fv.smem <= fvs[v].budget;
     }
   }
@@ -660,7 +664,7 @@ int check_ctx(tp3_ctx* c) {
 void apply_coupling(tp3_ctx* c, int form) {
   TcTables& tc = c->tc;
   tc.use_fold = (form == 5 && tc.fold[0].ok) ? 0 : (form == 6 && tc.fold[1].ok) ? 1
-                 : (form == 7 && tc.fold[2].ok) ? 2 : -1;
+                 : (form == 7 && tc.fold[2].ok) ? 2 : (form == 8 && tc.fold[3].ok) ? 3 : -1;
   tc.use_small = form == 2 && tc.small_ok;
   tc.use_warp = form == 3 && tc.warp_ok;
   tc.use_warp2 = form == 4 && tc.warp2_ok;
@@ -1026,6 +1030,7 @@ int tp3_autotune(tp3_ctx* c, int n, double* report, int* nreport) {
       if (c->tc.fold[0].ok) vars.push_back({m, 5, true});
       if (c->tc.fold[1].ok) vars.push_back({m, 6, true});
       if (c->tc.fold[2].ok) vars.push_back({m, 7, true});
+      if (c->tc.fold[3].ok) vars.push_back({m, 8, true});
     }
   // synthetic real-function coefficients (c[l,-m] = (-1)^m conj c[l,m]), n sets
   const size_t nco = (size_t)b.K * b.LMAX * b.LMAX;
@@ -1158,8 +1163,9 @@ int tp3_set_coupling(tp3_ctx* c, int form) {
   if (!c->tc_ok) return fail(c, TP3_ERR_UNSUPPORTED, "tensor-core path unavailable: " + c->tc_why);
   const bool ok = (form == 0 && c->tc.fused_ok) || (form == 1 && c->tc.split_ok) || (form == 2 && c->tc.small_ok) ||
                   (form == 3 && c->tc.warp_ok) || (form == 4 && c->tc.warp2_ok) || (form == 5 && c->tc.fold[0].ok) ||
-                  (form == 6 && c->tc.fold[1].ok) || (form == 7 && c->tc.fold[2].ok);
-  if (!ok) return fail(c, form < 0 || form > 7 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
+                  (form == 6 && c->tc.fold[1].ok) || (form == 7 && c->tc.fold[2].ok) ||
+                  (form == 8 && c->tc.fold[3].ok);
+  if (!ok) return fail(c, form < 0 || form > 8 ? TP3_ERR_ARG : TP3_ERR_UNSUPPORTED, "coupling form not available");
   apply_coupling(c, form);
   return TP3_OK;
 }

@@ -117,6 +117,7 @@ struct FoldVariant {
   int nw = 0, drows = 0, ps = 0, wmax = 0, cmax = 0;
   int stage = 0;  // floats of a warp's staging row (1 + K(K+1)/2 shell triples, rounded to 4)
   int maxne = 0;  // widest phase-1 column run of any block (even l3 count, rounded up to even)
+  int grp = 1;    // warps per unit (each group of grp warps shares one D buffer)
   size_t smem = 0;
   const FoldBlock* blks = nullptr;
   const FoldRow* rows = nullptr;
@@ -127,8 +128,8 @@ struct FoldVariant {
 // Device tables of the tensor-core path.
 struct TcTables {
   // folded-row coupling tilings: [0] 8 warps, [1] 7 warps, [2] 13 warps (smaller D
-  // buffers, more l3 chunks), one CTA per SM
-  FoldVariant fold[3];
+  // buffers, more l3 chunks), [3] 14 warps in pairs sharing 7 D buffers; one CTA per SM
+  FoldVariant fold[4];
   int use_fold = -1;
   int* err = nullptr;  // the context's device error flag (index checks of TP3_DEBUG builds)
   int n_pb = 0, maxs = 0, SDmax = 0;
@@ -232,7 +233,8 @@ cudaError_t couple_split_configure(const DevTables& t, const TcTables& tc);
 std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std::vector<FoldBlock>& blks,
                               std::vector<FoldRow>& rows, std::vector<float>& w, std::vector<int2>& chunks,
                               int& wmax, int& cmax);
-size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage);
+// ngroups: D buffers and staging rows (warps per CTA / warps per unit)
+size_t fold_smem_bytes(int ngroups, int ps, int drows, int wmax, int cmax, int stage);
 // Layout of the T operand: the folded-row coupling in BF16 mode writes it order-major,
 // [lt][ki] (shell triples contiguous), read by the angular kernel as an MN-major operand;
 // every other coupling form and the TF32 mode use [ki][lt].

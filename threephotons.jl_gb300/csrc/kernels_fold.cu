@@ -158,6 +158,16 @@ __device__ __forceinline__ void fold_tile(const float4* __restrict__ dp, const f
     for (int j = 0; j < 4; ++j) acc[i][j] = a2[i][j].x + a2[i][j].y;
 }
 
+// Synchronise the G warps that share a unit: the warp itself (G = 1) or a named barrier
+// (id 1 + group) over the group's 32 G threads.
+template <int G>
+__device__ __forceinline__ void fold_gsync(int group) {
+  if (G == 1)
+    __syncwarp();
+  else
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(32 * G) : "memory");
+}
+
 // Tile (q2, q3) of a unit's tile index t (tiles of one k1 row: q2 = 0.., q3 <= q2).
 __device__ __forceinline__ void fold_tile_of(int t, int& q2, int& q3) {
   q2 = 0;
@@ -170,8 +180,12 @@ __device__ __forceinline__ void fold_tile_of(int t, int& q2, int& q3) {
 // [prop][lt][ki] (row stride klp), written through a per-warp staging row of `stage`
 // floats so that each order's values of the unit's shell triples leave as contiguous runs.
 // MAXNE: the widest phase-1 column run compiled in (10 covers L <= 18); registers are sized
-// for it, so the narrower instance fits 13 warps without spilling.
-template <int NW, int MAXNE>
+// for it, so the narrower instance fits 13 warps without spilling.  G: warps per unit.
+// With G = 2 the two warps of a group share one D buffer and one staging row: phase 1
+// splits the unit's m3 pairs between them (disjoint D rows), phase 2 its tiles and T runs,
+// with a named barrier between the steps; units go to groups in a fixed order.  That keeps
+// the D depth (hence l3 chunks) of NW / G buffers with NW warps hiding latency.
+template <int NW, int MAXNE, int G>
 __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
     const float2* __restrict__ cc, int K, int nc, const int* __restrict__ coff, const FoldBlock* __restrict__ blks,
     const FoldRow* __restrict__ rows, const float* __restrict__ wtab, const int2* __restrict__ chunks, int ps,
@@ -233,7 +247,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
   float* W = reinterpret_cast<float*>(C2 + (size_t)(cmax + 2) * ps);
   float2* cT = reinterpret_cast<float2*>(W + wmax);
   float2* Dall = cT + (size_t)drows * ps;
-  float* Stage = reinterpret_cast<float*>(Dall + (size_t)NW * drows * ps);  // [NW][stage]
+  constexpr int NG = NW / G;  // unit groups, each with a D buffer and a staging row
+  float* Stage = reinterpret_cast<float*>(Dall + (size_t)NG * drows * ps);  // [NG][stage]
   const float2* src = cc + (size_t)prop * K * nc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   {
@@ -271,8 +286,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
   const int nch = sym ? fb.nch_sym : fb.nch_gen;
   if (threadIdx.x < kFoldMaxChunks) s_next[threadIdx.x] = 0;
 
-  float2* Dw = Dall + (size_t)warp * drows * ps;
-  float* Ts = Stage + (size_t)warp * stage;
+  const int group = warp / G, sub = warp - group * G;
+  float2* Dw = Dall + (size_t)group * drows * ps;
+  float* Ts = Stage + (size_t)group * stage;
   const size_t tbase = (size_t)prop * klp * KP;
   void* ThiP = tf32out ? (void*)((float*)Thi + tbase) : (void*)((__nv_bfloat16*)Thi + tbase);
   void* TloP = tf32out ? (void*)((float*)Tlo + tbase) : (void*)((__nv_bfloat16*)Tlo + tbase);
@@ -304,10 +320,14 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
       fold_cp_wait();
     }
     __syncthreads();
-    for (;;) {
+    for (int gu = group;; gu += NG) {
       int u = 0;
-      if (lane == 0) u = atomicAdd(&s_next[ch], 1);
-      u = __shfl_sync(0xffffffffu, u, 0);
+      if (G == 1) {
+        if (lane == 0) u = atomicAdd(&s_next[ch], 1);
+        u = __shfl_sync(0xffffffffu, u, 0);
+      } else {
+        u = gu;
+      }
       if (u >= nunits) break;
       const int k1a = u, k1b = Kp - 1 - u;
       const bool two = k1b != k1a;
@@ -321,7 +341,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
         if (slot <= u) { k2 = slot; valid = true; }
         else if (two && slot >= off2 && slot - off2 <= k1b) { k1 = k1b; k2 = slot - off2; valid = true; }
         const int mtop = min(M, l3top);
-        for (int pi = 0; pi < npairs; ++pi) {
+        for (int pi = sub; pi < npairs; pi += G) {
           const FoldRow fr = s_rows[pi];
           if ((fr.m3a < 0 ? -fr.m3a : fr.m3a) > mtop) continue;
           const int m3a = fr.m3a, m3b = m3a >= 0 ? m3a + 1 : m3a - 1;
@@ -362,7 +382,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
 #undef TP3_FOLD_P1
         }
       }
-      __syncwarp();
+      fold_gsync<G>(group);
       // ---------------- phase 2: T of the unit's shell triples ----------------
       const int qa = (k1a >> 2) + 1, ta = qa * (qa + 1) / 2;
       const int qb = (k1b >> 2) + 1, tb = two ? qb * (qb + 1) / 2 : 0;
@@ -380,7 +400,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           const int cnt = sym ? l3 + 1 : 2 * l3 + 1;
           const int r0 = fold_drow(s, s_lo, l3min, sym);
           const int lt = fb.lt_base + s;
-          for (int tile = lane; tile < nt; tile += 32) {
+          for (int tile = lane + 32 * sub; tile < nt; tile += 32 * G) {
             int t = tile, k1 = k1a, pbase = 0, lbase = 0;
             if (t >= ta) { t -= ta; k1 = k1b; pbase = off2; lbase = na; }
             int q2, q3;
@@ -405,10 +425,10 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
               }
             }
           }
-          __syncwarp();
+          fold_gsync<G>(group);
           __nv_bfloat16* hrow = reinterpret_cast<__nv_bfloat16*>(Thi) + ((size_t)prop * KP + lt) * klp;
           __nv_bfloat16* lrow = reinterpret_cast<__nv_bfloat16*>(Tlo) + ((size_t)prop * KP + lt) * klp;
-          for (int idx = lane; idx < na + nb; idx += 32) {
+          for (int idx = lane + 32 * sub; idx < na + nb; idx += 32 * G) {
             const int ki = idx < na ? t3a + idx : t3b + (idx - na);
             if (!TP3_DCHECK(ki < klp && lt < KP && idx < stage, err)) continue;
             const float v = Ts[idx];
@@ -416,10 +436,10 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
             hrow[ki] = h;
             lrow[ki] = __float2bfloat16_rn(v - __bfloat162float(h));
           }
-          __syncwarp();
+          fold_gsync<G>(group);
         }
       } else {
-        for (int base = 0; base < nitems; base += 32) {
+        for (int base = 32 * sub; base < nitems; base += 32 * G) {
           const int it = base + lane;
           if (it >= nitems) break;
           const int sidx = it / nt;
@@ -454,7 +474,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_couple_fold(
           }
         }
       }
-      __syncwarp();
+      fold_gsync<G>(group);  // the group's D and staging row are free for its next unit
     }
   }
 }
@@ -534,48 +554,87 @@ std::string build_fold_tables(const std::vector<PairBlock>& pbs, int drows, std:
     fb.wall = run;
     wmax = std::max(wmax, run);
     cmax = std::max(cmax, std::max(2 * pb.l1 + 1, 2 * pb.l2 + 1));
-    // chunks of l3 whose D rows fit drows (grown one order at a time)
+    // chunks of consecutive l3 orders whose D rows fit drows.  Each chunk forms its shell
+    // products again for every m3 row up to its highest order, so the split is chosen to
+    // minimise the estimated phase-1 instructions -- per m3-pair row reaching the chunk,
+    // n1 (11 + 2.5 ne): the product and load overhead of an m1 step plus its column loads
+    // and packed FMAs -- over at most kFoldMaxChunks chunks (dynamic programming over
+    // chunk ends; nl3 <= 16).
     for (int pass = 0; pass < 2; ++pass) {
       const bool sym = pass == 0;
-      (sym ? fb.ch_sym0 : fb.ch_gen0) = (int)chunks.size();
-      int n = 0;
-      for (int s_lo = 0; s_lo < pb.nl3;) {
-        int s_hi = s_lo, r = 0;
-        while (s_hi < pb.nl3) {
-          const int l3 = pb.l3min + 2 * s_hi;
-          const int add = sym ? l3 + 1 : 2 * l3 + 1;
-          if (r + add > drows) break;
-          r += add;
-          ++s_hi;
+      const int r_begin = fb.row0, r_end = fb.row0 + (sym ? fb.npair_sym : fb.npair_all);
+      auto drows_of = [&](int s_lo, int s_hi) {
+        int r = 0;
+        for (int s = s_lo; s < s_hi; ++s) {
+          const int l3 = pb.l3min + 2 * s;
+          r += sym ? l3 + 1 : 2 * l3 + 1;
         }
-        if (s_hi == s_lo) return "fold tables: one order of D exceeds the per-warp buffer";
-        chunks.push_back(make_int2(s_lo, s_hi));
-        s_lo = s_hi;
-        ++n;
+        return r;
+      };
+      auto cost = [&](int s_lo, int s_hi) {
+        const int l3top = pb.l3min + 2 * (s_hi - 1);
+        double c = 0.0;
+        for (int ri = r_begin; ri < r_end; ++ri) {
+          const FoldRow& fr = rows[ri];
+          if ((fr.m3a < 0 ? -fr.m3a : fr.m3a) > std::min(pb.M, l3top)) continue;
+          const int a = std::max(fr.c0, s_lo & ~1), b = std::min(fr.c0 + fr.rs, (s_hi + 1) & ~1);
+          if (b > a) c += fr.n1 * (11.0 + 2.5 * (b - a));
+        }
+        return c;
+      };
+      const int nl = pb.nl3;
+      const double inf = 1e300;
+      // best[n][e]: cheapest split of orders [0, e) into n chunks; from[n][e]: its last start
+      std::vector<std::vector<double>> best(kFoldMaxChunks + 1, std::vector<double>(nl + 1, inf));
+      std::vector<std::vector<int>> from(kFoldMaxChunks + 1, std::vector<int>(nl + 1, -1));
+      best[0][0] = 0.0;
+      for (int n = 1; n <= kFoldMaxChunks; ++n)
+        for (int e = 1; e <= nl; ++e)
+          for (int st = 0; st < e; ++st) {
+            if (best[n - 1][st] >= inf || drows_of(st, e) > drows) continue;
+            const double v = best[n - 1][st] + cost(st, e);
+            if (v < best[n][e]) { best[n][e] = v; from[n][e] = st; }
+          }
+      int nbest = -1;
+      for (int n = 1; n <= kFoldMaxChunks; ++n)
+        if (best[n][nl] < inf && (nbest < 0 || best[n][nl] < best[nbest][nl])) nbest = n;
+      if (nbest < 0) {
+        for (int s3 = 0; s3 < nl; ++s3)
+          if (drows_of(s3, s3 + 1) > drows) return "fold tables: one order of D exceeds the per-warp buffer";
+        return "fold tables: too many l3 chunks";
       }
-      if (n > kFoldMaxChunks) return "fold tables: too many l3 chunks";
-      (sym ? fb.nch_sym : fb.nch_gen) = n;
+      std::vector<int2> split;
+      for (int n = nbest, e = nl; n > 0; --n) {
+        const int st = from[n][e];
+        split.push_back(make_int2(st, e));
+        e = st;
+      }
+      (sym ? fb.ch_sym0 : fb.ch_gen0) = (int)chunks.size();
+      for (auto it = split.rbegin(); it != split.rend(); ++it) chunks.push_back(*it);
+      (sym ? fb.nch_sym : fb.nch_gen) = nbest;
     }
     blks.push_back(fb);
   }
   return "";
 }
 
-size_t fold_smem_bytes(int nw, int ps, int drows, int wmax, int cmax, int stage) {
+size_t fold_smem_bytes(int ngroups, int ps, int drows, int wmax, int cmax, int stage) {
   return (size_t)(2 * cmax + 2) * ps * sizeof(float2) + (size_t)wmax * sizeof(float) +
-         (size_t)(1 + nw) * drows * ps * sizeof(float2) + (size_t)nw * stage * sizeof(float);
+         (size_t)(1 + ngroups) * drows * ps * sizeof(float2) + (size_t)ngroups * stage * sizeof(float);
 }
 
 cudaError_t fold_configure() {
   cudaError_t e;
   const int cs = kCoupleMaxDynSmem;
   const cudaFuncAttribute ds = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if ((e = cudaFuncSetAttribute(k_couple_fold<7, 10>, ds, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<8, 10>, ds, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<13, 10>, ds, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<7, 16>, ds, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<8, 16>, ds, cs)) != cudaSuccess ||
-      (e = cudaFuncSetAttribute(k_couple_fold<13, 16>, ds, cs)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(k_couple_fold<7, 10, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<8, 10, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<13, 10, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<14, 10, 2>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<7, 16, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<8, 16, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<13, 16, 1>, ds, cs)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_couple_fold<14, 16, 2>, ds, cs)) != cudaSuccess)
     return e;
   return cudaSuccess;
 }
@@ -585,15 +644,17 @@ cudaError_t launch_couple_fold(const DevTables& t, const TcTables& tc, const Fol
                                const RagInfo* rag) {
   dim3 grid(tc.n_pb, n);
   const bool ltmaj = t_order_major(tc, tf32);
-#define TP3_FOLD_LAUNCH(NW, MX)                                                                                  \
-  k_couple_fold<NW, MX><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w, fv.chunks, \
-                                                       fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage, t.klp, tc.KP,   \
-                                                       sym, Thi, Tlo, tf32, ltmaj, T32, t.n_ltp, rag, tc.err)
+#define TP3_FOLD_LAUNCH(NW, MX, G)                                                                                \
+  k_couple_fold<NW, MX, G><<<grid, NW * 32, fv.smem, s>>>(cc, t.K, t.nc, tc.coff, fv.blks, fv.rows, fv.w,          \
+                                                          fv.chunks, fv.ps, fv.drows, fv.wmax, fv.cmax, fv.stage,   \
+                                                          t.klp, tc.KP, sym, Thi, Tlo, tf32, ltmaj, T32, t.n_ltp,   \
+                                                          rag, tc.err)
   const bool narrow = fv.maxne <= 10;
-  switch (fv.nw) {
-    case 7: if (narrow) TP3_FOLD_LAUNCH(7, 10); else TP3_FOLD_LAUNCH(7, 16); break;
-    case 8: if (narrow) TP3_FOLD_LAUNCH(8, 10); else TP3_FOLD_LAUNCH(8, 16); break;
-    case 13: if (narrow) TP3_FOLD_LAUNCH(13, 10); else TP3_FOLD_LAUNCH(13, 16); break;
+  switch (fv.nw * 4 + fv.grp) {
+    case 7 * 4 + 1: if (narrow) TP3_FOLD_LAUNCH(7, 10, 1); else TP3_FOLD_LAUNCH(7, 16, 1); break;
+    case 8 * 4 + 1: if (narrow) TP3_FOLD_LAUNCH(8, 10, 1); else TP3_FOLD_LAUNCH(8, 16, 1); break;
+    case 13 * 4 + 1: if (narrow) TP3_FOLD_LAUNCH(13, 10, 1); else TP3_FOLD_LAUNCH(13, 16, 1); break;
+    case 14 * 4 + 2: if (narrow) TP3_FOLD_LAUNCH(14, 10, 2); else TP3_FOLD_LAUNCH(14, 16, 2); break;
     default: return cudaErrorInvalidValue;
   }
 #undef TP3_FOLD_LAUNCH

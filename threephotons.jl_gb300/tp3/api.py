@@ -150,7 +150,8 @@ class BasisTypeGB300:
 
     def set_coupling(self, form: int) -> None:
         """Tensor-core coupling form: 0 one-kernel, 1 split, 2 one-kernel on 256 threads, 3 warp-local,
-        4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7 folded-row at 8 / 7 / 13 warps."""
+        4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7 folded-row at 8 / 7 / 13 warps,
+        8 folded-row at 14 warps in pairs (two warps per unit, 7 D buffers)."""
         check(self._lib.tp3_set_coupling(self._ctx, form), self._ctx)
 
     def autotune(self, n: int = 64) -> list:
@@ -159,7 +160,7 @@ class BasisTypeGB300:
         [(mode, coupling form, angular schedule, ms/proposal)] with coupling form 0 one-kernel,
         1 split, 2 one-kernel on 256 threads (two CTAs per SM), 3 warp-local one-kernel,
         4 warp-local on 256 threads (two CTAs per SM), 5 / 6 / 7 folded-row at 8 / 7 / 13
-        warps, and angular schedule TP3_ANGULAR_PERSISTENT or TP3_ANGULAR_TILE (the
+        warps, 8 folded-row at 14 warps in pairs, and angular schedule TP3_ANGULAR_PERSISTENT or TP3_ANGULAR_TILE (the
         fastest tensor-core variant is timed with both)."""
         cap = ctypes.c_int(24)
         rep = np.zeros(4 * 24)
