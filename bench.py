@@ -73,6 +73,10 @@ STAGE_TRAFFIC = {
                                  "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal "
                                            "launch, scaled in proportion to the proposals "
                                            "(profiles/traffic_L18K26N32_b32_folded7w.md)"},
+    ("tc_bf16x3", "folded_13w", "persistent"): {
+        "coupling": (155.9e6 / 32, 0.0), "angular": (230.8e6 / 32, 0.0),
+        "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal launch of each stage, "
+                  "scaled in proportion to the proposals (profiles/traffic_L18K26N32_b32_folded13w.md)"},
     ("tc_bf16x3", "folded_7w", "persistent"): {
         "coupling": (154.2e6 / 32, 0.0), "angular": (231.1e6 / 32, 0.0),
         "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 32-proposal launch of each stage, "
