@@ -388,6 +388,23 @@ int tp3_intensity_max(tp3_ctx* ctx, const void* d_coeff, int KMAX, int LMAX, dou
 int tp3_structure_sh(tp3_ctx* ctx, const double* atoms, const int* mol_start, int n_mol, int LMAX, int KMAX,
                      double rmax, int route, double* density, double* amplitude, double* intensity);
 
+/* Post-processing fit, fitStructures_random (src/data_processing.jl:51-75), on the
+ * context's device for a structure of the context's shape: volume and reference are host
+ * [K][LMAX^2] complex (seanindex order); shells k_lo..k_hi (1-based) are scored.  Each of
+ * `repetitions` random restarts walks rotations rotationMatrix(theta, phi, gamma) of orders
+ * 2:2:L, step size pi shrunk by stepsizefactor (0 < f < 1) per step while it exceeds one
+ * degree (S steps), and keeps a proposal whose similarity -- the mean over the shells of the
+ * Pearson correlation of the two intensities on the synthesis grid of transform /
+ * backtransform (2 LMAX x 2 LMAX) -- beats its best.  draws: [repetitions][3 + 3 S]: three
+ * uniforms in [0, 1) for the start (phi = 2 pi u0, theta = acos(u1), gamma = 2 pi u2), then
+ * per step three standard normals (theta += n0 step / 2, phi += n1 step, gamma += n2 step).
+ * best (out): similarity, theta, phi, gamma of the best restart (the first on ties).
+ * rotated (nullable): [K][LMAX^2] complex, the volume with shells 1..k_hi rotated by it.
+ * FP64.  Synchronises. */
+int tp3_fit_structures_random(tp3_ctx* ctx, const double* volume, const double* reference, int k_lo, int k_hi, int L,
+                              double stepsizefactor, int repetitions, const double* draws, double* best,
+                              double* rotated);
+
 /* ---- Wigner-D rotations (src/spherical_harmonics.jl:572-603) --------------- */
 /* rotationMatrix(theta, phi, gamma, l) of src/spherical_harmonics.jl:590-592:
  * D[m, s] = exp(-i s gamma - i m phi) d^l_{ms}(theta), m, s = -l..l, written

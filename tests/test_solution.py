@@ -1,9 +1,11 @@
 """Start structures from two-photon correlations: the inversion recovers every shell
 Gram matrix G_l[k1, k2] = sum_m c_k1lm conj(c_k2lm) of a band-limited intensity, and the
-recovered coefficients reproduce the model c2 (host-side linear algebra, no GPU)."""
+recovered coefficients reproduce the model c2 (host-side linear algebra); the rotation fit
+on the host and (GPU) on the device."""
 import math
 
 import numpy as np
+import pytest
 
 from tp3.solution import twoPhotons, retrieveSolution
 from tp3.structure import seanindex0
@@ -62,3 +64,40 @@ def test_similarity_and_rotation_fit(config1):
     fitted, best, *_ = fitStructures_random(rot, c, LMAX, range(2, K + 1), L, 0.99, repetitions=8, seed=1)
     assert best > 0.995 and best > s_rot
     assert abs(similarity(c, fitted, LMAX, range(2, K + 1)) - best) < 1e-12
+
+
+def test_fit_draws_follow_the_host_search_order():
+    """The device search is fed the host search's random numbers in its order."""
+    from tp3.postprocess import fit_draws
+    d = fit_draws(3, 0.9, seed=4)
+    rng = np.random.default_rng(4)
+    S = (d.shape[1] - 3) // 3
+    assert S > 0 and math.pi * 0.9 ** S <= math.pi / 180 < math.pi * 0.9 ** (S - 1)
+    for r in range(3):
+        np.testing.assert_array_equal(d[r, :3], [rng.random() for _ in range(3)])
+        np.testing.assert_array_equal(d[r, 3:], [rng.normal() for _ in range(3 * S)])
+
+
+@pytest.mark.gpu
+def test_device_fit_matches_host_fit(config1):
+    """tp3_fit_structures_random walks the same restarts as the host search: the same best
+    rotation, the similarity to 1e-10, and the rotated structure (shells 1..max(K_range),
+    orders 2:2:L) to 1e-10."""
+    import tp3
+    from tp3.postprocess import fitStructures_random, rotateStructure, similarity
+    p = config1["params"]
+    LMAX, K, L = p["LMAX"], p["K"], p["L"]
+    c = config1["coeff"][:K]
+    rot = rotateStructure(c, 1.1, 0.4, -0.7, K, range(2, L + 1, 2), LMAX)
+    basis = tp3.calculate_basis(L, LMAX, p["N"], K)
+    try:
+        for K_range in (range(2, K + 1), range(1, K - 2)):
+            h = fitStructures_random(rot, c, LMAX, K_range, L, 0.97, repetitions=6, seed=3)
+            d = fitStructures_random(rot, c, LMAX, K_range, L, 0.97, repetitions=6, seed=3, basis=basis)
+            assert abs(d[1] - h[1]) < 1e-10
+            np.testing.assert_allclose(d[2:], h[2:], atol=1e-12)
+            scale = np.abs(h[0]).max()
+            assert np.abs(d[0] - h[0]).max() < 1e-10 * scale
+            assert abs(similarity(c, d[0], LMAX, K_range) - d[1]) < 1e-10
+    finally:
+        basis.close()

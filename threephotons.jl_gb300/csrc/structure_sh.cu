@@ -24,13 +24,24 @@
 //     spherical Bessel transform (sphBesselTransform with frdr and the J_{l+1/2} matrices,
 //     src/spherical_harmonics.jl:291-347) -> inverse transform, |.|^2, forward transform
 //     (absoluteSquare, src/spherical_harmonics.jl:376-381).
+//
+// The same grid and synthesis serve the post-processing fit, fitStructures_random
+// (src/data_processing.jl:51-75): random-restart search over rotations of a structure
+// onto a reference, scored by similarity = the mean over K_range of the per-shell Pearson
+// correlation of the two intensities on the synthesis grid (shell_correlation_ISC,
+// similarity, src/spherical_harmonics.jl:398-435).  All repetitions advance in lockstep:
+// per step one kernel rotates the K_range shells of every repetition's proposal (orders
+// 2:2:L, rotateStructure), one synthesises their surfaces and one correlates them with
+// the reference's, and the host keeps each repetition's state and accept decisions.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
 
 #include "ctx_internal.h"
+#include "shellrot.cuh"
 
 namespace {
 
@@ -202,6 +213,78 @@ __global__ void __launch_bounds__(128) k_sh_hankel(const double2* __restrict__ i
   out[((size_t)mol * KMAX + kp) * nco + i] = o;
 }
 
+// grid: (nsets * nk); block 128.  Set r, shell j: copy the volume's shell k0 + j to
+// out[r][j] and rotate its orders 2, 4, ..., lend by the set's Euler angles (theta, phi,
+// gamma) -- rotationMatrix convention -- when rotate is set.
+__global__ void __launch_bounds__(128) k_fit_rotate(const double2* __restrict__ vol, double2* __restrict__ out,
+                                                    const double* __restrict__ euler, int k0, int nk, int LMAX,
+                                                    int lend, int nrot, const double* __restrict__ delta,
+                                                    const int* __restrict__ doff) {
+  __shared__ double2 xs[4][2 * tp3::kMaxRotL + 1], ys[4][2 * tp3::kMaxRotL + 1];
+  const int ncoef = LMAX * LMAX;
+  const int set = blockIdx.x / nk, j = blockIdx.x - set * nk;
+  const double2* c = vol + (size_t)(k0 + j) * ncoef;
+  double2* o = out + (size_t)blockIdx.x * ncoef;
+  for (int e = threadIdx.x; e < ncoef; e += blockDim.x) o[e] = c[e];
+  __syncthreads();
+  if (j >= nrot) return;
+  const double th = euler[3 * set], ph = euler[3 * set + 1], ga = euler[3 * set + 2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nord = lend / 2;  // orders 2 .. lend (even)
+  for (int i = warp; i < nord; i += nw) {
+    const int l = lend - 2 * i;  // largest orders first
+    tp3::rotate_order_warp(o, o, l, LMAX, th, ph, ga, delta + doff[l], xs[warp], ys[warp], lane);
+  }
+}
+
+// grid: nsets * nk; block 256.  Pearson correlation of the real parts of surface
+// (set, j) and reference surface j over the P grid points (two passes, FP64).
+__global__ void __launch_bounds__(256) k_fit_corr(const double2* __restrict__ surf, const double2* __restrict__ ref,
+                                                  int nk, int P, double* __restrict__ corr) {
+  __shared__ double sa[256], sb[256], sc[256];
+  const int j = blockIdx.x % nk;
+  const double2* a = surf + (size_t)blockIdx.x * P;
+  const double2* b = ref + (size_t)j * P;
+  double ma = 0.0, mb = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    ma += a[i].x;
+    mb += b[i].x;
+  }
+  sa[threadIdx.x] = ma;
+  sb[threadIdx.x] = mb;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      sa[threadIdx.x] += sa[threadIdx.x + h];
+      sb[threadIdx.x] += sb[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  ma = sa[0] / P;
+  mb = sb[0] / P;
+  __syncthreads();
+  double sab = 0.0, saa = 0.0, sbb = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const double x = a[i].x - ma, y = b[i].x - mb;
+    sab += x * y;
+    saa += x * x;
+    sbb += y * y;
+  }
+  sa[threadIdx.x] = sab;
+  sb[threadIdx.x] = saa;
+  sc[threadIdx.x] = sbb;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      sa[threadIdx.x] += sa[threadIdx.x + h];
+      sb[threadIdx.x] += sb[threadIdx.x + h];
+      sc[threadIdx.x] += sc[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) corr[blockIdx.x] = sa[0] / sqrt(sb[0] * sc[0]);
+}
+
 int seanindex0(int l, int m, int bw) {
   const int bigL = bw - 1;
   if (m >= 0) return m * (bigL + 1) - (m * (m - 1)) / 2 + (l - m);
@@ -360,3 +443,128 @@ int tp3_structure_sh(tp3_ctx* c, const double* atoms, const int* mol_start, int 
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "structure_sh");
   return TP3_OK;
 }
+
+int tp3_fit_structures_random(tp3_ctx* c, const double* volume, const double* reference, int k_lo, int k_hi, int L,
+                              double stepsizefactor, int repetitions, const double* draws, double* best,
+                              double* rotated) {
+  if (int r = tp3::ctx_check(c)) return r;
+  const int K = c->b.K, LMAX = c->b.LMAX;
+  if (!volume || !reference || !draws || !best || repetitions < 1 || repetitions > 4096 || k_lo < 1 ||
+      k_hi < k_lo || k_hi > K || L < 0 || !(stepsizefactor > 0.0 && stepsizefactor < 1.0) || LMAX > kShMaxLMAX)
+    return tp3::ctx_fail(c, TP3_ERR_ARG, "bad fit arguments");
+  const int lend = std::min(L, LMAX - 1) & ~1;
+  const double pi = kPi;
+  int S = 0;
+  for (double st = pi; st > pi / 180.0; st *= stepsizefactor)
+    if (++S > 10000000) return tp3::ctx_fail(c, TP3_ERR_ARG, "step size factor too close to 1");
+  if (int r = tp3::ctx_ensure_rot_tables(c, std::max(lend, 0))) return r;
+  const int bw = LMAX, size = 2 * bw, P = size * size, ncoef = LMAX * LMAX;
+  const int nk = k_hi - k_lo + 1, R = repetitions;
+  ShTables T;
+  build_sh_tables(bw, 1, false, T);
+  cudaStream_t s = c->stream;
+  double *d_plm = nullptr, *d_w = nullptr, *d_eu = nullptr, *d_corr = nullptr;
+  double2 *d_root = nullptr, *d_vol = nullptr, *d_ref = nullptr, *d_rot = nullptr, *d_surf = nullptr,
+          *d_refs = nullptr;
+  int2* d_lm = nullptr;
+  int* d_idx = nullptr;
+  const size_t smem = (size_t)size * (2 * bw - 1) * sizeof(double2);
+  std::vector<double2> hv((size_t)K * ncoef), hr((size_t)K * ncoef);
+  for (size_t i = 0; i < hv.size(); ++i) {
+    hv[i] = make_double2(volume[2 * i], volume[2 * i + 1]);
+    hr[i] = make_double2(reference[2 * i], reference[2 * i + 1]);
+  }
+  cudaError_t e;
+  auto cleanup = [&]() {
+    cudaFree(d_plm); cudaFree(d_w); cudaFree(d_eu); cudaFree(d_corr); cudaFree(d_root); cudaFree(d_vol);
+    cudaFree(d_ref); cudaFree(d_rot); cudaFree(d_surf); cudaFree(d_refs); cudaFree(d_lm); cudaFree(d_idx);
+  };
+  if ((e = upload(T.plm, &d_plm, s)) != cudaSuccess || (e = upload(T.w, &d_w, s)) != cudaSuccess ||
+      (e = upload(T.root, &d_root, s)) != cudaSuccess || (e = upload(T.lm, &d_lm, s)) != cudaSuccess ||
+      (e = upload(T.idx, &d_idx, s)) != cudaSuccess || (e = upload(hv, &d_vol, s)) != cudaSuccess ||
+      (e = upload(hr, &d_ref, s)) != cudaSuccess ||
+      (e = cudaMalloc(&d_eu, (size_t)R * 3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&d_corr, (size_t)R * nk * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&d_rot, (size_t)std::max(R * nk, K) * ncoef * sizeof(double2))) != cudaSuccess ||
+      (e = cudaMalloc(&d_surf, (size_t)R * nk * P * sizeof(double2))) != cudaSuccess ||
+      (e = cudaMalloc(&d_refs, (size_t)nk * P * sizeof(double2))) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_sht_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess) {
+    cleanup();
+    cudaGetLastError();
+    return tp3::ctx_cuda_fail(c, e, "fit setup");
+  }
+  // the reference's surfaces of the K_range shells, once
+  k_sht_inverse<<<nk, 256, smem, s>>>(d_ref + (size_t)(k_lo - 1) * ncoef, bw, d_plm, d_root, d_idx, d_refs);
+  // repetition state: (theta, phi, gamma, best similarity); draws [R][3 + 3 S]
+  const size_t nd = 3 + 3 * (size_t)S;
+  std::vector<double> th(R), ph(R), ga(R), sc(R, 0.0), eu(3 * R), corr((size_t)R * nk);
+  for (int r = 0; r < R; ++r) {
+    const double* d = draws + (size_t)r * nd;
+    ph[r] = 2.0 * pi * d[0];
+    th[r] = std::acos(d[1]);
+    ga[r] = 2.0 * pi * d[2];
+  }
+  double st = pi;
+  for (int step = 0; step < S && e == cudaSuccess; ++step, st *= stepsizefactor) {
+    for (int r = 0; r < R; ++r) {
+      const double* d = draws + (size_t)r * nd + 3 + 3 * (size_t)step;
+      eu[3 * r] = th[r] + d[0] * st / 2;
+      eu[3 * r + 1] = ph[r] + d[1] * st;
+      eu[3 * r + 2] = ga[r] + d[2] * st;
+    }
+    if ((e = cudaMemcpyAsync(d_eu, eu.data(), eu.size() * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      break;
+    k_fit_rotate<<<R * nk, 128, 0, s>>>(d_vol, d_rot, d_eu, k_lo - 1, nk, LMAX, lend, nk, c->d_delta, c->d_doff);
+    k_sht_inverse<<<R * nk, 256, smem, s>>>(d_rot, bw, d_plm, d_root, d_idx, d_surf);
+    k_fit_corr<<<R * nk, 256, 0, s>>>(d_surf, d_refs, nk, P, d_corr);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = cudaMemcpyAsync(corr.data(), d_corr, corr.size() * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      break;
+    for (int r = 0; r < R; ++r) {
+      double m = 0.0;
+      for (int j = 0; j < nk; ++j) m += corr[(size_t)r * nk + j];
+      m /= nk;
+      if (m > sc[r]) {
+        sc[r] = m;
+        th[r] = eu[3 * r];
+        ph[r] = eu[3 * r + 1];
+        ga[r] = eu[3 * r + 2];
+      }
+    }
+  }
+  int rb = 0;
+  for (int r = 1; r < R; ++r)
+    if (sc[r] > sc[rb]) rb = r;
+  if (e == cudaSuccess) {
+    best[0] = sc[rb];
+    best[1] = th[rb];
+    best[2] = ph[rb];
+    best[3] = ga[rb];
+    if (rotated) {
+      // rotateStructure(volume, theta, phi, gamma, k_hi, 2:2:L): shells past k_hi unchanged
+      eu[0] = th[rb];
+      eu[1] = ph[rb];
+      eu[2] = ga[rb];
+      if ((e = cudaMemcpyAsync(d_eu, eu.data(), 3 * sizeof(double), cudaMemcpyHostToDevice, s)) == cudaSuccess) {
+        k_fit_rotate<<<K, 128, 0, s>>>(d_vol, d_rot, d_eu, 0, K, LMAX, lend, k_hi, c->d_delta, c->d_doff);
+        e = cudaGetLastError();
+      }
+      std::vector<double2> out((size_t)K * ncoef);
+      if (e == cudaSuccess &&
+          (e = cudaMemcpyAsync(out.data(), d_rot, out.size() * sizeof(double2), cudaMemcpyDeviceToHost, s)) ==
+              cudaSuccess &&
+          (e = cudaStreamSynchronize(s)) == cudaSuccess)
+        for (size_t i = 0; i < out.size(); ++i) {
+          rotated[2 * i] = out[i].x;
+          rotated[2 * i + 1] = out[i].y;
+        }
+    }
+  }
+  cleanup();
+  if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "fit");
+  return TP3_OK;
+}
+

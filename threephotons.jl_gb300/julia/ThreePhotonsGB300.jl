@@ -18,7 +18,7 @@ export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_
        GB300_energy_batch, GB300_set_mode, GB300_autotune, GB300_chains_log, GB300_chains_snapshot,
        GB300_chains_restore, GB300_chains_coeff, GB300_chains_destroy, GB300_chains_set_move,
        GB300_chains_enable_move_log, GB300_mlp_create, GB300_mlp_destroy, GB300_set_angular,
-       GB300_createSphericalHarmonicsStructure
+       GB300_createSphericalHarmonicsStructure, GB300_fitStructures_random
 
 const libtp3 = joinpath(@__DIR__, "..", "lib", "libtp3.so")
 
@@ -173,6 +173,35 @@ function GB300_createSphericalHarmonicsStructure(basis::BasisTypeGB300, molecule
     qmax = pi * KMAX / rmax
     vol(c, r) = SphericalHarmonicsVolume([c[:, k] for k = 1:KMAX], LMAX, KMAX, r)
     return vol(out[1], rmax), vol(out[2], qmax), vol(out[3], qmax)
+end
+
+"""fitStructures_random (src/data_processing.jl:51-75) on the GPU (tp3_fit_structures_random)
+for a volume of the basis's shape; returns (rotated volume, similarity, theta, phi, gamma)."""
+function GB300_fitStructures_random(basis::BasisTypeGB300, volume::SphericalHarmonicsVolume,
+                                    reference::SphericalHarmonicsVolume, K_range::UnitRange{Int64}, L::Int64,
+                                    stepsizefactor::Float64, repititions::Int64=4)
+    S = 0
+    st = pi
+    while st > pi / 180.0
+        S += 1
+        st *= stepsizefactor
+    end
+    draws = zeros(Float64, 3 + 3 * S, repititions)
+    for r = 1:repititions
+        draws[1:3, r] = rand(3)
+        draws[4:end, r] = randn(3 * S)
+    end
+    vol = hcat(volume.coeff[1:basis.K]...)
+    ref = hcat(reference.coeff[1:basis.K]...)
+    best = zeros(Float64, 4)
+    rotated = similar(vol)
+    check(ccall((:tp3_fit_structures_random, libtp3), Int32,
+                (Ptr{Void}, Ptr{Complex{Float64}}, Ptr{Complex{Float64}}, Int32, Int32, Int32, Float64, Int32,
+                 Ptr{Float64}, Ptr{Float64}, Ptr{Complex{Float64}}),
+                basis.ctx, vol, ref, first(K_range), last(K_range), L, stepsizefactor, repititions, draws, best,
+                rotated), basis.ctx)
+    out = SphericalHarmonicsVolume([rotated[:, k] for k = 1:basis.K], volume.LMAX, basis.K, volume.rmax)
+    return out, best[1], best[2], best[3], best[4]
 end
 
 # ---- device-resident chains (rotate_all_at_once on the GPU) ---------------------------

@@ -89,10 +89,41 @@ def rotateStructure(coeff: np.ndarray, theta: float, phi: float, gamma: float, K
     return out
 
 
+def fit_draws(repetitions: int, stepsizefactor: float, seed: int = 0) -> np.ndarray:
+    """The random numbers of fitStructures_random in the order the host search draws them:
+    per restart three uniforms, then three normals per step; [repetitions][3 + 3 S]."""
+    S, st = 0, math.pi
+    while st > math.pi / 180.0:
+        S += 1
+        st *= stepsizefactor
+    rng = np.random.default_rng(seed)
+    out = np.empty((repetitions, 3 + 3 * S))
+    for r in range(repetitions):
+        out[r, :3] = [rng.random() for _ in range(3)]
+        out[r, 3:] = [rng.normal() for _ in range(3 * S)]
+    return out
+
+
 def fitStructures_random(coeff: np.ndarray, reference: np.ndarray, LMAX: int, K_range, L: int,
-                         stepsizefactor: float, repetitions: int = 4, seed: int = 0):
+                         stepsizefactor: float, repetitions: int = 4, seed: int = 0, basis=None):
     """Best rotation of `coeff` onto `reference` by random-restart local search
-    (src/data_processing.jl:51-72).  Returns (rotated coefficients, similarity, theta, phi, gamma)."""
+    (src/data_processing.jl:51-72).  Returns (rotated coefficients, similarity, theta, phi, gamma).
+    With `basis` (a context of the structure's K and LMAX) the search runs on its device
+    (tp3_fit_structures_random) with the same random numbers."""
+    if basis is not None:
+        from . import _lib
+        ks = list(K_range)
+        if ks != list(range(ks[0], ks[-1] + 1)):
+            raise ValueError("K_range must be consecutive shells")
+        vol = np.ascontiguousarray(coeff, dtype=np.complex128)
+        ref = np.ascontiguousarray(reference, dtype=np.complex128)
+        draws = np.ascontiguousarray(fit_draws(repetitions, stepsizefactor, seed))
+        best = np.zeros(4)
+        rotated = np.zeros_like(vol)
+        _lib.check(basis._lib.tp3_fit_structures_random(basis._ctx, vol.ctypes.data, ref.ctypes.data, ks[0], ks[-1], L,
+                                                        float(stepsizefactor), repetitions, draws.ctypes.data,
+                                                        best.ctypes.data, rotated.ctypes.data), basis._ctx)
+        return rotated, float(best[0]), float(best[1]), float(best[2]), float(best[3])
     rng = np.random.default_rng(seed)
     K = max(K_range)
     lr = range(2, L + 1, 2)
