@@ -405,6 +405,19 @@ int tp3_fit_structures_random(tp3_ctx* ctx, const double* volume, const double* 
                               double stepsizefactor, int repetitions, const double* draws, double* best,
                               double* rotated);
 
+/* retrieveSolution (src/correlations.jl:261-319): intensity coefficients consistent with
+ * a two-photon correlation, on the context's device.  c2: host [N][Kd][Kd] doubles,
+ * c2[alpha][k2 - 1][k1 - 1] as twoPhotons writes it; shells k_lo..k_hi (K2 = k_hi - k_lo + 1
+ * <= 64, L even with 2 L < K2), dq = qmax / k_hi.  Per shell pair a least-squares fit of
+ * the slice (symmetrised in alpha at lambda = 0) on (1/4pi) P_l(cos alpha*), l = 0:2:upperL,
+ * upperL = min(L, 2 min(k1, k2) - 2), gives G_l[k1, k2]; the top 2l+1 eigenpairs of each
+ * G_l (eigenvector signs fixed by making the largest entry positive) give real SH
+ * coefficients sqrt(w) v^T, mapped to complex ones with Umat(l)^*; the whole structure is
+ * negated when negativityCheck on the synthesis grid exceeds 0.33.  out: host [k_hi][LMAX^2]
+ * complex (shells below k_lo zero).  FP64.  Synchronises. */
+int tp3_retrieve_solution(tp3_ctx* ctx, const double* c2, int N, int Kd, int L, int LMAX, int k_lo, int k_hi,
+                          double qmax, double lambda, double* out);
+
 /* ---- Wigner-D rotations (src/spherical_harmonics.jl:572-603) --------------- */
 /* rotationMatrix(theta, phi, gamma, l) of src/spherical_harmonics.jl:590-592:
  * D[m, s] = exp(-i s gamma - i m phi) d^l_{ms}(theta), m, s = -l..l, written

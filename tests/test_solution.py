@@ -101,3 +101,24 @@ def test_device_fit_matches_host_fit(config1):
             assert abs(similarity(c, d[0], LMAX, K_range) - d[1]) < 1e-10
     finally:
         basis.close()
+
+
+@pytest.mark.gpu
+def test_device_retrieve_solution_matches_host(config1):
+    """tp3_retrieve_solution: the same least-squares Gram matrices, eigenpairs (signs fixed
+    the same way) and negativity flip as the host inversion, so the same coefficients; at
+    lambda = 0 and lambda = 1.2."""
+    import tp3
+    p = config1["params"]
+    basis = tp3.calculate_basis(p["L"], p["LMAX"], p["N"], p["K"])
+    try:
+        for K, LMAX, L, N, lam in ((12, 9, 4, 24, 0.0), (16, 11, 6, 32, 1.2)):
+            c = _band_limited(K, LMAX, L, seed=K)
+            qmax = 8.0
+            c2 = twoPhotons(c, LMAX, L, N, K, qmax / K, lam)
+            h = retrieveSolution(c2, L, LMAX, range(1, K + 1), qmax, lam)
+            d = retrieveSolution(c2, L, LMAX, range(1, K + 1), qmax, lam, basis=basis)
+            np.testing.assert_allclose(d, h, atol=1e-9 * np.abs(h).max())
+    finally:
+        basis.close()
+

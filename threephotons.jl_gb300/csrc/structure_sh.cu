@@ -33,6 +33,16 @@
 // per step one kernel rotates the K_range shells of every repetition's proposal (orders
 // 2:2:L, rotateStructure), one synthesises their surfaces and one correlates them with
 // the reference's, and the host keeps each repetition's state and accept decisions.
+//
+// retrieveSolution (src/correlations.jl:261-319), the start structure from a two-photon
+// correlation c2: one thread per shell pair fits the pair's c2 slice (symmetrised in
+// alpha at lambda = 0) by least squares against (1/4pi) P_l(cos alpha*), l = 0:2:upperL
+// (normal equations, Cholesky, FP64), giving G_l[k1, k2]; one warp per order l runs cyclic
+// Jacobi on G_l (K2 x K2, rotations' row and column updates across the lanes); the host
+// keeps the top 2l+1 eigenpairs (each eigenvector's largest entry made positive), forms
+// sqrt(w) v^T in the real SH basis, maps it to complex coefficients with Umat(l)^* and
+// negates the result when negativityCheck (src/spherical_harmonics.jl:622-625) on the
+// synthesis grid exceeds 0.33.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -283,6 +293,129 @@ __global__ void __launch_bounds__(256) k_fit_corr(const double2* __restrict__ su
     __syncthreads();
   }
   if (threadIdx.x == 0) corr[blockIdx.x] = sa[0] / sqrt(sb[0] * sc[0]);
+}
+
+// P_l(x), the Legendre polynomial by its three-term recurrence.
+__device__ inline double rs_legendre(int l, double x) {
+  double p0 = 1.0, p1 = x;
+  if (l == 0) return p0;
+  for (int n = 1; n < l; ++n) {
+    const double p2 = ((2.0 * n + 1.0) * x * p1 - n * p0) / (n + 1.0);
+    p0 = p1;
+    p1 = p2;
+  }
+  return p1;
+}
+
+// One thread per shell pair (k1 >= k2 of lo..hi): least-squares coefficients of the c2
+// slice c2[alpha][k2 - 1][k1 - 1] (c2 is [N][Kd][Kd]) on (1/4pi) P_{2j}(cos alpha*),
+// j = 0..upperL/2, written to G[j][k1 - lo][k2 - lo] and its mirror (G zeroed before).
+__global__ void k_rs_fit(const double* __restrict__ c2, int N, int Kd, int lo, int hi, int L, double dq,
+                         double lambda, double* __restrict__ G) {
+  const int n = hi - lo + 1;
+  const int pair = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= n * (n + 1) / 2) return;
+  int a1 = 0;
+  while ((a1 + 1) * (a1 + 2) / 2 <= pair) ++a1;
+  const int a2 = pair - a1 * (a1 + 1) / 2;  // a2 <= a1
+  const int k1 = lo + a1, k2 = lo + a2;
+  const int upperL = min(L, 2 * min(k1, k2) - 2);
+  const int J = upperL / 2 + 1;
+  constexpr int kMaxJ = 32;
+  if (J > kMaxJ) return;
+  double M[kMaxJ * (kMaxJ + 1) / 2], r[kMaxJ], p[kMaxJ];
+  for (int i = 0; i < J * (J + 1) / 2; ++i) M[i] = 0.0;
+  for (int i = 0; i < J; ++i) r[i] = 0.0;
+  const double t1 = acos(k1 * dq * lambda / (4.0 * kPi)), t2 = acos(k2 * dq * lambda / (4.0 * kPi));
+  const double s12 = sin(t1) * sin(t2), c12 = cos(t1) * cos(t2);
+  for (int a = 0; a < N; ++a) {
+    double sl = c2[((size_t)a * Kd + (k2 - 1)) * Kd + (k1 - 1)];
+    if (lambda == 0.0) sl = 0.5 * (sl + c2[((size_t)(N - 1 - a) * Kd + (k2 - 1)) * Kd + (k1 - 1)]);
+    const double al = (a + 0.5) * (kPi / N);
+    const double x = cos(acos(fmin(fmax(s12 * cos(al) + c12, -1.0), 1.0)));
+    for (int j = 0; j < J; ++j) p[j] = rs_legendre(2 * j, x) / (4.0 * kPi);
+    for (int i = 0; i < J; ++i) {
+      r[i] += p[i] * sl;
+      for (int j = 0; j <= i; ++j) M[i * (i + 1) / 2 + j] += p[i] * p[j];
+    }
+  }
+  // Cholesky M = C C^T in place (lower triangle), then forward and back substitution
+  for (int i = 0; i < J; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      double v = M[i * (i + 1) / 2 + j];
+      for (int k = 0; k < j; ++k) v -= M[i * (i + 1) / 2 + k] * M[j * (j + 1) / 2 + k];
+      M[i * (i + 1) / 2 + j] = i == j ? sqrt(fmax(v, 0.0)) : v / M[j * (j + 1) / 2 + j];
+    }
+  }
+  for (int i = 0; i < J; ++i) {
+    double v = r[i];
+    for (int k = 0; k < i; ++k) v -= M[i * (i + 1) / 2 + k] * r[k];
+    r[i] = v / M[i * (i + 1) / 2 + i];
+  }
+  for (int i = J - 1; i >= 0; --i) {
+    double v = r[i];
+    for (int k = i + 1; k < J; ++k) v -= M[k * (k + 1) / 2 + i] * r[k];
+    r[i] = v / M[i * (i + 1) / 2 + i];
+  }
+  for (int j = 0; j < J; ++j) {
+    G[((size_t)j * n + a1) * n + a2] = r[j];
+    G[((size_t)j * n + a2) * n + a1] = r[j];
+  }
+}
+
+// One warp per matrix G[j] (n x n, symmetric): cyclic Jacobi until the off-diagonal
+// norm is below 1e-15 of the Frobenius norm (at most 60 sweeps).  Writes the eigenvalues
+// to w[j][i] and the eigenvectors as columns of V[j].  dynamic shared memory: 2 n^2 doubles.
+__global__ void __launch_bounds__(32) k_rs_eig(const double* __restrict__ G, int n, double* __restrict__ w,
+                                               double* __restrict__ V) {
+  extern __shared__ double sm_eig[];
+  double* A = sm_eig;           // [n][n]
+  double* Q = sm_eig + n * n;   // [n][n] eigenvectors (columns)
+  const int lane = threadIdx.x;
+  const double* g = G + (size_t)blockIdx.x * n * n;
+  for (int i = lane; i < n * n; i += 32) {
+    A[i] = g[i];
+    Q[i] = (i / n == i % n) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  double fro = 0.0;
+  for (int i = lane; i < n * n; i += 32) fro += A[i] * A[i];
+  for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int i = lane; i < n * n; i += 32)
+      if (i / n != i % n) off += A[i] * A[i];
+    for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+    if (off <= 1e-30 * fro) break;
+    for (int pp = 0; pp < n - 1; ++pp)
+      for (int qq = pp + 1; qq < n; ++qq) {
+        const double apq = A[pp * n + qq];
+        if (fabs(apq) <= 1e-300) continue;
+        const double app = A[pp * n + pp], aqq = A[qq * n + qq];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        __syncwarp();
+        // columns p, q of A (then rows, by symmetry) and of Q
+        for (int i = lane; i < n; i += 32) {
+          const double aip = A[i * n + pp], aiq = A[i * n + qq];
+          A[i * n + pp] = c * aip - s * aiq;
+          A[i * n + qq] = s * aip + c * aiq;
+          const double qip = Q[i * n + pp], qiq = Q[i * n + qq];
+          Q[i * n + pp] = c * qip - s * qiq;
+          Q[i * n + qq] = s * qip + c * qiq;
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+          const double api = A[pp * n + i], aqi = A[qq * n + i];
+          A[pp * n + i] = c * api - s * aqi;
+          A[qq * n + i] = s * api + c * aqi;
+        }
+        __syncwarp();
+      }
+  }
+  for (int i = lane; i < n; i += 32) w[(size_t)blockIdx.x * n + i] = A[i * n + i];
+  for (int i = lane; i < n * n; i += 32) V[(size_t)blockIdx.x * n * n + i] = Q[i];
 }
 
 int seanindex0(int l, int m, int bw) {
@@ -565,6 +698,135 @@ int tp3_fit_structures_random(tp3_ctx* c, const double* volume, const double* re
   }
   cleanup();
   if (e != cudaSuccess) return tp3::ctx_cuda_fail(c, e, "fit");
+  return TP3_OK;
+}
+
+int tp3_retrieve_solution(tp3_ctx* c, const double* c2, int N, int Kd, int L, int LMAX, int k_lo, int k_hi,
+                          double qmax, double lambda, double* out) {
+  if (int r = tp3::ctx_check(c)) return r;
+  const int n = k_hi - k_lo + 1;
+  if (!c2 || !out || N < 2 || Kd < 1 || k_lo < 1 || k_hi > Kd || k_hi < k_lo || L < 0 || (L & 1) ||
+      LMAX < L + 1 || LMAX > kShMaxLMAX || n > 64 || L / 2 + 1 > 32 || !(qmax > 0.0) || !(lambda >= 0.0) ||
+      !(2 * L < n))
+    return tp3::ctx_fail(c, TP3_ERR_ARG, "bad retrieve_solution arguments (needs L < K2 / 2, K2 <= 64)");
+  const double dq = qmax / k_hi;
+  if (k_hi * dq * lambda / (4.0 * kPi) > 1.0) return tp3::ctx_fail(c, TP3_ERR_ARG, "lambda too large for qmax");
+  const int nl = L / 2 + 1;
+  cudaStream_t s = c->stream;
+  std::vector<double> hc2(c2, c2 + (size_t)N * Kd * Kd);
+  double *d_c2 = nullptr, *d_G = nullptr, *d_w = nullptr, *d_V = nullptr;
+  cudaError_t e;
+  const size_t esmem = 2 * (size_t)n * n * sizeof(double);
+  auto cleanup = [&]() { cudaFree(d_c2); cudaFree(d_G); cudaFree(d_w); cudaFree(d_V); };
+  if ((e = upload(hc2, &d_c2, s)) != cudaSuccess ||
+      (e = cudaMalloc(&d_G, (size_t)nl * n * n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&d_w, (size_t)nl * n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&d_V, (size_t)nl * n * n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMemsetAsync(d_G, 0, (size_t)nl * n * n * sizeof(double), s)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_rs_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem)) != cudaSuccess) {
+    cleanup();
+    cudaGetLastError();
+    return tp3::ctx_cuda_fail(c, e, "retrieve_solution setup");
+  }
+  const int npairs = n * (n + 1) / 2;
+  k_rs_fit<<<(npairs + 63) / 64, 64, 0, s>>>(d_c2, N, Kd, k_lo, k_hi, L, dq, lambda, d_G);
+  k_rs_eig<<<nl, 32, esmem, s>>>(d_G, n, d_w, d_V);
+  std::vector<double> w((size_t)nl * n), V((size_t)nl * n * n);
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaMemcpyAsync(w.data(), d_w, w.size() * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(V.data(), d_V, V.size() * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    cleanup();
+    return tp3::ctx_cuda_fail(c, e, "retrieve_solution");
+  }
+  cleanup();
+  // top 2l+1 eigenpairs -> real SH coefficients -> complex (Umat(l)^* applied per shell)
+  const int ncoef = LMAX * LMAX;
+  std::vector<double2> res((size_t)k_hi * ncoef, make_double2(0.0, 0.0));
+  for (int j = 0; j < nl; ++j) {
+    const int l = 2 * j, d = 2 * l + 1;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return w[(size_t)j * n + a] < w[(size_t)j * n + b]; });
+    // real coefficients r[k][u], u = -l..l: u-th of the top d eigenpairs in ascending order
+    std::vector<double> rr((size_t)n * d, 0.0);
+    for (int u = 0; u < d && u < n; ++u) {
+      const int col = order[n - d + u];
+      const double* vcol = &V[(size_t)j * n * n];
+      int imax = 0;
+      for (int i = 1; i < n; ++i)
+        if (std::fabs(vcol[i * n + col]) > std::fabs(vcol[imax * n + col])) imax = i;
+      const double sg = vcol[imax * n + col] < 0.0 ? -1.0 : 1.0;
+      const double sw = std::sqrt(std::max(0.0, w[(size_t)j * n + col]));
+      for (int k = 0; k < n; ++k) rr[(size_t)k * d + u] = sw * sg * vcol[k * n + col];
+    }
+    // complex c_m = sum_u conj(Umat[u][m]) r_u, Umat(l) of src/spherical_harmonics.jl:445-457
+    const double is2 = 1.0 / std::sqrt(2.0);
+    for (int k = 0; k < n; ++k)
+      for (int m = -l; m <= l; ++m) {
+        double re = 0.0, im = 0.0;
+        for (int u = -l; u <= l; ++u) {
+          const double ru = rr[(size_t)k * d + (u + l)];
+          double ur = 0.0, ui = 0.0;  // Umat[u][m]
+          const double sgm = (m & 1) ? -1.0 : 1.0;
+          if (m == 0 && u == 0) ur += 1.0;
+          if (u > 0 && m == u) ur += is2;
+          if (u < 0 && m == u) ui += is2 * sgm;
+          if (u < 0 && m == -u) ui -= is2;
+          if (u > 0 && m == -u) ur += is2 * sgm;
+          re += ur * ru;
+          im -= ui * ru;
+        }
+        res[(size_t)(k_lo - 1 + k) * ncoef + seanindex0(l, m, LMAX)] = make_double2(re, im);
+      }
+  }
+  // negativityCheck on the synthesis grid of the scored shells
+  {
+    const int bw = LMAX, size = 2 * bw, P = size * size;
+    ShTables T;
+    build_sh_tables(bw, 1, false, T);
+    double *d_plm = nullptr;
+    double2 *d_root = nullptr, *d_co = nullptr, *d_surf = nullptr;
+    int* d_idx = nullptr;
+    const size_t smem = (size_t)size * (2 * bw - 1) * sizeof(double2);
+    std::vector<double2> co(res.begin() + (size_t)(k_lo - 1) * ncoef, res.end());
+    std::vector<double2> surf((size_t)n * P);
+    auto clean2 = [&]() { cudaFree(d_plm); cudaFree(d_root); cudaFree(d_co); cudaFree(d_surf); cudaFree(d_idx); };
+    if ((e = upload(T.plm, &d_plm, s)) != cudaSuccess || (e = upload(T.root, &d_root, s)) != cudaSuccess ||
+        (e = upload(T.idx, &d_idx, s)) != cudaSuccess || (e = upload(co, &d_co, s)) != cudaSuccess ||
+        (e = cudaMalloc(&d_surf, surf.size() * sizeof(double2))) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_sht_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess) {
+      clean2();
+      cudaGetLastError();
+      return tp3::ctx_cuda_fail(c, e, "negativity setup");
+    }
+    k_sht_inverse<<<n, 256, smem, s>>>(d_co, bw, d_plm, d_root, d_idx, d_surf);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = cudaMemcpyAsync(surf.data(), d_surf, surf.size() * sizeof(double2), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+      clean2();
+      return tp3::ctx_cuda_fail(c, e, "negativity");
+    }
+    clean2();
+    double neg = 0.0;
+    for (int k = 0; k < n; ++k) {
+      double sneg = 0.0, sabs = 0.0;
+      for (int i = 0; i < P; ++i) {
+        const double2 v = surf[(size_t)k * P + i];
+        sneg += std::fabs(std::min(v.x, 0.0));
+        sabs += std::fabs(v.x);
+      }
+      if (sabs > 0.0) neg += std::max(sneg / sabs, 0.0);
+    }
+    const double sg = neg > 0.33 ? -1.0 : 1.0;
+    for (size_t i = 0; i < res.size(); ++i) {
+      out[2 * i] = sg * res[i].x;
+      out[2 * i + 1] = sg * res[i].y;
+    }
+  }
   return TP3_OK;
 }
 

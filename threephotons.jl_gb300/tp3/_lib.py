@@ -60,6 +60,8 @@ SIGNATURES = {
     "tp3_set_coupling": (c_int, [c_void_p, c_int]),
     "tp3_set_angular": (c_int, [c_void_p, c_int]),
     "tp3_set_host_input": (c_int, [c_void_p, c_int]),
+    "tp3_retrieve_solution": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_double,
+                                      c_double, c_void_p]),
     "tp3_fit_structures_random": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_int,
                                           c_void_p, c_void_p, c_void_p]),
     "tp3_structure_sh": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_int, c_void_p,

@@ -5,7 +5,9 @@ for every even l the shell Gram matrix G_l[k1, k2] = sum_m c_k1lm conj(c_k2lm) i
 from the c2 slices by least squares against (1/4pi) P_l(cos alpha*), and the
 coefficients are the top 2l+1 eigenvectors of G_l scaled by the square roots of their
 eigenvalues (real SH basis, then real_to_comp).  The result matches the data up to one
-rotation in O(2l+1) per l — the ambiguity the annealer removes.  Small host-side
+rotation in O(2l+1) per l — the ambiguity the annealer removes; eigenvector signs are
+fixed by making each one's largest entry positive, and the whole structure is negated
+when the reference's negativityCheck exceeds 0.33.  Small host-side
 eigenproblems (K2 x K2 per l), run once per chain start; nothing here is on the
 per-proposal path.
 """
@@ -55,30 +57,48 @@ def twoPhotons(coeff: np.ndarray, LMAX: int, L: int, N: int, K2: int, dq: float,
     return c / np.sum(np.abs(c)) if normalize else c / (4 * math.pi)
 
 
-def _negativity(coeff: np.ndarray, LMAX: int, krange, n_theta: int = 2 * 25, n_phi: int = 4 * 25) -> float:
-    """negativityCheck (src/spherical_harmonics.jl:622-625): sum over shells of
-    sum|min(I, 0)| / sum|I| on an angular grid."""
-    from .structure import _sph_plm_table
-    xg, _ = np.polynomial.legendre.leggauss(n_theta)
-    phi = (np.arange(n_phi) + 0.5) * (2 * math.pi / n_phi)
-    P = _sph_plm_table(LMAX, xg)
+def _negativity(coeff: np.ndarray, LMAX: int, krange) -> float:
+    """negativityCheck (src/spherical_harmonics.jl:622-625): over the shells of krange, the
+    sum of sum|min(Re I, 0)| / sum|I| of the intensity surfaces on the backtransform grid
+    (2 LMAX x 2 LMAX, theta_j = pi (2j+1) / (4 LMAX), phi_k = 2 pi k / (2 LMAX))."""
+    from .postprocess import _grid
+    ks = [k - 1 for k in krange]
+    I = _grid(LMAX).surfaces(np.asarray(coeff)[ks])
     tot = 0.0
-    for k in krange:
-        I = np.zeros((n_theta, n_phi))
-        for l in range(LMAX):
-            for m in range(0, l + 1):
-                cl = coeff[k - 1, seanindex0(l, m, LMAX)]
-                f = 1.0 if m == 0 else 2.0
-                I += f * np.outer(P[l, m], (cl * np.exp(1j * m * phi)).real)
-        s = np.sum(np.abs(I))
-        tot += max(np.sum(np.abs(np.minimum(I, 0.0))) / s, 0.0) if s > 0 else 0.0
+    for Ik in I:
+        s = np.sum(np.abs(Ik))
+        tot += max(np.sum(np.abs(np.minimum(Ik, 0.0))) / s, 0.0) if s > 0 else 0.0
     return tot
 
 
-def retrieveSolution(c2: np.ndarray, L: int, LMAX: int, K2_range, qmax: float, lambda_: float = 0.0) -> np.ndarray:
-    """Intensity coefficients [K2_high, LMAX^2] consistent with c2 (src/correlations.jl:261-319)."""
+def _canonical(v: np.ndarray) -> np.ndarray:
+    """Eigenvector columns with the sign that makes each one's largest-magnitude entry
+    positive (the first such entry on ties); eigensolvers leave the sign free."""
+    v = v.copy()
+    for j in range(v.shape[1]):
+        i = int(np.argmax(np.abs(v[:, j])))
+        if v[i, j] < 0:
+            v[:, j] = -v[:, j]
+    return v
+
+
+def retrieveSolution(c2: np.ndarray, L: int, LMAX: int, K2_range, qmax: float, lambda_: float = 0.0,
+                     basis=None) -> np.ndarray:
+    """Intensity coefficients [K2_high, LMAX^2] consistent with c2 (src/correlations.jl:261-319).
+    With `basis` (any context) the fits and eigenproblems run on its device
+    (tp3_retrieve_solution)."""
     N = c2.shape[0]
     krange = list(K2_range)
+    if basis is not None:
+        from . import _lib
+        if krange != list(range(krange[0], krange[-1] + 1)):
+            raise ValueError("K2_range must be consecutive shells")
+        cc = np.ascontiguousarray(c2, dtype=np.float64)
+        out = np.zeros((krange[-1], LMAX * LMAX), dtype=np.complex128)
+        _lib.check(basis._lib.tp3_retrieve_solution(basis._ctx, cc.ctypes.data, N, cc.shape[1], L, LMAX, krange[0],
+                                                    krange[-1], float(qmax), float(lambda_), out.ctypes.data),
+                   basis._ctx)
+        return out
     K2, lo, hi = len(krange), min(krange), max(krange)
     if not L < K2 / 2:
         raise ValueError("retrieveSolution needs L < K2 / 2")
@@ -99,7 +119,7 @@ def retrieveSolution(c2: np.ndarray, L: int, LMAX: int, K2_range, qmax: float, l
                 if l <= upperL:
                     G[k2 - lo, k1 - lo] = G[k1 - lo, k2 - lo] = fac[l // 2]
         w, v = np.linalg.eigh(G)
-        w, v = w[K2 - (2 * l + 1):], v[:, K2 - (2 * l + 1):]
+        w, v = w[K2 - (2 * l + 1):], _canonical(v[:, K2 - (2 * l + 1):])
         m = np.diag(np.sqrt(np.maximum(0.0, w))) @ v.T          # (2l+1) x K2, real SH basis
         idx = [seanindex0(l, mm, LMAX) for mm in range(-l, l + 1)]
         for k in krange:
