@@ -18,7 +18,7 @@ export BasisTypeGB300, GB300_calculate_basis, GB300_chains_create, GB300_chains_
        GB300_energy_batch, GB300_set_mode, GB300_autotune, GB300_chains_log, GB300_chains_snapshot,
        GB300_chains_restore, GB300_chains_coeff, GB300_chains_destroy, GB300_chains_set_move,
        GB300_chains_enable_move_log, GB300_mlp_create, GB300_mlp_destroy, GB300_set_angular,
-       GB300_createSphericalHarmonicsStructure, GB300_fitStructures_random
+       GB300_createSphericalHarmonicsStructure, GB300_fitStructures_random, GB300_retrieveSolution
 
 const libtp3 = joinpath(@__DIR__, "..", "lib", "libtp3.so")
 
@@ -202,6 +202,20 @@ function GB300_fitStructures_random(basis::BasisTypeGB300, volume::SphericalHarm
                 rotated), basis.ctx)
     out = SphericalHarmonicsVolume([rotated[:, k] for k = 1:basis.K], volume.LMAX, basis.K, volume.rmax)
     return out, best[1], best[2], best[3], best[4]
+end
+
+"""retrieveSolution (src/correlations.jl:261-319) on the GPU (tp3_retrieve_solution): c2 is
+the reference's C2 array (N x K2 x K2, alpha first); returns the intensity volume."""
+function GB300_retrieveSolution(basis::BasisTypeGB300, c2::Array{Float64,3}, L::Int64, LMAX::Int64,
+                                K2_range::UnitRange{Int64}, qmax::Float64, lambda::Float64=0.0)
+    N, Kd = size(c2, 1), size(c2, 2)
+    c = permutedims(c2, [3, 2, 1])   # row-major [alpha][k2][k1] for the C side
+    out = zeros(Complex{Float64}, LMAX^2, last(K2_range))
+    check(ccall((:tp3_retrieve_solution, libtp3), Int32,
+                (Ptr{Void}, Ptr{Float64}, Int32, Int32, Int32, Int32, Int32, Int32, Float64, Float64,
+                 Ptr{Complex{Float64}}),
+                basis.ctx, c, N, Kd, L, LMAX, first(K2_range), last(K2_range), qmax, lambda, out), basis.ctx)
+    return SphericalHarmonicsVolume([out[:, k] for k = 1:last(K2_range)], LMAX, last(K2_range), qmax)
 end
 
 # ---- device-resident chains (rotate_all_at_once on the GPU) ---------------------------
